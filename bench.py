@@ -1,0 +1,404 @@
+#!/usr/bin/env python3
+"""Benchmark of the ray-marching path (one JSON line on rank 0).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload multiview|volume|tubes]
+
+Default workload: the batched multi-view configuration -- a 1024^3 u8
+Gaussian-blob volume in 64^3 bricks, 64 cameras on a seeded orbit sphere at
+resolutions drawn from {256^2, 512^2, 1024^2, 2048^2}, Volume shader, the
+9-knot transfer function, 1-voxel steps, density 1e-2.  One step renders all
+64 views.  Metric: Gsamples/s (brick trilinear samples per second); views/s
+is reported beside it.
+
+--impl ours       the GB300 path: one hy_render_device launch per view;
+                  `e2e` goes through hy_render with host buffers (host ->
+                  device view/params, device -> host RGBA per view).
+--impl reference  the reference's own CPU multi-thread backend for this path
+                  (restated in oracle/, the reference cannot be built here)
+                  on all host threads, on a bounded sample of the workload.
+
+Multi-GPU: every rank renders the full batch (replicas, weak scaling); the
+timed region is bracketed by a barrier and the max over ranks is reported.
+"""
+
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+BYTES_PER_SAMPLE = 8  # 2x2x2 u8 trilinear footprint per brick sample
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=["multiview", "volume", "tubes"], default="multiview")
+    ap.add_argument("--views", type=int, default=64)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-sample-rows", type=int, default=0,
+                    help="rows of the CPU-baseline sample (0 = auto)")
+    return ap.parse_args()
+
+
+def workload(args):
+    from hydrant_gb300 import workloads as wl
+
+    if args.workload == "volume":
+        return wl.volume_c0()
+    if args.workload == "tubes":
+        return wl.tubes_c1()
+    return wl.multiview_c3(nviews=args.views)
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic_per_sample():
+    """dram bytes per brick sample from the committed ncu summary, if any."""
+    p = ROOT / "profiles" / "render_kernel_multiview.txt"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.startswith("dram_bytes_per_sample:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+class Clocks:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in Path(self.path).read_text().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) >= 9:
+                rows.append(f)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def build_all():
+    import __graft_entry__
+
+    __graft_entry__.build()
+
+
+def cpu_sample(args, w, vox, nthreads, budget_rows=None):
+    """Time the oracle (the reference's CPU backend, restated) on a bounded sample."""
+    import numpy as np
+
+    import hydrant_gb300 as hy
+    from oracle import oracle as orc
+
+    ov = orc.OracleVolume(vox, w.block_size, w.padding)
+    # the largest view; a band of rows through its middle
+    view = max(w.views, key=lambda v: v.width * v.height)
+    cam = __import__("hydrant_gb300.workloads", fromlist=["x"]).make_camera(view.camera)
+    ocam = np.array(list(cam.position) + list(cam.target) + list(cam.up) + [cam.ctg_fovy_2],
+                    np.float32)
+    oview = orc.camera_view(ov, ocam)
+    p = hy.shader_params(**w.params)
+    op = orc.params_from(p)
+    if p.shader == hy._abi.SHADER_ISOSURFACE:
+        orc.iso_lighting(ov, ocam, op)
+    rows = budget_rows or args.cpu_sample_rows or max(8, view.height // 32)
+    y0 = view.height // 2 - rows // 2
+    return ov, (oview, op, view, y0, y0 + rows)
+
+
+def run_cpu_sample(ov, spec, tf, nthreads):
+    from oracle import oracle as orc
+
+    oview, op, view, y0, y1 = spec
+    t = time.perf_counter()
+    r = orc.render(ov, tf, op, oview, view.width, view.height, nthreads=nthreads, want_v=False,
+                   want_aux=False, rows=(y0, y1))
+    dt = time.perf_counter() - t
+    return r["samples"], dt
+
+
+def main_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    build_all()
+    w = workload(args)
+    vox = w.voxels()
+    nthreads = os.cpu_count() or 1
+    ov, spec = cpu_sample(args, w, vox, nthreads)
+    for _ in range(args.warmup):
+        run_cpu_sample(ov, spec, w.tf, nthreads)
+    tot_s, tot_t = 0, 0.0
+    for _ in range(args.steps):
+        s, dt = run_cpu_sample(ov, spec, w.tf, nthreads)
+        tot_s += s
+        tot_t += dt
+    value = tot_s / tot_t / 1e9
+    oview, op, view, y0, y1 = spec
+    sample = (f"rows {y0}..{y1} of the {view.width}x{view.height} view "
+              f"({(y1 - y0) * view.width} rays), {tot_s // max(1, args.steps)} samples per step")
+    out = {
+        "impl": "reference",
+        "metric": "Gsamples/s",
+        "value": value,
+        "unit": "Gsamples/s",
+        "n_gpus": args.gpus,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": tot_t / args.steps * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": w.name, "inputs": "host memory (CPU backend)"},
+        "cpu_baseline": {"value": value, "unit": "Gsamples/s", "cores": nthreads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "Gsamples/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+def main_ours(args):
+    import numpy as np
+    import torch
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    build_all()
+    import hydrant_gb300 as hy
+    from hydrant_gb300 import workloads as wl
+
+    w = workload(args)
+    t0 = time.perf_counter()
+    vox = w.voxels()
+    t_gen = time.perf_counter() - t0
+    ctx = hy.Context(local)
+    t0 = time.perf_counter()
+    vol = hy.Volume(ctx, vox, w.block_size, w.padding)
+    t_up = time.perf_counter() - t0
+    ctx.set_transfer_fn(w.tf)
+    info = vol.info
+
+    views, params, bufs = [], [], []
+    for v in w.views:
+        cam = wl.make_camera(v.camera)
+        p = hy.shader_params(**w.params)
+        if p.shader == hy._abi.SHADER_ISOSURFACE:
+            hy.iso_lighting(vol, cam, p)
+        views.append((hy.camera_view(vol, cam), v.width, v.height))
+        params.append(p)
+        bufs.append(torch.empty(v.height * v.width * 4, dtype=torch.uint8, device=f"cuda:{local}"))
+    npix = sum(W * H for _, W, H in views)
+
+    # brick samples per step (deterministic; counted once, outside the timed region)
+    samples = 0
+    for (view, W, H), p, b in zip(views, params, bufs):
+        pc = hy.shader_params(**w.params, count_samples=True)
+        if pc.shader == hy._abi.SHADER_ISOSURFACE:
+            pc = p
+            pc.count_samples = 1
+        hy.render_device(ctx, vol, pc, view, W, H, b.data_ptr())
+        samples += ctx.stats().samples
+        if pc is p:
+            p.count_samples = 0
+
+    stream = torch.cuda.ExternalStream(ctx.stream)
+
+    def step(evs=None):
+        for i, ((view, W, H), p, b) in enumerate(zip(views, params, bufs)):
+            if evs is not None:
+                evs[i][0].record(stream)
+            hy.render_device(ctx, vol, p, view, W, H, b.data_ptr())
+            if evs is not None:
+                evs[i][1].record(stream)
+
+    for _ in range(args.warmup):
+        step()
+    ctx.synchronize()
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    clocks = Clocks(local)
+    clocks.start()
+    launch_ev = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                  for _ in views] for _ in range(args.steps)]
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for k in range(args.steps):
+        step(launch_ev[k])
+    e1.record(stream)
+    ctx.synchronize()
+    torch.cuda.synchronize()
+    ck = clocks.stop()
+    t = e0.elapsed_time(e1) / 1e3
+    kernel_ms = [a.elapsed_time(b) for evs in launch_ev for a, b in evs]
+    if ws > 1:
+        tt = torch.tensor([t], device=f"cuda:{local}")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t = float(tt.item())
+        torch.distributed.barrier()
+
+    # e2e through the host-buffer entry point
+    for _ in range(max(1, args.warmup // 2)):
+        for (view, W, H), p in zip(views, params):
+            hy.render(ctx, vol, p, view, W, H)
+    if ws > 1:
+        torch.distributed.barrier()
+    te = time.perf_counter()
+    for _ in range(args.steps):
+        for (view, W, H), p in zip(views, params):
+            hy.render(ctx, vol, p, view, W, H)
+    t_e2e = time.perf_counter() - te
+    if ws > 1:
+        tt = torch.tensor([t_e2e], device=f"cuda:{local}")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_e2e = float(tt.item())
+
+    value = samples * ws * args.steps / t / 1e9
+    e2e = samples * ws * args.steps / t_e2e / 1e9
+    views_per_s = len(views) * ws * args.steps / t
+    hbm, peak_kind = measured_peaks()
+    # dominant kernel: the fused render kernel, one launch per view
+    mean_launch_s = (sum(kernel_ms) / len(kernel_ms)) / 1e3
+    bytes_per_launch = samples / len(views) * BYTES_PER_SAMPLE
+    achieved = bytes_per_launch / mean_launch_s / 1e9
+    tps = profile_traffic_per_sample()
+    out = None
+    if rank == 0:
+        cpu = None
+        if not args.no_cpu_baseline:
+            nth = os.cpu_count() or 1
+            ov, spec = cpu_sample(args, w, vox, nth)
+            s, dt = run_cpu_sample(ov, spec, w.tf, nth)
+            oview, op, view, y0, y1 = spec
+            cpu = {"value": s / dt / 1e9, "unit": "Gsamples/s", "cores": nth, "kind": "port",
+                   "sample": f"rows {y0}..{y1} of the {view.width}x{view.height} view, {s} samples, "
+                             f"{dt:.2f} s"}
+        out = {
+            "metric": "Gsamples/s",
+            "value": value,
+            "unit": "Gsamples/s",
+            "n_gpus": ws,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": t / args.steps * 1e3,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f32",
+            "data": "synthetic",
+            "config": {
+                "workload": w.name,
+                "volume": list(w.dim), "block_size": w.block_size, "padding": w.padding,
+                "views": len(views), "pixels_per_step": npix,
+                "samples_per_step": samples,
+                "path": "plain per-view (one fused launch per view)",
+                "l2": "inputs larger than L2 (brick pool %.2f GB)" % (info.pool_bytes / 1e9),
+            },
+            "views_per_s": views_per_s,
+            "e2e": {"value": e2e, "unit": "Gsamples/s",
+                    "h2d_bytes_per_step": len(views) * (ctypes.sizeof(hy._abi.HyView) + ctypes.sizeof(hy._abi.HyShaderParams)),
+                    "d2h_bytes_per_step": npix * 4},
+            "roofline": {
+                "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm, "peak_kind": peak_kind,
+                "traffic": (tps * samples / len(views)) if tps else None,
+                "note": "8 B/sample algorithmic footprint; the kernel is L1/issue bound",
+            },
+            "cpu_baseline": cpu,
+            "gpu_launches": args.steps * len(views),
+            "clocks": ck,
+            "setup_s": {"generate": t_gen, "upload_and_brick": t_up},
+        }
+        print(json.dumps(out), flush=True)
+    vol.close()
+    ctx.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        return main_reference(args)
+    return main_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

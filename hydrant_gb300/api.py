@@ -1,0 +1,262 @@
+"""Python handles over the C ABI: context, volume, camera, render calls."""
+
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import _abi
+from ._abi import (
+    HyCamera,
+    HyRenderStats,
+    HyShaderParams,
+    HyView,
+    HyVolumeDesc,
+    HyVolumeInfo,
+    check,
+    lib,
+)
+
+SHADERS = {"Volume": _abi.SHADER_VOLUME, "Blocks": _abi.SHADER_BLOCKS, "Isosurface": _abi.SHADER_ISOSURFACE}
+MODES = {
+    _abi.SHADER_VOLUME: {"Default": 0, "Partition": 1, "Paging": 2},
+    _abi.SHADER_BLOCKS: {"Volume": 0, "Solid": 1},
+    _abi.SHADER_ISOSURFACE: {"Color": 0, "Normal": 1, "Position": 2},
+}
+
+
+def _ptr(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class Context:
+    """One device, one stream (hy_ctx)."""
+
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        check(lib().hy_ctx_create(device, C.byref(h)))
+        self.handle = h
+        self.device = device
+
+    def close(self) -> None:
+        if self.handle:
+            lib().hy_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):  # pragma: no cover - interpreter shutdown order varies
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def check(self, rc: int) -> None:
+        check(rc, self.handle)
+
+    @property
+    def stream(self) -> int:
+        return int(lib().hy_ctx_stream(self.handle) or 0)
+
+    def synchronize(self) -> None:
+        self.check(lib().hy_ctx_synchronize(self.handle))
+
+    def set_transfer_fn(self, knots) -> None:
+        k = np.ascontiguousarray(np.asarray(knots, dtype=np.float32).reshape(-1, 4))
+        self.check(lib().hy_tf_set(self.handle, _ptr(k), k.shape[0]))
+
+    def stats(self) -> HyRenderStats:
+        s = HyRenderStats()
+        self.check(lib().hy_render_stats_get(self.handle, C.byref(s)))
+        return s
+
+
+class Volume:
+    """A bricked volume resident on the device (hy_volume)."""
+
+    def __init__(self, ctx: Context, voxels: np.ndarray, block_size: int, padding: int = 1):
+        if voxels.ndim != 3:
+            raise ValueError("voxels must be a (z, y, x) array")
+        if voxels.dtype == np.uint8:
+            dtype = _abi.DTYPE_U8
+        elif voxels.dtype == np.float32:
+            dtype = _abi.DTYPE_F32
+        else:
+            raise ValueError("voxels must be uint8 or float32")
+        self.ctx = ctx
+        nz, ny, nx = voxels.shape
+        desc = HyVolumeDesc((nx, ny, nz), block_size, padding, dtype)
+        h = C.c_void_p()
+        ctx.check(lib().hy_volume_create(ctx.handle, C.byref(desc), C.byref(h)))
+        self.handle = h
+        self.desc = desc
+        vox = np.ascontiguousarray(voxels)
+        ctx.check(lib().hy_volume_upload(self.handle, _ptr(vox)))
+
+    def close(self) -> None:
+        if self.handle:
+            lib().hy_volume_destroy(self.handle)
+            self.handle = None
+
+    @property
+    def info(self) -> HyVolumeInfo:
+        i = HyVolumeInfo()
+        self.ctx.check(lib().hy_volume_get_info(self.handle, C.byref(i)))
+        return i
+
+    def thumbnails(self):
+        i = self.info
+        n = i.nbricks
+        cheb = np.zeros(n, np.int32)
+        mean = np.zeros(n, np.float32)
+        self.ctx.check(lib().hy_volume_thumbnails(self.handle, _ptr(cheb), _ptr(mean)))
+        shape = (i.grid[2], i.grid[1], i.grid[0])
+        return cheb.reshape(shape), mean.reshape(shape)
+
+
+def camera_orbit(arm: Sequence[float], center=(0.0, 0.0, 0.0), fovy: float = 60.0) -> HyCamera:
+    cam = HyCamera()
+    a = (C.c_float * 3)(*arm)
+    c = (C.c_float * 3)(*center)
+    check(lib().hy_camera_orbit(C.cast(a, C.c_void_p), C.cast(c, C.c_void_p), fovy, C.byref(cam)))
+    return cam
+
+
+def camera_ptu(position, target=(0.0, 0.0, 0.0), up=(0.0, 1.0, 0.0), fovy: float = 60.0) -> HyCamera:
+    cam = HyCamera()
+    p, t, u = ((C.c_float * 3)(*v) for v in (position, target, up))
+    check(
+        lib().hy_camera_ptu(
+            C.cast(p, C.c_void_p), C.cast(t, C.c_void_p), C.cast(u, C.c_void_p), fovy, C.byref(cam)
+        )
+    )
+    return cam
+
+
+def camera_view(vol: Volume, cam: HyCamera) -> HyView:
+    v = HyView()
+    check(lib().hy_camera_view(vol.handle, C.byref(cam), C.byref(v)))
+    return v
+
+
+def shader_params(
+    shader="Volume",
+    mode=0,
+    sample_rate: float = 1.0,
+    max_steps: int = 4000000,
+    density: float = 1.0,
+    isovalue: float = 0.5,
+    surface_color=(1.0, 1.0, 1.0),
+    clear_color=(0.0, 0.0, 0.0),
+    rank: float = 0.0,
+    lowest_blkcnt: int = 0,
+    composite: bool = False,
+    srgb: bool = False,
+    count_samples: bool = False,
+) -> HyShaderParams:
+    p = HyShaderParams()
+    p.shader = SHADERS[shader] if isinstance(shader, str) else int(shader)
+    p.mode = MODES[p.shader][mode] if isinstance(mode, str) else int(mode)
+    p.sample_rate = sample_rate
+    p.max_steps = max_steps
+    p.density = density
+    p.isovalue = isovalue
+    p.surface_color = (C.c_float * 3)(*surface_color)
+    p.clear_color = (C.c_float * 3)(*clear_color)
+    p.rank = rank
+    p.lowest_blkcnt = lowest_blkcnt
+    p.composite = int(bool(composite))
+    p.srgb = int(bool(srgb))
+    p.count_samples = int(bool(count_samples))
+    return p
+
+
+def iso_lighting(vol: Volume, cam: HyCamera, params: HyShaderParams) -> HyShaderParams:
+    check(lib().hy_iso_lighting(vol.handle, C.byref(cam), C.byref(params)))
+    return params
+
+
+@dataclass
+class RenderResult:
+    rgba: np.ndarray
+    v: Optional[np.ndarray] = None
+    aux: Optional[np.ndarray] = None
+    samples: int = -1
+    ms: float = 0.0
+
+
+def render(
+    ctx: Context,
+    vol: Volume,
+    params: HyShaderParams,
+    view: HyView,
+    width: int,
+    height: int,
+    want_v: bool = False,
+    want_aux: bool = False,
+) -> RenderResult:
+    """hy_render: host buffers in and out."""
+    rgba = np.empty((height, width, 4), np.uint8)
+    v = np.empty((height, width, 4), np.float32) if want_v else None
+    aux = np.empty((height, width, 4), np.float32) if want_aux else None
+    ctx.check(
+        lib().hy_render(
+            ctx.handle, vol.handle, C.byref(params), C.byref(view), width, height,
+            _ptr(rgba), _ptr(v), _ptr(aux),
+        )
+    )
+    st = ctx.stats()
+    return RenderResult(rgba, v, aux, int(st.samples), float(st.ms))
+
+
+def render_device(ctx: Context, vol: Volume, params: HyShaderParams, view: HyView, width: int,
+                  height: int, rgba_ptr: int, v_ptr: int = 0, aux_ptr: int = 0) -> None:
+    """hy_render_device: device pointers, asynchronous on the context stream."""
+    ctx.check(
+        lib().hy_render_device(
+            ctx.handle, vol.handle, C.byref(params), C.byref(view), width, height,
+            C.c_void_p(rgba_ptr), C.c_void_p(v_ptr or None), C.c_void_p(aux_ptr or None),
+        )
+    )
+
+
+def shade_pass(ctx: Context, vol: Volume, params: HyShaderParams, pass_: int, view: Optional[HyView],
+               film_ptr: int, width: int, height: int, dst_ptr: int = 0, clear_rgb=None) -> None:
+    """hy_shade_pass: one reference-layout pass over a device film."""
+    clear = None
+    if clear_rgb is not None:
+        clear = (C.c_uint8 * 3)(*clear_rgb)
+    ctx.check(
+        lib().hy_shade_pass(
+            ctx.handle, vol.handle, C.byref(params), pass_,
+            C.byref(view) if view is not None else None,
+            C.c_void_p(film_ptr), width, height, C.c_void_p(dst_ptr or None),
+            C.cast(clear, C.c_void_p) if clear is not None else None,
+        )
+    )
+
+
+def synth_blobs_u8(seed: int, dim, nblobs: int, nthreads: int = 0) -> np.ndarray:
+    nx, ny, nz = dim
+    out = np.empty((nz, ny, nx), np.uint8)
+    d = (C.c_int32 * 3)(nx, ny, nz)
+    rc = lib().hy_synth_blobs_u8(seed, C.cast(d, C.c_void_p), nblobs, _ptr(out), nthreads)
+    check(rc)
+    return out
+
+
+def synth_blobs_f32(seed: int, dim, nblobs: int, nthreads: int = 0) -> np.ndarray:
+    nx, ny, nz = dim
+    out = np.empty((nz, ny, nx), np.float32)
+    d = (C.c_int32 * 3)(nx, ny, nz)
+    check(lib().hy_synth_blobs_f32(seed, C.cast(d, C.c_void_p), nblobs, _ptr(out), nthreads))
+    return out
+
+
+def synth_tubes_u8(seed: int, dim, ntubes: int, nthreads: int = 0) -> np.ndarray:
+    nx, ny, nz = dim
+    out = np.empty((nz, ny, nx), np.uint8)
+    d = (C.c_int32 * 3)(nx, ny, nz)
+    check(lib().hy_synth_tubes_u8(seed, C.cast(d, C.c_void_p), ntubes, _ptr(out), nthreads))
+    return out

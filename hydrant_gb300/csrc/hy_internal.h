@@ -1,0 +1,134 @@
+// hy_internal.h -- shared host/device declarations of libhydrant_gb300.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/hydrant_gb300.h"
+
+namespace hy {
+
+// One registry entry: the BlockSampler of block_paging.hpp:24-36 (a storage
+// slot plus its BlockSamplerMapping {k, b}, block_paging.hpp:11-22).
+struct __align__(16) RegEntry {
+    float k, bx, by, bz;   // mapped(x) = k * x + b
+    long long offset;      // byte offset of the slot in the brick pool
+    int pad_[2];
+};
+static_assert(sizeof(RegEntry) == 32, "RegEntry is two 16-byte loads");
+
+// Device view of a volume: the brick pool, the page table + chebyshev
+// thumbnail packed per brick as int2 {chebyshev, registry id or -1}, the
+// registry, and the mean thumbnail.
+struct DevVolume {
+    const unsigned char *pool;
+    const int2 *info;
+    const RegEntry *reg;
+    const float *mean;
+    int gx, gy, gz;
+    int P;      // padded brick edge
+    int dtype;  // HY_DTYPE_*
+    int pad_;
+};
+
+// Everything one shading launch reads; passed as a __grid_constant__ kernel
+// parameter (the reference copies its shader struct into a 16 KiB
+// __constant__ buffer per launch, cuda_shading.cu:5-10).
+struct ShadeArgs {
+    DevVolume vol;
+    // IShaderTypeErased (shader.hpp:16-22)
+    float bbox_max[3];
+    float step, du;
+    int max_steps;
+    // shader parameters
+    int shader, mode;
+    float density, isovalue;
+    float surface[3];
+    float rank;
+    int lowest_blkcnt;
+    float to_world[16];
+    float eye[3];
+    float light[3];
+    int composite, srgb, count;
+    unsigned char clear_u8[4];
+    // ViewArgs (shader.hpp:63-68)
+    float trans[16];
+    float ctg;
+    float ray_o[3];
+    int W, H;
+    const float4 *tf;
+    int ntf;
+    // outputs
+    uchar4 *rgba;
+    float4 *vout;
+    float4 *aux;
+    void *film;
+    void *dst;
+    unsigned long long *counter;
+};
+
+}  // namespace hy
+
+struct hy_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    float4 *tf_dev = nullptr;
+    int ntf = 0;
+    int tf_cap = 0;
+    unsigned long long *counter_dev = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    hy_render_stats stats{};
+    bool stats_pending = false;   // a launch whose events/counter are not read yet
+    int pend_count = 0;
+    int64_t pend_pixels = 0;
+    // device staging for the host-pointer entry points, grown on demand
+    void *stage = nullptr;
+    size_t stage_bytes = 0;
+};
+
+struct hy_volume {
+    hy_ctx *ctx = nullptr;
+    hy_volume_desc desc{};
+    int grid[3] = {0, 0, 0};
+    int nbricks = 0;
+    int P = 0;
+    int nonempty = 0;
+    int resident = 0;
+    size_t elem = 1;
+    size_t slot_stride = 0;
+    unsigned char *pool = nullptr;
+    size_t pool_bytes = 0;
+    int2 *info_dev = nullptr;
+    hy::RegEntry *reg_dev = nullptr;
+    float *mean_dev = nullptr;
+    std::vector<int> cheb;
+    std::vector<float> mean;
+    std::vector<int> reg_of_brick;
+    float k = 0.f, b = 0.f;   // uniform mapping of full-resolution bricks
+    float bbox_max[3] = {0, 0, 0};
+    float du = 0.f;
+    bool uploaded = false;
+};
+
+// error helpers (hy_api.cc)
+int hy_fail(hy_ctx *ctx, int code, const std::string &msg);
+int hy_cuda_fail(hy_ctx *ctx, cudaError_t e, const char *what);
+#define HY_CUDA(ctx, call)                                   \
+    do {                                                     \
+        cudaError_t e_ = (call);                             \
+        if (e_ != cudaSuccess) return hy_cuda_fail(ctx, e_, #call); \
+    } while (0)
+
+// staging buffer (hy_api.cc)
+int hy_stage(hy_ctx *ctx, size_t bytes, void **out);
+
+// launchers (hy_render.cu)
+int hy_launch_render(hy_ctx *ctx, const hy::ShadeArgs &args);
+int hy_launch_pass(hy_ctx *ctx, const hy::ShadeArgs &args, int pass);
+int hy_finish_stats(hy_ctx *ctx);
+int hy_fill_args(hy_ctx *ctx, const hy_volume *vol, const hy_shader_params *p, const hy_view *view,
+                 int W, int H, hy::ShadeArgs *a);

@@ -1,0 +1,461 @@
+// hy_render.cu -- shading kernels and the rendering entry points.
+//
+// Two ways in:
+//  * hy_render / hy_render_device: one fused kernel per view does ray
+//    generation, the march and the write_to quantisation; no film goes
+//    through HBM.  A warp shades an 8x4 ray tile, a 128-thread block a 16x8
+//    pixel tile; the transfer function and the u8 normalisation table sit in
+//    shared memory.
+//  * hy_shade_pass: the four passes of the reference (cuda_shading.cu:14-96)
+//    over a caller-owned film in the reference's pixel layout, so a renderer
+//    can swap its ShaderMeta.devices[Cuda] entry for this one.
+
+#include <algorithm>
+#include <cstring>
+
+#include "hy_shade.cuh"
+
+using namespace hy;
+using namespace hy::dev;
+
+namespace {
+
+constexpr int kTileW = 16, kTileH = 8, kThreads = 128;
+
+__device__ __forceinline__ void load_shared(const ShadeArgs &A, float4 *tf, float *lut) {
+    for (int i = threadIdx.x; i < A.ntf; i += blockDim.x) tf[i] = A.tf[i];
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) lut[i] = float(i) / 255.f;
+    __syncthreads();
+}
+
+__device__ __forceinline__ void tile_xy(int &x, int &y) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    x = blockIdx.x * kTileW + (warp & 1) * 8 + (lane & 7);
+    y = blockIdx.y * kTileH + (warp >> 1) * 4 + (lane >> 3);
+}
+
+__device__ __forceinline__ void count_samples(const ShadeArgs &A, long long samples) {
+    if (!A.count) return;
+    unsigned long long s = (unsigned long long)samples;
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0 && s) atomicAdd(A.counter, s);
+}
+
+// StdVec4Pixel::write_to (pixel_template.hpp:11-20), RGBA: alpha = saturate(v.a).
+__device__ __forceinline__ uchar4 quantise(const ShadeArgs &A, float4 v) {
+    if (v.w != 0.f)
+        return make_uchar4(saturate_u8(v.x), saturate_u8(v.y), saturate_u8(v.z), saturate_u8(v.w));
+    return make_uchar4(A.clear_u8[0], A.clear_u8[1], A.clear_u8[2], 0);
+}
+
+template <int SHADER, int PC, int DT, int COMPOSITE>
+__global__ void __launch_bounds__(kThreads) render_kernel(const __grid_constant__ ShadeArgs A) {
+    extern __shared__ float4 smem[];
+    float4 *tf = smem;
+    float *lut = reinterpret_cast<float *>(smem + A.ntf);
+    load_shared(A, tf, lut);
+    const Shared S{tf, A.ntf, float(A.ntf), lut};
+    int x, y;
+    tile_xy(x, y);
+    long long samples = 0;
+    if (x < A.W && y < A.H) {
+        float ox, oy, oz, dx, dy, dz;
+        gen_ray(A, x, y, ox, oy, oz, dx, dy, dz);
+        float4 v, aux;
+        if (COMPOSITE) {
+            samples = composite_ray<SHADER, PC, DT>(A, S, ox, oy, oz, dx, dy, dz, v, aux);
+        } else {
+            Px p;
+            samples = emit<SHADER, PC, DT>(p, A, S, ox, oy, oz, dx, dy, dz, 0.f, 0.f, 0.f,
+                                           A.bbox_max[0], A.bbox_max[1], A.bbox_max[2]);
+            v = make_float4(p.vx, p.vy, p.vz, p.vw);
+            if (SHADER == HY_SHADER_VOLUME)
+                aux = make_float4(p.e0, p.e1, p.e2, p.e3);
+            else if (SHADER == HY_SHADER_ISOSURFACE)
+                aux = make_float4(p.e3, 0.f, 0.f, 0.f);
+            else
+                aux = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        const size_t idx = size_t(y) * A.W + x;
+        A.rgba[idx] = quantise(A, v);
+        if (A.vout) A.vout[idx] = v;
+        if (A.aux) A.aux[idx] = aux;
+    }
+    count_samples(A, samples);
+}
+
+// ---- reference-layout film passes ------------------------------------------
+
+template <int SHADER>
+__device__ __forceinline__ size_t film_bytes() {
+    return SHADER == HY_SHADER_BLOCKS ? 48 : 64;
+}
+
+template <int SHADER>
+__device__ __forceinline__ void store_film(void *film, size_t idx, const Px &p) {
+    float4 *q = reinterpret_cast<float4 *>(static_cast<char *>(film) + idx * film_bytes<SHADER>());
+    q[0] = make_float4(p.ox, p.oy, p.oz, p.dx);
+    q[1] = make_float4(p.dy, p.dz, __int_as_float(p.nsteps), __int_as_float(p.step_size));
+    q[2] = make_float4(p.vx, p.vy, p.vz, p.vw);
+    if (SHADER != HY_SHADER_BLOCKS) q[3] = make_float4(p.e0, p.e1, p.e2, p.e3);
+}
+
+template <int SHADER>
+__device__ __forceinline__ Px load_film(const void *film, size_t idx) {
+    const float4 *q =
+        reinterpret_cast<const float4 *>(static_cast<const char *>(film) + idx * film_bytes<SHADER>());
+    Px p;
+    float4 a = q[0], b = q[1], c = q[2];
+    p.ox = a.x;
+    p.oy = a.y;
+    p.oz = a.z;
+    p.dx = a.w;
+    p.dy = b.x;
+    p.dz = b.y;
+    p.nsteps = __float_as_int(b.z);
+    p.step_size = __float_as_int(b.w);
+    p.vx = c.x;
+    p.vy = c.y;
+    p.vz = c.z;
+    p.vw = c.w;
+    if (SHADER != HY_SHADER_BLOCKS) {
+        float4 d = q[3];
+        p.e0 = d.x;
+        p.e1 = d.y;
+        p.e2 = d.z;
+        p.e3 = d.w;
+    } else {
+        p.e0 = p.e1 = p.e2 = p.e3 = 0.f;
+    }
+    return p;
+}
+
+// ray_emit_kernel_impl (cuda_shading.cu:14-35)
+template <int SHADER, int DT>
+__global__ void __launch_bounds__(kThreads) emit_pass_kernel(const __grid_constant__ ShadeArgs A) {
+    extern __shared__ float4 smem[];
+    float4 *tf = smem;
+    float *lut = reinterpret_cast<float *>(smem + A.ntf);
+    load_shared(A, tf, lut);
+    const Shared S{tf, A.ntf, float(A.ntf), lut};
+    int x, y;
+    tile_xy(x, y);
+    long long samples = 0;
+    if (x < A.W && y < A.H) {
+        float ox, oy, oz, dx, dy, dz;
+        gen_ray(A, x, y, ox, oy, oz, dx, dy, dz);
+        Px p;
+        samples = emit<SHADER, 0, DT>(p, A, S, ox, oy, oz, dx, dy, dz, 0.f, 0.f, 0.f,
+                                      A.bbox_max[0], A.bbox_max[1], A.bbox_max[2]);
+        store_film<SHADER>(A.film, size_t(y) * A.W + x, p);
+    }
+    count_samples(A, samples);
+}
+
+// ray_march_kernel_impl (cuda_shading.cu:41-54): resumes every pixel.
+template <int SHADER, int DT>
+__global__ void __launch_bounds__(kThreads) march_pass_kernel(const __grid_constant__ ShadeArgs A) {
+    extern __shared__ float4 smem[];
+    float4 *tf = smem;
+    float *lut = reinterpret_cast<float *>(smem + A.ntf);
+    load_shared(A, tf, lut);
+    const Shared S{tf, A.ntf, float(A.ntf), lut};
+    int x, y;
+    tile_xy(x, y);
+    long long samples = 0;
+    if (x < A.W && y < A.H) {
+        const size_t idx = size_t(y) * A.W + x;
+        Px p = load_film<SHADER>(A.film, idx);
+        samples = run_main<SHADER, 0, DT>(p, A, S);
+        store_film<SHADER>(A.film, idx, p);
+    }
+    count_samples(A, samples);
+}
+
+// pixel_kernel_impl (cuda_shading.cu:60-74): film -> uchar3 via write_to.
+template <int SHADER>
+__global__ void __launch_bounds__(kThreads) pixel_pass_kernel(const __grid_constant__ ShadeArgs A) {
+    int x, y;
+    tile_xy(x, y);
+    if (x >= A.W || y >= A.H) return;
+    const size_t idx = size_t(y) * A.W + x;
+    Px p = load_film<SHADER>(A.film, idx);
+    unsigned char *d = static_cast<unsigned char *>(A.dst) + idx * 3;
+    if (p.vw != 0.f) {
+        d[0] = saturate_u8(p.vx);
+        d[1] = saturate_u8(p.vy);
+        d[2] = saturate_u8(p.vz);
+    } else {
+        d[0] = A.clear_u8[0];
+        d[1] = A.clear_u8[1];
+        d[2] = A.clear_u8[2];
+    }
+}
+
+// fetch_kernel_impl (cuda_shading.cu:80-94): VolumeShaderKernel::fetch
+// (volume_shader.cu:23-30) and IsosurfaceShaderKernel::fetch
+// (isosurface_shader.cu:41-48).  The Blocks shader has no fetch.
+template <int SHADER>
+__global__ void __launch_bounds__(kThreads) fetch_pass_kernel(const __grid_constant__ ShadeArgs A) {
+    int x, y;
+    tile_xy(x, y);
+    if (x >= A.W || y >= A.H) return;
+    const size_t idx = size_t(y) * A.W + x;
+    Px p = load_film<SHADER>(A.film, idx);
+    if (SHADER == HY_SHADER_VOLUME) {
+        float4 *d = reinterpret_cast<float4 *>(static_cast<char *>(A.dst) + idx * 32);
+        d[0] = make_float4(p.e0, p.e1, p.e2, p.e3);
+        d[1] = make_float4(p.vx, p.vy, p.vz, p.vw);
+    } else if (SHADER == HY_SHADER_ISOSURFACE) {
+        unsigned char *d = static_cast<unsigned char *>(A.dst) + idx * 8;
+        d[0] = saturate_u8(p.vx);
+        d[1] = saturate_u8(p.vy);
+        d[2] = saturate_u8(p.vz);
+        d[3] = 0;
+        *reinterpret_cast<float *>(d + 4) = p.e3;
+    }
+}
+
+size_t smem_bytes(const ShadeArgs &a) { return size_t(a.ntf) * sizeof(float4) + 256 * sizeof(float); }
+
+dim3 grid_of(const ShadeArgs &a) {
+    return dim3((a.W + kTileW - 1) / kTileW, (a.H + kTileH - 1) / kTileH);
+}
+
+template <int SHADER, int PC, int DT>
+void launch_fused(const ShadeArgs &a, cudaStream_t s) {
+    if (a.composite)
+        render_kernel<SHADER, PC, DT, 1><<<grid_of(a), kThreads, smem_bytes(a), s>>>(a);
+    else
+        render_kernel<SHADER, PC, DT, 0><<<grid_of(a), kThreads, smem_bytes(a), s>>>(a);
+}
+
+template <int SHADER>
+int dispatch_fused(const ShadeArgs &a, cudaStream_t s) {
+    if (SHADER == HY_SHADER_BLOCKS) {
+        launch_fused<SHADER, 0, HY_DTYPE_U8>(a, s);
+        return HY_OK;
+    }
+    if (a.vol.dtype == HY_DTYPE_F32) {
+        launch_fused<SHADER, 0, HY_DTYPE_F32>(a, s);
+    } else if (a.vol.P == 66) {
+        launch_fused<SHADER, 66, HY_DTYPE_U8>(a, s);
+    } else if (a.vol.P == 130) {
+        launch_fused<SHADER, 130, HY_DTYPE_U8>(a, s);
+    } else {
+        launch_fused<SHADER, 0, HY_DTYPE_U8>(a, s);
+    }
+    return HY_OK;
+}
+
+template <int SHADER>
+void dispatch_pass(const ShadeArgs &a, int pass, cudaStream_t s) {
+    const dim3 g = grid_of(a);
+    const size_t sm = smem_bytes(a);
+    const bool f32 = a.vol.dtype == HY_DTYPE_F32;
+    switch (pass) {
+        case HY_PASS_RAY_EMIT:
+            if (f32)
+                emit_pass_kernel<SHADER, HY_DTYPE_F32><<<g, kThreads, sm, s>>>(a);
+            else
+                emit_pass_kernel<SHADER, HY_DTYPE_U8><<<g, kThreads, sm, s>>>(a);
+            break;
+        case HY_PASS_RAY_MARCH:
+            if (f32)
+                march_pass_kernel<SHADER, HY_DTYPE_F32><<<g, kThreads, sm, s>>>(a);
+            else
+                march_pass_kernel<SHADER, HY_DTYPE_U8><<<g, kThreads, sm, s>>>(a);
+            break;
+        case HY_PASS_PIXEL:
+            pixel_pass_kernel<SHADER><<<g, kThreads, 0, s>>>(a);
+            break;
+        default:
+            fetch_pass_kernel<SHADER><<<g, kThreads, 0, s>>>(a);
+            break;
+    }
+}
+
+unsigned char sat_host(float f) {
+    float x = f * 255.f;
+    x = (x < 0.f) ? 0.f : x;
+    x = (255.f < x) ? 255.f : x;
+    return (unsigned char)x;
+}
+
+}  // namespace
+
+int hy_fill_args(hy_ctx *ctx, const hy_volume *vol, const hy_shader_params *p, const hy_view *view,
+                 int W, int H, ShadeArgs *a) {
+    if (!vol || !p) return hy_fail(ctx, HY_ERR_INVALID, "render: null volume or params");
+    if (vol->ctx != ctx) return hy_fail(ctx, HY_ERR_INVALID, "render: volume of another context");
+    if (!vol->uploaded) return hy_fail(ctx, HY_ERR_STATE, "render: volume not uploaded");
+    if (W <= 0 || H <= 0 || (long long)W * H > (1ll << 31))
+        return hy_fail(ctx, HY_ERR_INVALID, "render: bad resolution");
+    if (p->shader < HY_SHADER_VOLUME || p->shader > HY_SHADER_ISOSURFACE)
+        return hy_fail(ctx, HY_ERR_INVALID, "render: unknown shader");
+    if (!(p->sample_rate > 0.f)) return hy_fail(ctx, HY_ERR_INVALID, "render: sample_rate <= 0");
+    if (p->shader == HY_SHADER_VOLUME && ctx->ntf <= 0)
+        return hy_fail(ctx, HY_ERR_STATE, "render: Volume shader needs a transfer function");
+    std::memset(a, 0, sizeof(*a));
+    a->vol = DevVolume{vol->pool, vol->info_dev, vol->reg_dev, vol->mean_dev, vol->grid[0],
+                       vol->grid[1], vol->grid[2], vol->P, vol->desc.dtype, 0};
+    for (int i = 0; i < 3; ++i) a->bbox_max[i] = vol->bbox_max[i];
+    a->du = vol->du;
+    a->step = vol->du / 4.f / p->sample_rate;  // basic_renderer.hpp:129
+    a->max_steps = p->max_steps;
+    a->shader = p->shader;
+    a->mode = p->mode;
+    a->density = p->density;
+    a->isovalue = p->isovalue;
+    for (int i = 0; i < 3; ++i) {
+        a->surface[i] = p->surface_color[i];
+        a->eye[i] = p->eye_pos[i];
+        a->light[i] = p->light_pos[i];
+        a->clear_u8[i] = sat_host(p->clear_color[i]);  // raycaster.hpp:211
+    }
+    a->rank = p->rank;
+    a->lowest_blkcnt = p->lowest_blkcnt;
+    std::memcpy(a->to_world, p->to_world, sizeof(a->to_world));
+    a->composite = p->composite;
+    a->srgb = p->srgb;
+    a->count = p->count_samples;
+    if (view) {
+        std::memcpy(a->trans, view->trans, sizeof(a->trans));
+        a->ctg = view->ctg_fovy_2;
+        for (int i = 0; i < 3; ++i) a->ray_o[i] = view->ray_o[i];
+    }
+    a->W = W;
+    a->H = H;
+    a->tf = ctx->tf_dev;
+    a->ntf = ctx->ntf;
+    a->counter = ctx->counter_dev;
+    return HY_OK;
+}
+
+int hy_launch_render(hy_ctx *ctx, const ShadeArgs &a) {
+    if (a.count) HY_CUDA(ctx, cudaMemsetAsync(ctx->counter_dev, 0, sizeof(unsigned long long), ctx->stream));
+    HY_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
+    switch (a.shader) {
+        case HY_SHADER_VOLUME:
+            dispatch_fused<HY_SHADER_VOLUME>(a, ctx->stream);
+            break;
+        case HY_SHADER_BLOCKS:
+            dispatch_fused<HY_SHADER_BLOCKS>(a, ctx->stream);
+            break;
+        default:
+            dispatch_fused<HY_SHADER_ISOSURFACE>(a, ctx->stream);
+            break;
+    }
+    HY_CUDA(ctx, cudaGetLastError());
+    HY_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
+    ctx->stats_pending = true;
+    ctx->pend_count = a.count;
+    ctx->pend_pixels = (int64_t)a.W * a.H;
+    return HY_OK;
+}
+
+int hy_launch_pass(hy_ctx *ctx, const ShadeArgs &a, int pass) {
+    if (a.count && pass <= HY_PASS_RAY_MARCH)
+        HY_CUDA(ctx, cudaMemsetAsync(ctx->counter_dev, 0, sizeof(unsigned long long), ctx->stream));
+    HY_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
+    switch (a.shader) {
+        case HY_SHADER_VOLUME:
+            dispatch_pass<HY_SHADER_VOLUME>(a, pass, ctx->stream);
+            break;
+        case HY_SHADER_BLOCKS:
+            dispatch_pass<HY_SHADER_BLOCKS>(a, pass, ctx->stream);
+            break;
+        default:
+            dispatch_pass<HY_SHADER_ISOSURFACE>(a, pass, ctx->stream);
+            break;
+    }
+    HY_CUDA(ctx, cudaGetLastError());
+    HY_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
+    ctx->stats_pending = true;
+    ctx->pend_count = a.count && pass <= HY_PASS_RAY_MARCH;
+    ctx->pend_pixels = (int64_t)a.W * a.H;
+    return HY_OK;
+}
+
+int hy_finish_stats(hy_ctx *ctx) {
+    HY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (!ctx->stats_pending) return HY_OK;
+    ctx->stats_pending = false;
+    float ms = 0.f;
+    HY_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+    ctx->stats.ms = ms;
+    ctx->stats.pixels = ctx->pend_pixels;
+    ctx->stats.samples = -1;
+    if (ctx->pend_count) {
+        unsigned long long n = 0;
+        HY_CUDA(ctx, cudaMemcpy(&n, ctx->counter_dev, sizeof(n), cudaMemcpyDeviceToHost));
+        ctx->stats.samples = (int64_t)n;
+    }
+    return HY_OK;
+}
+
+extern "C" int hy_render_device(hy_ctx *ctx, const hy_volume *vol, const hy_shader_params *p,
+                                const hy_view *view, int32_t W, int32_t H, uint8_t *rgba_dev,
+                                float *v_dev, float *aux_dev) {
+    if (!ctx) return HY_ERR_INVALID;
+    if (!view || !rgba_dev) return hy_fail(ctx, HY_ERR_INVALID, "render: null view or output");
+    ShadeArgs a;
+    int rc = hy_fill_args(ctx, vol, p, view, W, H, &a);
+    if (rc) return rc;
+    a.rgba = reinterpret_cast<uchar4 *>(rgba_dev);
+    a.vout = reinterpret_cast<float4 *>(v_dev);
+    a.aux = reinterpret_cast<float4 *>(aux_dev);
+    return hy_launch_render(ctx, a);
+}
+
+extern "C" int hy_render(hy_ctx *ctx, const hy_volume *vol, const hy_shader_params *p,
+                         const hy_view *view, int32_t W, int32_t H, uint8_t *rgba_out,
+                         float *v_out, float *aux_out) {
+    if (!ctx) return HY_ERR_INVALID;
+    if (!view || !rgba_out) return hy_fail(ctx, HY_ERR_INVALID, "render: null view or output");
+    ShadeArgs a;
+    int rc = hy_fill_args(ctx, vol, p, view, W, H, &a);
+    if (rc) return rc;
+    HY_CUDA(ctx, cudaSetDevice(ctx->device));
+    const size_t npx = size_t(W) * H;
+    const size_t rgba_b = (npx * 4 + 255) / 256 * 256, f4_b = npx * 16;
+    const size_t total = rgba_b + (v_out ? f4_b : 0) + (aux_out ? f4_b : 0);
+    void *stage = nullptr;
+    rc = hy_stage(ctx, total, &stage);
+    if (rc) return rc;
+    char *base = static_cast<char *>(stage);
+    a.rgba = reinterpret_cast<uchar4 *>(base);
+    size_t off = rgba_b;
+    if (v_out) {
+        a.vout = reinterpret_cast<float4 *>(base + off);
+        off += f4_b;
+    }
+    if (aux_out) a.aux = reinterpret_cast<float4 *>(base + off);
+    rc = hy_launch_render(ctx, a);
+    if (rc) return rc;
+    HY_CUDA(ctx, cudaMemcpyAsync(rgba_out, a.rgba, npx * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    if (v_out) HY_CUDA(ctx, cudaMemcpyAsync(v_out, a.vout, f4_b, cudaMemcpyDeviceToHost, ctx->stream));
+    if (aux_out)
+        HY_CUDA(ctx, cudaMemcpyAsync(aux_out, a.aux, f4_b, cudaMemcpyDeviceToHost, ctx->stream));
+    return hy_finish_stats(ctx);
+}
+
+extern "C" int hy_shade_pass(hy_ctx *ctx, const hy_volume *vol, const hy_shader_params *p,
+                             int32_t pass, const hy_view *view, void *film_dev, int32_t W,
+                             int32_t H, void *dst_dev, const uint8_t clear_rgb[3]) {
+    if (!ctx) return HY_ERR_INVALID;
+    if (pass < HY_PASS_RAY_EMIT || pass > HY_PASS_FETCH)
+        return hy_fail(ctx, HY_ERR_INVALID, "pass: unknown pass");
+    if (!film_dev) return hy_fail(ctx, HY_ERR_INVALID, "pass: null film");
+    if (pass == HY_PASS_RAY_EMIT && !view) return hy_fail(ctx, HY_ERR_INVALID, "pass: emit needs a view");
+    if (pass >= HY_PASS_PIXEL && !dst_dev) return hy_fail(ctx, HY_ERR_INVALID, "pass: null destination");
+    if (p && p->composite) return hy_fail(ctx, HY_ERR_UNSUPPORTED, "pass: composite is fused-only");
+    ShadeArgs a;
+    int rc = hy_fill_args(ctx, vol, p, view, W, H, &a);
+    if (rc) return rc;
+    a.film = film_dev;
+    a.dst = dst_dev;
+    if (clear_rgb)
+        for (int i = 0; i < 3; ++i) a.clear_u8[i] = clear_rgb[i];
+    return hy_launch_pass(ctx, a, pass);
+}

@@ -1,0 +1,625 @@
+// hy_shade.cuh -- per-ray device code of the ray-marching path.
+//
+// Translation units that include this file are compiled with -fmad=false,
+// -prec-div=true, -prec-sqrt=true, -ftz=false: each multiply and add rounds
+// separately and divisions and square roots are IEEE, so a ray marched here
+// takes the same steps and produces the same floats as the reference's CPU
+// backend (the __host__ __device__ shaders run through CpuSampler).  Where a
+// shortcut is taken it is exact; each one says why.
+//
+// Conventions: min(a,b) = (b < a) ? b : a and max(a,b) = (a < b) ? b : a
+// (the forms the reference's math library uses); sums run left to right.
+#pragma once
+
+#include "hy_internal.h"
+
+namespace hy {
+namespace dev {
+
+__device__ __forceinline__ float gmin(float a, float b) { return (b < a) ? b : a; }
+__device__ __forceinline__ float gmax(float a, float b) { return (a < b) ? b : a; }
+__device__ __forceinline__ int iclamp(int x, int lo, int hi) { return min(max(x, lo), hi); }
+__device__ __forceinline__ float fclamp(float x, float lo, float hi) { return gmin(gmax(x, lo), hi); }
+__device__ __forceinline__ float fsign(float x) { return float((0.f < x) - (x < 0.f)); }
+
+// IPixel + StdVec4Pixel + shader extras (shader.hpp:26-34,
+// pixel_template.hpp:11-20, volume_shader.hpp:11-15, isosurface_shader.hpp:11-15).
+// e0..e2: theta (Volume) or origin (Isosurface); e3: phi (Volume) or depth.
+struct Px {
+    float ox, oy, oz, dx, dy, dz;
+    int nsteps, step_size;
+    float vx, vy, vz, vw;
+    float e0, e1, e2, e3;
+};
+
+// Slab test (glm_math.hpp:58-72) with the reciprocal direction precomputed
+// (1/d is the same value on every call, so caching it is exact).
+__device__ __forceinline__ bool intersect(float ox, float oy, float oz, float rx, float ry,
+                                          float rz, float x0, float y0, float z0, float x1,
+                                          float y1, float z1, float &tnear, float &tfar) {
+    float tbx = rx * (x0 - ox), tby = ry * (y0 - oy), tbz = rz * (z0 - oz);
+    float ttx = rx * (x1 - ox), tty = ry * (y1 - oy), ttz = rz * (z1 - oz);
+    float nx = gmin(ttx, tbx), ny = gmin(tty, tby), nz = gmin(ttz, tbz);
+    float fx = gmax(ttx, tbx), fy = gmax(tty, tby), fz = gmax(ttz, tbz);
+    tnear = gmax(gmax(nx, ny), nz);
+    tfar = gmin(gmin(fx, fy), fz);
+    return tfar > tnear;
+}
+
+// Thumbnail / page-table lookup: non-normalised nearest texel with Clamp
+// (cpu_sampler.hpp:142-166, filter_none 72-76).  ip is integral and the
+// clamp bounds are integers, so floor() after the float clamp is the identity.
+__device__ __forceinline__ int thumb_index(const DevVolume &V, float fgx, float fgy, float fgz,
+                                           float ipx, float ipy, float ipz) {
+    int x = iclamp(int(fclamp(ipx, 0.f, fgx)), 0, V.gx - 1);
+    int y = iclamp(int(fclamp(ipy, 0.f, fgy)), 0, V.gy - 1);
+    int z = iclamp(int(fclamp(ipz, 0.f, fgz)), 0, V.gz - 1);
+    return (z * V.gy + y) * V.gx + x;
+}
+
+// skip_nblock_steps (volume_shader.cu:5-14, same in blocks/isosurface).
+__device__ __forceinline__ int skip_nblock_steps(Px &p, float rx, float ry, float rz, float ipx,
+                                                 float ipy, float ipz, int nblocks, float cdu,
+                                                 float step) {
+    float tnear, tfar;
+    intersect(p.ox, p.oy, p.oz, rx, ry, rz, ipx, ipy, ipz, ipx + 1.f, ipy + 1.f, ipz + 1.f, tnear,
+              tfar);
+    float di = ceilf((tfar + float(nblocks - 1) * cdu) / step);
+    p.ox = p.ox + (p.dx * di) * step;
+    p.oy = p.oy + (p.dy * di) * step;
+    p.oz = p.oz + (p.dz * di) * step;
+    return int(di);
+}
+
+// A resident brick: BlockSampler {storage, mapping} (block_paging.hpp:24-36).
+struct BrickRef {
+    const unsigned char *base;
+    float k, bx, by, bz;
+};
+
+__device__ __forceinline__ BrickRef load_brick(const DevVolume &V, int reg) {
+    const float4 *e = reinterpret_cast<const float4 *>(V.reg + reg);
+    float4 m = __ldg(e);
+    float4 o = __ldg(e + 1);
+    long long off = (long long)__float_as_uint(o.x) | ((long long)__float_as_uint(o.y) << 32);
+    return BrickRef{V.pool + off, m.x, m.y, m.z, m.w};
+}
+
+// Brick sample: BlockSampler::sample_3d -> CpuSampler with normalised
+// coordinates, Wrap and Linear (cpu_sampler.hpp:88-104, 126-129, 142-166).
+//  * Wrap is mod(f, P) = f - P*floor(f/P), which is f itself for 0 <= f < P;
+//    only the out-of-range case pays for the division.
+//  * With the lower corner i = floor(u) in [0, P-2] every neighbour index is
+//    unclamped and the upper one is i+1 -- or i when u is integral, where the
+//    weight a is 0 and x*(1-0) + y*0 == x for any finite y, so reading i+1
+//    gives the same float.  Offsets are then immediates when P is a
+//    compile-time constant.
+// U8 voxels are normalised with lut[u] = u / 255.f (texture_3d.hpp:78-86).
+template <int PC, int DT>
+__device__ __forceinline__ float sample_brick(const BrickRef &b, int Prt, float lx, float ly,
+                                              float lz, const float *__restrict__ lut) {
+    const int P = PC ? PC : Prt;
+    const float fd = float(P);
+    float mx = b.k * lx + b.bx, my = b.k * ly + b.by, mz = b.k * lz + b.bz;
+    float fx = fd * mx, fy = fd * my, fz = fd * mz;
+    if (!(fx >= 0.f && fx < fd)) fx = fx - fd * floorf(fx / fd);
+    if (!(fy >= 0.f && fy < fd)) fy = fy - fd * floorf(fy / fd);
+    if (!(fz >= 0.f && fz < fd)) fz = fz - fd * floorf(fz / fd);
+    float ux = fx - .5f, uy = fy - .5f, uz = fz - .5f;
+    float flx = floorf(ux), fly = floorf(uy), flz = floorf(uz);
+    float ax = ux - flx, ay = uy - fly, az = uz - flz;
+    int ix = int(flx), iy = int(fly), iz = int(flz);
+    float v000, v100, v010, v110, v001, v101, v011, v111;
+    if (ix >= 0 && ix <= P - 2 && iy >= 0 && iy <= P - 2 && iz >= 0 && iz <= P - 2) {
+        const long long base = ((long long)iz * P + iy) * P + ix;
+        if (DT == HY_DTYPE_U8) {
+            const unsigned char *q = b.base + base;
+            v000 = lut[__ldg(q)];
+            v100 = lut[__ldg(q + 1)];
+            v010 = lut[__ldg(q + P)];
+            v110 = lut[__ldg(q + P + 1)];
+            v001 = lut[__ldg(q + P * P)];
+            v101 = lut[__ldg(q + P * P + 1)];
+            v011 = lut[__ldg(q + P * P + P)];
+            v111 = lut[__ldg(q + P * P + P + 1)];
+        } else {
+            const float *q = reinterpret_cast<const float *>(b.base) + base;
+            v000 = __ldg(q);
+            v100 = __ldg(q + 1);
+            v010 = __ldg(q + P);
+            v110 = __ldg(q + P + 1);
+            v001 = __ldg(q + P * P);
+            v101 = __ldg(q + P * P + 1);
+            v011 = __ldg(q + P * P + P);
+            v111 = __ldg(q + P * P + P + 1);
+        }
+    } else {
+        int jx = iclamp(int(ceilf(ux)), 0, P - 1), jy = iclamp(int(ceilf(uy)), 0, P - 1),
+            jz = iclamp(int(ceilf(uz)), 0, P - 1);
+        ix = iclamp(ix, 0, P - 1);
+        iy = iclamp(iy, 0, P - 1);
+        iz = iclamp(iz, 0, P - 1);
+        const long long r00 = ((long long)iz * P + iy) * P, r10 = ((long long)iz * P + jy) * P,
+                        r01 = ((long long)jz * P + iy) * P, r11 = ((long long)jz * P + jy) * P;
+        if (DT == HY_DTYPE_U8) {
+            const unsigned char *q = b.base;
+            v000 = lut[__ldg(q + r00 + ix)];
+            v100 = lut[__ldg(q + r00 + jx)];
+            v010 = lut[__ldg(q + r10 + ix)];
+            v110 = lut[__ldg(q + r10 + jx)];
+            v001 = lut[__ldg(q + r01 + ix)];
+            v101 = lut[__ldg(q + r01 + jx)];
+            v011 = lut[__ldg(q + r11 + ix)];
+            v111 = lut[__ldg(q + r11 + jx)];
+        } else {
+            const float *q = reinterpret_cast<const float *>(b.base);
+            v000 = __ldg(q + r00 + ix);
+            v100 = __ldg(q + r00 + jx);
+            v010 = __ldg(q + r10 + ix);
+            v110 = __ldg(q + r10 + jx);
+            v001 = __ldg(q + r01 + ix);
+            v101 = __ldg(q + r01 + jx);
+            v011 = __ldg(q + r11 + ix);
+            v111 = __ldg(q + r11 + jx);
+        }
+    }
+    const float bx = 1.f - ax, by = 1.f - ay, bz = 1.f - az;
+    float x0_0 = v000 * bx + v100 * ax;
+    float x1_0 = v010 * bx + v110 * ax;
+    float x0_1 = v001 * bx + v101 * ax;
+    float x1_1 = v011 * bx + v111 * ax;
+    float y0 = x0_0 * by + x1_0 * ay;
+    float y1 = x0_1 * by + x1_1 * ay;
+    return y0 * bz + y1 * az;
+}
+
+// TransferFn lookup: 1-D, normalised, Border, Linear (transfer_fn.hpp:16-23,
+// cpu_sampler.hpp:117-124, 137-140), knots in shared memory.
+__device__ __forceinline__ float4 sample_tf(const float4 *__restrict__ tf, int n, float fn,
+                                            float s) {
+    float fx = fn * s;
+    if (!(0.f <= fx && fx <= fn)) return make_float4(0.f, 0.f, 0.f, 0.f);
+    float u = fx - .5f;
+    float flr = floorf(u);
+    float a = u - flr;
+    int i = iclamp(int(flr), 0, n - 1);
+    int j = iclamp(int(ceilf(u)), 0, n - 1);
+    float4 x = tf[i], y = tf[j];
+    float b = 1.f - a;
+    return make_float4(x.x * b + y.x * a, x.y * b + y.y * a, x.z * b + y.z * a, x.w * b + y.w * a);
+}
+
+struct Shared {
+    const float4 *tf;
+    int ntf;
+    float fntf;
+    const float *lut;
+};
+
+// v.w > 0.93 and v.w > 0.85 are double comparisons in the reference
+// (volume_shader.cu:71-75).  Both constants round up to float, so for a
+// float x: x > 0.93 (double)  <=>  x >= 0.93f, and likewise for 0.85.
+#define HY_T93 0.93f
+#define HY_T85 0.85f
+
+// VolumeShaderKernel::main (volume_shader.cu:32-81).  The brick lookup is
+// cached while floor(o) stays in the same brick (same texel, same result).
+template <int PC, int DT>
+__device__ __forceinline__ long long volume_main(Px &p, const ShadeArgs &A, const Shared &S) {
+    const DevVolume &V = A.vol;
+    long long samples = 0;
+    const float cdu = 1.f / gmax(gmax(fabsf(p.dx), fabsf(p.dy)), fabsf(p.dz));
+    const float rx = 1.f / p.dx, ry = 1.f / p.dy, rz = 1.f / p.dz;
+    const float fgx = float(V.gx), fgy = float(V.gy), fgz = float(V.gz);
+    int cur = -1, cd = 0, pg = -1;
+    BrickRef br{};
+    int cur_ss = 0;
+    float sx = 0.f, sy = 0.f, sz = 0.f;
+    while (p.nsteps > 0) {
+        float ipx = floorf(p.ox), ipy = floorf(p.oy), ipz = floorf(p.oz);
+        int bid = thumb_index(V, fgx, fgy, fgz, ipx, ipy, ipz);
+        if (bid != cur) {
+            cur = bid;
+            int2 in = __ldg(&V.info[bid]);
+            cd = in.x;
+            pg = in.y;
+            if (cd == 0 && pg >= 0) br = load_brick(V, pg);
+        }
+        if (cd) {
+            p.nsteps -= skip_nblock_steps(p, rx, ry, rz, ipx, ipy, ipz, cd, cdu,
+                                          A.step * float(p.step_size));
+        } else {
+            if (pg == -1) break;
+            float s = sample_brick<PC, DT>(br, V.P, p.ox - ipx, p.oy - ipy, p.oz - ipz, S.lut);
+            ++samples;
+            float4 ub = sample_tf(S.tf, S.ntf, S.fntf, s);
+            if (A.mode == HY_VOLUME_PARTITION) {
+                float r = A.rank;
+                float mr = 1.f * (1.f - r) + 0.f * r, mg = 0.f * (1.f - r) + 0.f * r,
+                      mb = 0.f * (1.f - r) + 1.f * r;
+                float len = sqrtf(ub.x * ub.x + ub.y * ub.y + ub.z * ub.z);
+                ub = make_float4(mr * len, mg * len, mb * len, ub.w);
+            } else if (A.mode == HY_VOLUME_PAGING) {
+                ub = pg >= A.lowest_blkcnt ? make_float4(0.f, 1.f, 0.f, ub.w)
+                                           : make_float4(1.f, 0.f, 0.f, ub.w);
+            }
+            ub.w = ub.w * A.density;  // opacity scale; exact identity at 1
+            const float w = ub.w;
+            ub.x = ub.x * w;
+            ub.y = ub.y * w;
+            ub.z = ub.z * w;
+            p.e0 = p.e0 + ub.x * p.e3;
+            p.e1 = p.e1 + ub.y * p.e3;
+            p.e2 = p.e2 + ub.z * p.e3;
+            p.e3 = p.e3 * (1.f - ub.w);
+            const float t = 1.f - p.vw;
+            p.vx = p.vx + ub.x * t;
+            p.vy = p.vy + ub.y * t;
+            p.vz = p.vz + ub.z * t;
+            p.vw = p.vw + ub.w * t;
+            if (p.vw >= HY_T93) {
+                p.step_size = 16;
+            } else if (p.vw >= HY_T85) {
+                p.step_size = 4;
+            }
+        }
+        if (p.step_size != cur_ss) {  // (d * step) * step_size, recomputed only when it changes
+            cur_ss = p.step_size;
+            const float fs = float(cur_ss);
+            sx = (p.dx * A.step) * fs;
+            sy = (p.dy * A.step) * fs;
+            sz = (p.dz * A.step) * fs;
+        }
+        p.ox = p.ox + sx;
+        p.oy = p.oy + sy;
+        p.oz = p.oz + sz;
+        p.nsteps -= p.step_size;
+    }
+    return samples;
+}
+
+// VisBlocksShaderKernel::main (blocks_shader.cu:16-50).
+__device__ __forceinline__ long long blocks_main(Px &p, const ShadeArgs &A) {
+    const DevVolume &V = A.vol;
+    long long samples = 0;
+    const float cdu = 1.f / gmax(gmax(fabsf(p.dx), fabsf(p.dy)), fabsf(p.dz));
+    const float rx = 1.f / p.dx, ry = 1.f / p.dy, rz = 1.f / p.dz;
+    const float fgx = float(V.gx), fgy = float(V.gy), fgz = float(V.gz);
+    const float opacity_threshold = 0.95f;
+    const float hx = A.bbox_max[0] - 1.f, hy = A.bbox_max[1] - 1.f, hz = A.bbox_max[2] - 1.f;
+    const float ex = A.bbox_max[0] - 0.f, ey = A.bbox_max[1] - 0.f, ez = A.bbox_max[2] - 0.f;
+    const float sx = p.dx * A.step, sy = p.dy * A.step, sz = p.dz * A.step;
+    while (p.nsteps > 0) {
+        float ipx = floorf(p.ox), ipy = floorf(p.oy), ipz = floorf(p.oz);
+        int bid = thumb_index(V, fgx, fgy, fgz, ipx, ipy, ipz);
+        int cd = __ldg(&V.info[bid].x);
+        if (cd) {
+            p.nsteps -= skip_nblock_steps(p, rx, ry, rz, ipx, ipy, ipz, cd, cdu, A.step);
+        } else {
+            float rpx = fclamp(ipx, 0.f, hx) / ex, rpy = fclamp(ipy, 0.f, hy) / ey,
+                  rpz = fclamp(ipz, 0.f, hz) / ez;
+            ++samples;
+            if (A.mode == HY_BLOCKS_VOLUME) {
+                const float mean = __ldg(&V.mean[bid]);
+                const float cx = rpx * A.density * mean, cy = rpy * A.density * mean,
+                            cz = rpz * A.density * mean, cw = 1.f * A.density * mean;
+                const float t = 1.f - p.vw;
+                p.vx = p.vx + cx * t;
+                p.vy = p.vy + cy * t;
+                p.vz = p.vz + cz * t;
+                p.vw = p.vw + cw * t;
+                if (p.vw > opacity_threshold) {
+                    p.nsteps = 0;
+                    break;
+                }
+            } else {
+                p.vx = rpx;
+                p.vy = rpy;
+                p.vz = rpz;
+                p.vw = 1.f;
+                p.nsteps = 0;
+                break;
+            }
+        }
+        p.ox = p.ox + sx;
+        p.oy = p.oy + sy;
+        p.oz = p.oz + sz;
+        p.nsteps -= 1;
+    }
+    return samples;
+}
+
+// linear_to_srgb of the isosurface shader: double-precision constants
+// (isosurface_shader.cu:25-32).
+__device__ __forceinline__ float iso_linear_to_srgb(float linear) {
+    double l = double(linear);
+    if (l <= 0.0031308) return float(12.92 * l);
+    return float((1.0 + 0.055) * pow(l, 1.0 / 2.4) - 0.055);
+}
+
+__device__ __forceinline__ void mat_vec4(const float *m, float x, float y, float z, float w,
+                                         float &ox, float &oy, float &oz) {
+    ox = m[0] * x + m[4] * y + m[8] * z + m[12] * w;
+    oy = m[1] * x + m[5] * y + m[9] * z + m[13] * w;
+    oz = m[2] * x + m[6] * y + m[10] * z + m[14] * w;
+}
+
+__device__ __forceinline__ void normalize3(float &x, float &y, float &z) {
+    const float r = 1.f / sqrtf(x * x + y * y + z * z);
+    x = x * r;
+    y = y * r;
+    z = z * r;
+}
+
+// IsosurfaceShaderKernel::main (isosurface_shader.cu:50-125).  prev_value
+// stays 0, as in the reference (it is never updated there).
+template <int PC, int DT>
+__device__ __forceinline__ long long iso_main(Px &p, const ShadeArgs &A, const Shared &S) {
+    const DevVolume &V = A.vol;
+    long long samples = 0;
+    const float cdu = 1.f / gmax(gmax(fabsf(p.dx), fabsf(p.dy)), fabsf(p.dz));
+    const float rx = 1.f / p.dx, ry = 1.f / p.dy, rz = 1.f / p.dz;
+    const float fgx = float(V.gx), fgy = float(V.gy), fgz = float(V.gz);
+    const float prev_value = 0.0f;
+    const float iso = A.isovalue;
+    const float prev_sign = fsign(prev_value - iso);
+    const float sx = p.dx * A.step, sy = p.dy * A.step, sz = p.dz * A.step;
+    int cur = -1, cd = 0, pg = -1;
+    BrickRef br{};
+    while (p.nsteps > 0) {
+        float ipx = floorf(p.ox), ipy = floorf(p.oy), ipz = floorf(p.oz);
+        int bid = thumb_index(V, fgx, fgy, fgz, ipx, ipy, ipz);
+        if (bid != cur) {
+            cur = bid;
+            int2 in = __ldg(&V.info[bid]);
+            cd = in.x;
+            pg = in.y;
+            if (cd == 0 && pg >= 0) br = load_brick(V, pg);
+        }
+        if (cd) {
+            p.nsteps -= skip_nblock_steps(p, rx, ry, rz, ipx, ipy, ipz, cd, cdu, A.step);
+        } else {
+            if (pg == -1) break;  // page fault: resume in the next march pass
+            float value = sample_brick<PC, DT>(br, V.P, p.ox - ipx, p.oy - ipy, p.oz - ipz, S.lut);
+            ++samples;
+            if (fsign(value - iso) != prev_sign) {
+                const float dt = A.step;
+                p.vx = A.surface[0];
+                p.vy = A.surface[1];
+                p.vz = A.surface[2];
+                p.vw = 1.f;
+                const float a = (iso - prev_value) / (value - prev_value);
+                const float qx = p.ox - dt * p.dx, qy = p.oy - dt * p.dy, qz = p.oz - dt * p.dz;
+                const float ia = 1.f - a;
+                const float ipx2 = ia * qx + a * p.ox, ipy2 = ia * qy + a * p.oy,
+                            ipz2 = ia * qz + a * p.oz;
+                // central difference in brick-local coordinates, dt = du * 2
+                const float lx = ipx2 - ipx, ly = ipy2 - ipy, lz = ipz2 - ipz;
+                const float g = A.du * 2.f;
+                float nnx = sample_brick<0, DT>(br, V.P, lx - g, ly - 0.f, lz - 0.f, S.lut) -
+                            sample_brick<0, DT>(br, V.P, lx + g, ly + 0.f, lz + 0.f, S.lut);
+                float nny = sample_brick<0, DT>(br, V.P, lx - 0.f, ly - g, lz - 0.f, S.lut) -
+                            sample_brick<0, DT>(br, V.P, lx + 0.f, ly + g, lz + 0.f, S.lut);
+                float nnz = sample_brick<0, DT>(br, V.P, lx - 0.f, ly - 0.f, lz - g, S.lut) -
+                            sample_brick<0, DT>(br, V.P, lx + 0.f, ly + 0.f, lz + g, S.lut);
+                samples += 6;
+                float wx, wy, wz, nx, ny, nz;
+                mat_vec4(A.to_world, ipx2, ipy2, ipz2, 1.f, wx, wy, wz);
+                mat_vec4(A.to_world, nnx, nny, nnz, 0.f, nx, ny, nz);
+                normalize3(nx, ny, nz);
+                float lx2 = A.light[0] - wx, ly2 = A.light[1] - wy, lz2 = A.light[2] - wz;
+                normalize3(lx2, ly2, lz2);
+                float hx = lx2 - wx, hy = ly2 - wy, hz = lz2 - wz;
+                normalize3(hx, hy, hz);
+                const float ambient = 0.2f;
+                const float diffuse = .6f * fclamp(lx2 * nx + ly2 * ny + lz2 * nz, 0.f, 1.f);
+                const float specular =
+                    .2f * powf(fclamp(hx * nx + hy * ny + hz * nz, 0.f, 1.f), 100.f);
+                const float ex = wx - A.eye[0], ey = wy - A.eye[1], ez = wz - A.eye[2];
+                const float distance = sqrtf(ex * ex + ey * ey + ez * ez) / 2.f;
+                if (A.mode == HY_ISO_COLOR) {
+                    const float f = ambient + (diffuse + specular) / distance;
+                    p.vx = iso_linear_to_srgb(p.vx * f);
+                    p.vy = iso_linear_to_srgb(p.vy * f);
+                    p.vz = iso_linear_to_srgb(p.vz * f);
+                    p.vw = p.vw * f;
+                } else if (A.mode == HY_ISO_POSITION) {
+                    p.vx = ipx2 / A.bbox_max[0];
+                    p.vy = ipy2 / A.bbox_max[1];
+                    p.vz = ipz2 / A.bbox_max[2];
+                    p.vw = 1.f;
+                } else {
+                    p.vx = nx;
+                    p.vy = ny;
+                    p.vz = nz;
+                    p.vw = 1.f;
+                }
+                const float ddx = p.e0 - p.ox, ddy = p.e1 - p.oy, ddz = p.e2 - p.oz;
+                p.e3 = sqrtf(ddx * ddx + ddy * ddy + ddz * ddz);
+                p.nsteps = 0;
+                break;
+            }
+        }
+        p.ox = p.ox + sx;
+        p.oy = p.oy + sy;
+        p.oz = p.oz + sz;
+        p.nsteps -= 1;
+    }
+    return samples;
+}
+
+template <int SHADER, int PC, int DT>
+__device__ __forceinline__ long long run_main(Px &p, const ShadeArgs &A, const Shared &S) {
+    if (SHADER == HY_SHADER_VOLUME) return volume_main<PC, DT>(p, A, S);
+    if (SHADER == HY_SHADER_BLOCKS) return blocks_main(p, A);
+    return iso_main<PC, DT>(p, A, S);
+}
+
+// Ray generation (cuda_shading.cu:24-29 == cpu_shading.cc:14-21).
+__device__ __forceinline__ void gen_ray(const ShadeArgs &A, int x, int y, float &ox, float &oy,
+                                        float &oz, float &dx, float &dy, float &dz) {
+    const float ccx = float(A.W) / 2.f, ccy = float(A.H) / 2.f;
+    const float fh = float(A.H);
+    const float ux = (float(x) - ccx) * 2.f / fh;
+    const float uy = (float(y) - ccy) * 2.f / fh;
+    float px, py, pz;
+    mat_vec4(A.trans, ux, -uy, -A.ctg, 1.f, px, py, pz);
+    ox = A.ray_o[0];
+    oy = A.ray_o[1];
+    oz = A.ray_o[2];
+    dx = px - ox;
+    dy = py - oy;
+    dz = pz - oz;
+    normalize3(dx, dy, dz);
+}
+
+// ray_emit_shader_impl (shader.hpp:113-137) against box [b0, b1]; init() of
+// the Volume (volume_shader.cu:16-21) and Isosurface (isosurface_shader.cu:34-39)
+// shaders.
+template <int SHADER, int PC, int DT>
+__device__ __forceinline__ long long emit(Px &p, const ShadeArgs &A, const Shared &S, float ox,
+                                          float oy, float oz, float dx, float dy, float dz,
+                                          float x0, float y0, float z0, float x1, float y1,
+                                          float z1) {
+    p.ox = ox;
+    p.oy = oy;
+    p.oz = oz;
+    p.dx = dx;
+    p.dy = dy;
+    p.dz = dz;
+    p.vx = p.vy = p.vz = p.vw = 0.f;
+    if (SHADER == HY_SHADER_VOLUME) {
+        p.e0 = p.e1 = p.e2 = 0.f;
+        p.e3 = 1.f;
+    } else if (SHADER == HY_SHADER_ISOSURFACE) {
+        p.e0 = ox;
+        p.e1 = oy;
+        p.e2 = oz;
+        p.e3 = __int_as_float(0x7f800000);  // INFINITY
+    } else {
+        p.e0 = p.e1 = p.e2 = p.e3 = 0.f;
+    }
+    float tnear, tfar;
+    if (intersect(ox, oy, oz, 1.f / dx, 1.f / dy, 1.f / dz, x0, y0, z0, x1, y1, z1, tnear, tfar)) {
+        if (tnear < 0) tnear = 0;
+        if (tfar < 0) tfar = 0;
+        p.ox = p.ox + p.dx * tnear;
+        p.oy = p.oy + p.dy * tnear;
+        p.oz = p.oz + p.dz * tnear;
+        p.nsteps = min(A.max_steps, int((tfar - tnear) / A.step));
+        p.step_size = 1;
+        return run_main<SHADER, PC, DT>(p, A, S);
+    }
+    p.nsteps = 0;
+    p.step_size = 1;
+    return 0;
+}
+
+__device__ __forceinline__ unsigned char saturate_u8(float f) {
+    return (unsigned char)fclamp(f * 255.f, 0.f, 255.f);  // glm_math.hpp:75-81 (truncating)
+}
+
+__device__ __forceinline__ float vol_linear_to_srgb(float x) {  // volume.cc:175-181
+    if (x <= 0.0031308f) return 12.92f * x;
+    return 1.055f * powf(x, 1.f / 2.4f) - 0.055f;
+}
+
+// Per-brick sort-last for one ray: 3-D DDA over the brick grid inside the
+// volume box; each non-empty brick is an emit against its own box (the
+// per-partition bbox of dbuf_renderer.hpp:38-40) and the partials are
+// composited front to back with volume.cc:267-280 (Volume),
+// isosurface.cc:272-290 (depth-min, Isosurface) or the over operator (Blocks).
+template <int SHADER, int PC, int DT>
+__device__ __forceinline__ long long composite_ray(const ShadeArgs &A, const Shared &S, float ox,
+                                                   float oy, float oz, float dx, float dy,
+                                                   float dz, float4 &acc, float4 &aux) {
+    long long samples = 0;
+    acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    aux = make_float4(0.f, 0.f, 0.f, 1.f);
+    float acc_depth = __int_as_float(0x7f800000);
+    if (SHADER == HY_SHADER_ISOSURFACE) aux.w = 0.f;
+    float tnear, tfar;
+    if (SHADER == HY_SHADER_BLOCKS) aux.w = 0.f;
+    if (!intersect(ox, oy, oz, 1.f / dx, 1.f / dy, 1.f / dz, 0.f, 0.f, 0.f, A.bbox_max[0],
+                   A.bbox_max[1], A.bbox_max[2], tnear, tfar)) {
+        if (SHADER == HY_SHADER_ISOSURFACE) aux.x = acc_depth;
+        return 0;
+    }
+    const float t0 = tnear < 0.f ? 0.f : tnear;
+    const float t1 = tfar;
+    if (!(t1 > t0)) {
+        if (SHADER == HY_SHADER_ISOSURFACE) aux.x = acc_depth;
+        return 0;
+    }
+    const DevVolume &V = A.vol;
+    const int g[3] = {V.gx, V.gy, V.gz};
+    const float o[3] = {ox, oy, oz}, d[3] = {dx, dy, dz};
+    int cell[3];
+    int stp[3];
+    float tmax[3], tdelta[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float pa = o[a] + d[a] * t0;
+        cell[a] = iclamp(int(floorf(pa)), 0, g[a] - 1);
+        stp[a] = d[a] > 0.f ? 1 : (d[a] < 0.f ? -1 : 0);
+        if (stp[a] != 0) {
+            const float nb = float(stp[a] > 0 ? cell[a] + 1 : cell[a]);
+            tmax[a] = (nb - o[a]) / d[a];
+            tdelta[a] = 1.f / fabsf(d[a]);
+        } else {
+            tmax[a] = __int_as_float(0x7f800000);
+            tdelta[a] = __int_as_float(0x7f800000);
+        }
+    }
+    bool first = true;
+    const int limit = g[0] + g[1] + g[2] + 3;
+    for (int it = 0; it < limit; ++it) {
+        const int bid = (cell[2] * g[1] + cell[1]) * g[0] + cell[0];
+        if (__ldg(&V.info[bid].x) == 0) {
+            const float bx = float(cell[0]), by = float(cell[1]), bz = float(cell[2]);
+            Px p;
+            samples += emit<SHADER, PC, DT>(p, A, S, ox, oy, oz, dx, dy, dz, bx, by, bz, bx + 1.f,
+                                            by + 1.f, bz + 1.f);
+            if (SHADER == HY_SHADER_VOLUME) {
+                if (first) {
+                    acc = make_float4(p.vx, p.vy, p.vz, p.vw);
+                    aux = make_float4(p.e0, p.e1, p.e2, p.e3);
+                } else {
+                    const float nx = acc.x + p.vx - acc.w * p.e0;
+                    const float ny = acc.y + p.vy - acc.w * p.e1;
+                    const float nz = acc.z + p.vz - acc.w * p.e2;
+                    const float na = p.e3 * acc.w + p.vw;
+                    acc = make_float4(nx, ny, nz, na);
+                }
+            } else if (SHADER == HY_SHADER_ISOSURFACE) {
+                if (first || p.e3 < acc_depth) {
+                    acc = make_float4(p.vx, p.vy, p.vz, p.vw);
+                    acc_depth = p.e3;
+                }
+            } else {
+                const float t = 1.f - acc.w;
+                acc = make_float4(acc.x + p.vx * t, acc.y + p.vy * t, acc.z + p.vz * t,
+                                  acc.w + p.vw * t);
+            }
+            first = false;
+        }
+        int a = 0;
+        if (tmax[1] < tmax[a]) a = 1;
+        if (tmax[2] < tmax[a]) a = 2;
+        if (!(tmax[a] < t1)) break;
+        cell[a] += stp[a];
+        if (cell[a] < 0 || cell[a] >= g[a]) break;
+        tmax[a] = tmax[a] + tdelta[a];
+    }
+    if (SHADER == HY_SHADER_VOLUME && A.srgb) {
+        acc.x = vol_linear_to_srgb(acc.x);
+        acc.y = vol_linear_to_srgb(acc.y);
+        acc.z = vol_linear_to_srgb(acc.z);
+    }
+    if (SHADER == HY_SHADER_ISOSURFACE) aux = make_float4(acc_depth, 0.f, 0.f, 0.f);
+    if (SHADER == HY_SHADER_BLOCKS) aux = make_float4(0.f, 0.f, 0.f, 0.f);
+    return samples;
+}
+
+}  // namespace dev
+}  // namespace hy

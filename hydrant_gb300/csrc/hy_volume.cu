@@ -1,0 +1,311 @@
+// hy_volume.cu -- brick pool, page table and thumbnails on the device.
+//
+// Replaces, for volumes that stay resident, what the reference does per
+// frame on the host: decode bricks and upload one 3-D texture per brick,
+// write vaddr[brick] = slot and re-upload the registry
+// (src/slave/paging/lossless_block_paging.cc:137-174).  Layout in HBM:
+//   pool  : resident bricks, (bs+2*pad)^3 voxels each, x fastest, slots
+//           256-byte aligned, u8 (1 B/voxel) or f32 (4 B/voxel);
+//   info  : int2 per brick {chebyshev distance, registry id or -1}, the
+//           chebyshev thumbnail and the vaddr texture read together
+//           (volume_shader.cu:45-50);
+//   reg   : RegEntry per registry id {k, b, slot offset} (block_paging.hpp:24-36);
+//   mean  : float per brick (the "mean" thumbnail read by blocks_shader.cu:33).
+// The dataset definition this builds: the apron of a brick holds the
+// neighbouring voxels, clamped at the volume border; a brick is non-empty if
+// any voxel of core or apron is non-zero; chebyshev = L-infinity distance in
+// bricks to the nearest non-empty brick (0 = non-empty, max(grid) if there is
+// none); mean = mean of the normalised core voxels.
+
+#include <algorithm>
+#include <cstring>
+
+#include "hy_internal.h"
+
+namespace {
+
+template <typename T>
+__global__ void brick_stats_kernel(const T *__restrict__ raw, int dx, int dy, int dz, int bs,
+                                   int pad, int gx, int gy, unsigned int *__restrict__ nonempty,
+                                   double *__restrict__ core_sum) {
+    const int bid = blockIdx.x;
+    const int bx = bid % gx, by = (bid / gx) % gy, bz = bid / (gx * gy);
+    const int P = bs + 2 * pad;
+    const long long P3 = (long long)P * P * P;
+    unsigned int any = 0;
+    double sum = 0.0;
+    for (long long i = threadIdx.x; i < P3; i += blockDim.x) {
+        int x = int(i % P), y = int((i / P) % P), z = int(i / ((long long)P * P));
+        int X = min(max(bx * bs + x - pad, 0), dx - 1);
+        int Y = min(max(by * bs + y - pad, 0), dy - 1);
+        int Z = min(max(bz * bs + z - pad, 0), dz - 1);
+        T v = raw[((long long)Z * dy + Y) * dx + X];
+        if (v != T(0)) any = 1;
+        bool core = x >= pad && x < pad + bs && y >= pad && y < pad + bs && z >= pad && z < pad + bs;
+        if (core) sum += double(v);
+    }
+    // block reduction
+    __shared__ double ssum[32];
+    __shared__ unsigned int sany[32];
+    for (int o = 16; o > 0; o >>= 1) {
+        sum += __shfl_down_sync(0xffffffffu, sum, o);
+        any |= __shfl_down_sync(0xffffffffu, any, o);
+    }
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+        ssum[warp] = sum;
+        sany[warp] = any;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        int nw = blockDim.x >> 5;
+        sum = lane < nw ? ssum[lane] : 0.0;
+        any = lane < nw ? sany[lane] : 0u;
+        for (int o = 16; o > 0; o >>= 1) {
+            sum += __shfl_down_sync(0xffffffffu, sum, o);
+            any |= __shfl_down_sync(0xffffffffu, any, o);
+        }
+        if (lane == 0) {
+            nonempty[bid] = any;
+            core_sum[bid] = sum;
+        }
+    }
+}
+
+template <typename T>
+__global__ void brick_fill_kernel(const T *__restrict__ raw, int dx, int dy, int dz, int bs,
+                                  int pad, int gx, int gy, const int *__restrict__ slot_brick,
+                                  unsigned char *__restrict__ pool, long long slot_stride) {
+    const int slot = blockIdx.y;
+    const int bid = slot_brick[slot];
+    const int bx = bid % gx, by = (bid / gx) % gy, bz = bid / (gx * gy);
+    const int P = bs + 2 * pad;
+    const long long P3 = (long long)P * P * P;
+    T *dst = reinterpret_cast<T *>(pool + (long long)slot * slot_stride);
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < P3;
+         i += (long long)gridDim.x * blockDim.x) {
+        int x = int(i % P), y = int((i / P) % P), z = int(i / ((long long)P * P));
+        int X = min(max(bx * bs + x - pad, 0), dx - 1);
+        int Y = min(max(by * bs + y - pad, 0), dy - 1);
+        int Z = min(max(bz * bs + z - pad, 0), dz - 1);
+        dst[i] = raw[((long long)Z * dy + Y) * dx + X];
+    }
+}
+
+// Chebyshev distance transform over the brick grid by 26-neighbour dilation.
+void chebyshev_transform(const std::vector<unsigned int> &nonempty, const int g[3],
+                         std::vector<int> &out) {
+    const int n = g[0] * g[1] * g[2];
+    const int cap = std::max(g[0], std::max(g[1], g[2]));
+    out.assign(n, -1);
+    for (int i = 0; i < n; ++i)
+        if (nonempty[i]) out[i] = 0;
+    std::vector<int> next;
+    for (int r = 1; r <= cap; ++r) {
+        next = out;
+        bool changed = false;
+        for (int z = 0; z < g[2]; ++z)
+            for (int y = 0; y < g[1]; ++y)
+                for (int x = 0; x < g[0]; ++x) {
+                    int id = (z * g[1] + y) * g[0] + x;
+                    if (out[id] >= 0) continue;
+                    for (int k = 0; k < 27; ++k) {
+                        int X = x + k % 3 - 1, Y = y + (k / 3) % 3 - 1, Z = z + k / 9 - 1;
+                        if (X < 0 || Y < 0 || Z < 0 || X >= g[0] || Y >= g[1] || Z >= g[2])
+                            continue;
+                        if (out[(Z * g[1] + Y) * g[0] + X] == r - 1) {
+                            next[id] = r;
+                            changed = true;
+                            break;
+                        }
+                    }
+                }
+        out.swap(next);
+        if (!changed) break;
+    }
+    for (int i = 0; i < n; ++i)
+        if (out[i] < 0) out[i] = cap;
+}
+
+void free_volume_device(hy_volume *v) {
+    if (v->pool) cudaFree(v->pool);
+    if (v->info_dev) cudaFree(v->info_dev);
+    if (v->reg_dev) cudaFree(v->reg_dev);
+    if (v->mean_dev) cudaFree(v->mean_dev);
+    v->pool = nullptr;
+    v->info_dev = nullptr;
+    v->reg_dev = nullptr;
+    v->mean_dev = nullptr;
+    v->pool_bytes = 0;
+    v->uploaded = false;
+}
+
+template <typename T>
+int upload_impl(hy_volume *vol, const void *host) {
+    hy_ctx *ctx = vol->ctx;
+    const hy_volume_desc &d = vol->desc;
+    const size_t nvox = size_t(d.dim[0]) * d.dim[1] * d.dim[2];
+    T *raw = nullptr;
+    unsigned int *ne_dev = nullptr;
+    double *sum_dev = nullptr;
+    int *slot_brick_dev = nullptr;
+    auto cleanup = [&] {
+        if (raw) cudaFree(raw);
+        if (ne_dev) cudaFree(ne_dev);
+        if (sum_dev) cudaFree(sum_dev);
+        if (slot_brick_dev) cudaFree(slot_brick_dev);
+    };
+#define HY_UP(call)                                            \
+    do {                                                       \
+        cudaError_t e_ = (call);                               \
+        if (e_ != cudaSuccess) {                               \
+            cleanup();                                         \
+            return hy_cuda_fail(ctx, e_, #call);               \
+        }                                                      \
+    } while (0)
+    free_volume_device(vol);
+    HY_UP(cudaMalloc(&raw, nvox * sizeof(T)));
+    HY_UP(cudaMemcpyAsync(raw, host, nvox * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
+    const int nb = vol->nbricks;
+    HY_UP(cudaMalloc(&ne_dev, nb * sizeof(unsigned int)));
+    HY_UP(cudaMalloc(&sum_dev, nb * sizeof(double)));
+    brick_stats_kernel<T><<<nb, 256, 0, ctx->stream>>>(raw, d.dim[0], d.dim[1], d.dim[2],
+                                                       d.block_size, d.padding, vol->grid[0],
+                                                       vol->grid[1], ne_dev, sum_dev);
+    HY_UP(cudaGetLastError());
+    std::vector<unsigned int> ne(nb);
+    std::vector<double> sums(nb);
+    HY_UP(cudaMemcpyAsync(ne.data(), ne_dev, nb * sizeof(unsigned int), cudaMemcpyDeviceToHost,
+                          ctx->stream));
+    HY_UP(cudaMemcpyAsync(sums.data(), sum_dev, nb * sizeof(double), cudaMemcpyDeviceToHost,
+                          ctx->stream));
+    HY_UP(cudaStreamSynchronize(ctx->stream));
+
+    chebyshev_transform(ne, vol->grid, vol->cheb);
+    const double ncore = double(d.block_size) * d.block_size * d.block_size;
+    vol->mean.resize(nb);
+    for (int i = 0; i < nb; ++i)
+        vol->mean[i] = (sizeof(T) == 1) ? float(sums[i] / 255.0 / ncore) : float(sums[i] / ncore);
+    std::vector<int> slot_brick;
+    vol->reg_of_brick.assign(nb, -1);
+    for (int i = 0; i < nb; ++i)
+        if (ne[i]) {
+            vol->reg_of_brick[i] = int(slot_brick.size());
+            slot_brick.push_back(i);
+        }
+    vol->nonempty = int(slot_brick.size());
+    vol->resident = vol->nonempty;
+    const int nslots = std::max(vol->resident, 1);
+    vol->pool_bytes = size_t(nslots) * vol->slot_stride;
+    HY_UP(cudaMalloc(&vol->pool, vol->pool_bytes));
+    HY_UP(cudaMemsetAsync(vol->pool, 0, vol->pool_bytes, ctx->stream));
+    if (vol->resident > 0) {
+        HY_UP(cudaMalloc(&slot_brick_dev, slot_brick.size() * sizeof(int)));
+        HY_UP(cudaMemcpyAsync(slot_brick_dev, slot_brick.data(), slot_brick.size() * sizeof(int),
+                              cudaMemcpyHostToDevice, ctx->stream));
+        const long long P3 = (long long)vol->P * vol->P * vol->P;
+        dim3 grid(unsigned((P3 + 255) / 256 < 512 ? (P3 + 255) / 256 : 512), vol->resident);
+        brick_fill_kernel<T><<<grid, 256, 0, ctx->stream>>>(
+            raw, d.dim[0], d.dim[1], d.dim[2], d.block_size, d.padding, vol->grid[0],
+            vol->grid[1], slot_brick_dev, vol->pool, (long long)vol->slot_stride);
+        HY_UP(cudaGetLastError());
+    }
+    std::vector<int2> info(nb);
+    for (int i = 0; i < nb; ++i) info[i] = make_int2(vol->cheb[i], vol->reg_of_brick[i]);
+    std::vector<hy::RegEntry> reg(nslots);
+    for (int s = 0; s < nslots; ++s) {
+        reg[s] = hy::RegEntry{vol->k, vol->b, vol->b, vol->b, (long long)s * (long long)vol->slot_stride,
+                              {0, 0}};
+    }
+    HY_UP(cudaMalloc(&vol->info_dev, nb * sizeof(int2)));
+    HY_UP(cudaMalloc(&vol->reg_dev, nslots * sizeof(hy::RegEntry)));
+    HY_UP(cudaMalloc(&vol->mean_dev, nb * sizeof(float)));
+    HY_UP(cudaMemcpyAsync(vol->info_dev, info.data(), nb * sizeof(int2), cudaMemcpyHostToDevice,
+                          ctx->stream));
+    HY_UP(cudaMemcpyAsync(vol->reg_dev, reg.data(), nslots * sizeof(hy::RegEntry),
+                          cudaMemcpyHostToDevice, ctx->stream));
+    HY_UP(cudaMemcpyAsync(vol->mean_dev, vol->mean.data(), nb * sizeof(float),
+                          cudaMemcpyHostToDevice, ctx->stream));
+    HY_UP(cudaStreamSynchronize(ctx->stream));
+#undef HY_UP
+    cleanup();
+    vol->uploaded = true;
+    return HY_OK;
+}
+
+}  // namespace
+
+extern "C" int hy_volume_create(hy_ctx *ctx, const hy_volume_desc *desc, hy_volume **out) {
+    if (!ctx || !desc || !out) return HY_ERR_INVALID;
+    *out = nullptr;
+    if (desc->dtype != HY_DTYPE_U8 && desc->dtype != HY_DTYPE_F32)
+        return hy_fail(ctx, HY_ERR_INVALID, "volume: dtype must be u8 or f32");
+    if (desc->block_size <= 0 || desc->padding < 0 || desc->padding > desc->block_size)
+        return hy_fail(ctx, HY_ERR_INVALID, "volume: bad block_size/padding");
+    for (int i = 0; i < 3; ++i)
+        if (desc->dim[i] <= 0) return hy_fail(ctx, HY_ERR_INVALID, "volume: bad dims");
+    hy_volume *v = new hy_volume();
+    v->ctx = ctx;
+    v->desc = *desc;
+    for (int i = 0; i < 3; ++i) v->grid[i] = (desc->dim[i] + desc->block_size - 1) / desc->block_size;
+    long long nb = (long long)v->grid[0] * v->grid[1] * v->grid[2];
+    if (nb > (1 << 24)) {
+        delete v;
+        return hy_fail(ctx, HY_ERR_INVALID, "volume: more than 2^24 bricks");
+    }
+    v->nbricks = int(nb);
+    v->P = desc->block_size + 2 * desc->padding;
+    v->elem = desc->dtype == HY_DTYPE_U8 ? 1 : 4;
+    size_t bytes = size_t(v->P) * v->P * v->P * v->elem;
+    v->slot_stride = (bytes + 255) / 256 * 256;
+    // lossless_block_paging.cc:20-22 / rt_block_paging.cc:219-221
+    v->k = float(desc->block_size) / float(v->P);
+    v->b = float(desc->padding) / float(desc->block_size) * v->k;
+    // basic_renderer.hpp:104-118: bbox = [0, raw / block_size], du = 1 / block_size
+    float blksz = float(desc->block_size);
+    for (int i = 0; i < 3; ++i) v->bbox_max[i] = float(desc->dim[i]) / blksz;
+    v->du = 1.f / blksz;
+    *out = v;
+    return HY_OK;
+}
+
+extern "C" int hy_volume_destroy(hy_volume *vol) {
+    if (!vol) return HY_OK;
+    cudaSetDevice(vol->ctx->device);
+    cudaStreamSynchronize(vol->ctx->stream);
+    free_volume_device(vol);
+    delete vol;
+    return HY_OK;
+}
+
+extern "C" int hy_volume_upload(hy_volume *vol, const void *host_voxels) {
+    if (!vol || !host_voxels) return HY_ERR_INVALID;
+    HY_CUDA(vol->ctx, cudaSetDevice(vol->ctx->device));
+    if (vol->desc.dtype == HY_DTYPE_U8) return upload_impl<unsigned char>(vol, host_voxels);
+    return upload_impl<float>(vol, host_voxels);
+}
+
+extern "C" int hy_volume_get_info(const hy_volume *vol, hy_volume_info *out) {
+    if (!vol || !out) return HY_ERR_INVALID;
+    for (int i = 0; i < 3; ++i) {
+        out->grid[i] = vol->grid[i];
+        out->bbox_max[i] = vol->bbox_max[i];
+    }
+    out->nbricks = vol->nbricks;
+    out->nonempty = vol->nonempty;
+    out->resident = vol->resident;
+    out->padded = vol->P;
+    out->slot_bytes = (int64_t)vol->slot_stride;
+    out->pool_bytes = (int64_t)vol->pool_bytes;
+    return HY_OK;
+}
+
+extern "C" int hy_volume_thumbnails(const hy_volume *vol, int32_t *chebyshev, float *mean) {
+    if (!vol) return HY_ERR_INVALID;
+    if (!vol->uploaded) return hy_fail(vol->ctx, HY_ERR_STATE, "volume: not uploaded");
+    for (int i = 0; i < vol->nbricks; ++i) {
+        if (chebyshev) chebyshev[i] = vol->cheb[i];
+        if (mean) mean[i] = vol->mean[i];
+    }
+    return HY_OK;
+}

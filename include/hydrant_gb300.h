@@ -1,0 +1,235 @@
+/*
+ * hydrant_gb300.h -- C ABI of the GB300 (sm_103a) ray-marching path.
+ *
+ * This is the drop-in boundary for Hydrant's CUDA shading backend.  In the
+ * reference a renderer reaches the GPU through
+ *   ShaderRegistrar::cuda<K>()  (include/hydrant/core/shader.hpp:319-345)
+ * which installs ShaderMeta.devices[Cuda] = std::function<ShadingResult(void*)>
+ * taking CudaShadingArgs{launch_info, BasicKernelArgs*, IShaderTypeErased*}
+ * (shader.hpp:202-276), called per pass from Raycaster::*_pass
+ * (include/hydrant/core/raycaster.hpp:32-123).  The entry points below take
+ * the same information as plain pointers and sizes: the shader parameters
+ * (the shader struct the reference copies into __constant__ memory), the view
+ * (ViewArgs, shader.hpp:63-68), the film / destination images (ImageDesc,
+ * shader.hpp:70-83) and the pass (ShadingPass, shader.hpp:55-61).
+ *
+ * Conventions
+ *  - Every call returns an int status: HY_OK (0) or a negative HY_ERR_*.
+ *    hy_last_error() gives a message for the last failure on a context.
+ *    No exception crosses this boundary.
+ *  - Buffers are caller-owned.  *_device entry points take device pointers and
+ *    are asynchronous on the context's stream; the others take host pointers
+ *    and return after the result is on the host.
+ *  - One stream per context; a context is not thread-safe (the reference
+ *    serialises renderers with cufx::Device::Lock, basic_renderer.hpp:89-92).
+ *  - Coordinates follow the reference: object space is measured in bricks,
+ *    the volume's bounding box is [0, raw/block_size] (basic_renderer.hpp:104-118).
+ */
+#ifndef HYDRANT_GB300_H
+#define HYDRANT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HY_OK 0
+#define HY_ERR_INVALID (-1)     /* bad argument or size */
+#define HY_ERR_CUDA (-2)        /* a CUDA runtime call failed */
+#define HY_ERR_OOM (-3)         /* device or pinned allocation failed */
+#define HY_ERR_TIMEOUT (-4)     /* a bounded device-side wait gave up */
+#define HY_ERR_UNSUPPORTED (-5) /* combination not built */
+#define HY_ERR_STATE (-6)       /* object not ready (e.g. no transfer function) */
+
+/* Shaders: the three REGISTER_SHADER_BUILDER registrations on the path
+ * (volume_shader.cu:84-88, blocks_shader.cu:53-57, isosurface_shader.cu:128-132). */
+enum { HY_SHADER_VOLUME = 0, HY_SHADER_BLOCKS = 1, HY_SHADER_ISOSURFACE = 2 };
+/* VolumeRenderMode (ui/volume.schema.hpp:11-14) */
+enum { HY_VOLUME_DEFAULT = 0, HY_VOLUME_PARTITION = 1, HY_VOLUME_PAGING = 2 };
+/* BlocksRenderMode (ui/blocks.schema.hpp:10-11) */
+enum { HY_BLOCKS_VOLUME = 0, HY_BLOCKS_SOLID = 1 };
+/* IsosurfaceRenderMode (ui/isosurface.schema.hpp:10-11) */
+enum { HY_ISO_COLOR = 0, HY_ISO_NORMAL = 1, HY_ISO_POSITION = 2 };
+/* ShadingPass (shader.hpp:55-61) */
+enum { HY_PASS_RAY_EMIT = 0, HY_PASS_RAY_MARCH = 1, HY_PASS_PIXEL = 2, HY_PASS_FETCH = 3 };
+/* voxel types: u8 is read as clamp(u/255,0,1) (texture_3d.hpp:78-86), f32 raw */
+enum { HY_DTYPE_U8 = 0, HY_DTYPE_F32 = 1 };
+
+typedef struct hy_ctx hy_ctx;
+typedef struct hy_volume hy_volume;
+
+/* ViewArgs (shader.hpp:63-68): trans = iet * inverse(lookAt) (column-major,
+ * camera -> object space), ctg_fovy_2 = 1/tan(fovy/2), ray_o = iet * eye. */
+typedef struct hy_view {
+    float trans[16];
+    float ctg_fovy_2;
+    float ray_o[3];
+} hy_view;
+
+/* Camera (include/hydrant/core/scene.hpp:32-82), world space. */
+typedef struct hy_camera {
+    float position[3];
+    float target[3];
+    float up[3];
+    float ctg_fovy_2;
+} hy_camera;
+
+/* The shader struct of each registered shader, flattened.  Fields a shader
+ * does not read are ignored.  step/du/bbox/max_steps of IShaderTypeErased
+ * (shader.hpp:16-22) are derived from the volume and sample_rate/max_steps
+ * exactly as BasicRenderer::init/update do (basic_renderer.hpp:104-131). */
+typedef struct hy_shader_params {
+    int32_t shader;          /* HY_SHADER_* */
+    int32_t mode;            /* the shader's render mode */
+    float sample_rate;       /* step = du / 4 / sample_rate */
+    int32_t max_steps;
+    float density;           /* Blocks: density*mean; Volume: opacity scale (1 = reference) */
+    float isovalue;          /* Isosurface, normalised */
+    float surface_color[3];  /* Isosurface */
+    float clear_color[3];    /* written where v.a == 0 (pixel_template.hpp:11-20) */
+    float rank;              /* Volume Partition tint, rank/(size-1) */
+    int32_t lowest_blkcnt;   /* Volume Paging tint: registry ids below are coarse bricks */
+    float to_world[16];      /* Isosurface: inverse(exhibit.get_iet()) */
+    float eye_pos[3];        /* Isosurface: camera position (world) */
+    float light_pos[3];      /* Isosurface: pos+target+up+cross(target,up) */
+    int32_t composite;       /* 0: one march through the volume box (offline path);
+                                1: per-brick segments composited front to back
+                                   (sort-last operator of volume.cc:267-280 /
+                                   isosurface.cc:272-290) */
+    int32_t srgb;            /* Volume: linear_to_srgb before quantising (volume.cc:282-292) */
+    int32_t count_samples;   /* 1: count trilinear brick samples into hy_render_stats */
+} hy_shader_params;
+
+/* Film pixel layouts of the reference (shader.hpp:26-34, pixel_template.hpp:11-20,
+ * volume_shader.hpp:11-22, isosurface_shader.hpp:11-21).  The pass-level entry
+ * point reads and writes films in exactly these layouts. */
+typedef struct hy_ray_pixel {
+    float o[3];
+    float d[3];
+    int32_t nsteps;
+    int32_t step_size;
+} hy_ray_pixel; /* IPixel, 32 B */
+
+typedef struct hy_std_pixel {
+    hy_ray_pixel ray;
+    float v[4];
+} hy_std_pixel; /* StdVec4Pixel (Blocks film), 48 B */
+
+typedef struct hy_volume_pixel {
+    hy_ray_pixel ray;
+    float v[4];
+    float theta[3];
+    float phi;
+} hy_volume_pixel; /* VolumePixel, 64 B */
+
+typedef struct hy_iso_pixel {
+    hy_ray_pixel ray;
+    float v[4];
+    float origin[3];
+    float depth;
+} hy_iso_pixel; /* IsosurfacePixel, 64 B */
+
+typedef struct hy_volume_fetch_pixel {
+    float theta[3];
+    float phi;
+    float val[4];
+} hy_volume_fetch_pixel; /* VolumeFetchPixel, 32 B */
+
+typedef struct hy_iso_fetch_pixel {
+    uint8_t val[3];
+    uint8_t pad_;
+    float depth;
+} hy_iso_fetch_pixel; /* IsosurfaceFetchPixel, 8 B */
+
+/* Dataset meta the renderers read (basic_renderer.hpp:104-118,
+ * lossless_block_paging.cc:17-22): raw dims, block size, apron. */
+typedef struct hy_volume_desc {
+    int32_t dim[3];
+    int32_t block_size;
+    int32_t padding;
+    int32_t dtype; /* HY_DTYPE_* */
+} hy_volume_desc;
+
+typedef struct hy_volume_info {
+    int32_t grid[3];        /* bricks per axis = ceil(dim/block_size) */
+    int32_t nbricks;
+    int32_t nonempty;       /* bricks with any non-zero voxel in core + apron */
+    int32_t resident;       /* bricks with a device slot */
+    int32_t padded;         /* block_size + 2*padding */
+    int64_t slot_bytes;     /* bytes between slots in the brick pool */
+    int64_t pool_bytes;
+    float bbox_max[3];      /* raw / block_size */
+} hy_volume_info;
+
+typedef struct hy_render_stats {
+    int64_t samples;        /* trilinear brick samples of the last render (count_samples=1) */
+    int64_t pixels;
+    float ms;               /* device time of the last render's kernels */
+} hy_render_stats;
+
+/* ---- context ---------------------------------------------------------------- */
+int hy_ctx_create(int device, hy_ctx **out);
+int hy_ctx_destroy(hy_ctx *ctx);
+const char *hy_last_error(const hy_ctx *ctx);
+int hy_ctx_synchronize(hy_ctx *ctx);
+/* The context's cudaStream_t, for callers that order their own work with it. */
+void *hy_ctx_stream(hy_ctx *ctx);
+int hy_render_stats_get(hy_ctx *ctx, hy_render_stats *out);
+
+/* Transfer function: n RGBA knots, float, flattened (transfer_fn.schema.hpp:12,
+ * transfer_fn.hpp:16-23: Border, Linear, normalised coordinates). */
+int hy_tf_set(hy_ctx *ctx, const float *rgba, int32_t n);
+
+/* ---- volume (brick pool, page table, thumbnails) ---------------------------- */
+int hy_volume_create(hy_ctx *ctx, const hy_volume_desc *desc, hy_volume **out);
+int hy_volume_destroy(hy_volume *vol);
+/* Upload a whole raw volume (x fastest) from host memory; bricks it on the
+ * device with a replicate-edge apron, builds the chebyshev and mean
+ * thumbnails and makes every non-empty brick resident.  Replaces the
+ * decode + Texture3D::source upload of LosslessBlockPagingServer (
+ * src/slave/paging/lossless_block_paging.cc:137-174) for resident volumes. */
+int hy_volume_upload(hy_volume *vol, const void *host_voxels);
+int hy_volume_get_info(const hy_volume *vol, hy_volume_info *out);
+/* Copy the per-brick thumbnails to the host (grid x fastest). */
+int hy_volume_thumbnails(const hy_volume *vol, int32_t *chebyshev, float *mean);
+
+/* ---- camera helpers (scene.hpp:20-81, raycaster.hpp:249-258) ----------------- */
+/* Orbit camera: arm = (azimuth deg about y, elevation deg about z, distance). */
+int hy_camera_orbit(const float arm[3], const float center[3], float fovy_deg, hy_camera *out);
+int hy_camera_ptu(const float position[3], const float target[3], const float up[3],
+                  float fovy_deg, hy_camera *out);
+int hy_camera_view(const hy_volume *vol, const hy_camera *cam, hy_view *out);
+/* Fill to_world / eye_pos / light_pos as IsosurfaceRenderer does (isosurface.cc:108-113). */
+int hy_iso_lighting(const hy_volume *vol, const hy_camera *cam, hy_shader_params *inout);
+
+/* ---- rendering -------------------------------------------------------------- */
+/* Fused emit + march + pixel for one view: rgba8 out (RGB by the reference's
+ * write_to rule, A = trunc(clamp(v.a,0,1)*255)); optional float outputs:
+ * v_out (W*H*4, pre-quantisation v), aux_out (W*H*4: Volume theta.xyz,phi;
+ * Isosurface depth in .x).  Host pointers; returns when results are on the host. */
+int hy_render(hy_ctx *ctx, const hy_volume *vol, const hy_shader_params *params,
+              const hy_view *view, int32_t width, int32_t height,
+              uint8_t *rgba_out, float *v_out, float *aux_out);
+/* Same with device pointers, asynchronous on the context's stream. */
+int hy_render_device(hy_ctx *ctx, const hy_volume *vol, const hy_shader_params *params,
+                     const hy_view *view, int32_t width, int32_t height,
+                     uint8_t *rgba_dev, float *v_dev, float *aux_dev);
+
+/* One shading pass over a device film in the reference's pixel layout --
+ * the body of ShaderMeta.devices[Cuda] (shader.hpp:319-345).
+ *   RAY_EMIT : view -> film (hy_*_pixel)           (cuda_shading.cu:14-35)
+ *   RAY_MARCH: film -> film, resumes every pixel    (cuda_shading.cu:41-54)
+ *   PIXEL    : film -> dst uchar3 (RGB8)            (cuda_shading.cu:60-74)
+ *   FETCH    : film -> dst fetch pixels             (cuda_shading.cu:80-94)
+ * Asynchronous on the context's stream. */
+int hy_shade_pass(hy_ctx *ctx, const hy_volume *vol, const hy_shader_params *params,
+                  int32_t pass, const hy_view *view, void *film_dev, int32_t width,
+                  int32_t height, void *dst_dev, const uint8_t clear_rgb[3]);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HYDRANT_GB300_H */

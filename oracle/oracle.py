@@ -1,0 +1,183 @@
+"""ctypes wrapper of the oracle -- TEST INFRASTRUCTURE ONLY.
+
+The oracle is a CPU restatement of Hydrant's CPU shading backend
+(hy_oracle.cc).  Only tests/, __graft_entry__.smoke() and bench.py's CPU
+baseline / reference arm load it, as the checker or as the timed CPU
+baseline.  PARITY UNPINNED: no reference build and no reference golden
+vectors exist for this path; see hy_oracle.h.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+from typing import Optional
+
+import numpy as np
+
+from . import build as _build  # type: ignore[attr-defined]
+
+f3 = C.c_float * 3
+f16 = C.c_float * 16
+
+
+class OrcParams(C.Structure):
+    _fields_ = [
+        ("shader", C.c_int32),
+        ("mode", C.c_int32),
+        ("sample_rate", C.c_float),
+        ("max_steps", C.c_int32),
+        ("density", C.c_float),
+        ("isovalue", C.c_float),
+        ("surface_color", f3),
+        ("clear_color", f3),
+        ("rank", C.c_float),
+        ("lowest_blkcnt", C.c_int32),
+        ("to_world", f16),
+        ("eye_pos", f3),
+        ("light_pos", f3),
+        ("composite", C.c_int32),
+        ("srgb", C.c_int32),
+        ("count_samples", C.c_int32),
+    ]
+
+
+P = C.c_void_p
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        l = C.CDLL(str(path))
+        protos = {
+            "orc_volume_create": (P, [P, C.c_int32, C.c_int32, C.c_int32, P]),
+            "orc_volume_free": (None, [P]),
+            "orc_volume_grid": (None, [P, P, P]),
+            "orc_volume_thumbnails": (None, [P, P, P]),
+            "orc_volume_set_present": (None, [P, P]),
+            "orc_volume_brick": (None, [P, C.c_int32, P]),
+            "orc_camera_orbit": (None, [P, P, C.c_float, P]),
+            "orc_camera_ptu": (None, [P, P, P, C.c_float, P]),
+            "orc_camera_view": (None, [P, P, P]),
+            "orc_iso_lighting": (None, [P, P, C.POINTER(OrcParams)]),
+            "orc_render": (C.c_int64, [P, P, C.c_int32, C.POINTER(OrcParams), P, C.c_int32, C.c_int32,
+                                       C.c_int32, P, P, P, P]),
+            "orc_render_rows": (C.c_int64, [P, P, C.c_int32, C.POINTER(OrcParams), P, C.c_int32,
+                                            C.c_int32, C.c_int32, C.c_int32, C.c_int32, P, P, P, P]),
+            "orc_march_film": (C.c_int64, [P, P, C.c_int32, C.POINTER(OrcParams), C.c_int32,
+                                           C.c_int32, C.c_int32, P]),
+        }
+        for name, (res, args) in protos.items():
+            fn = getattr(l, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = l
+    return _lib
+
+
+def _p(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def params_from(struct) -> OrcParams:
+    """Copy a layout-identical ctypes parameter structure into OrcParams."""
+    p = OrcParams()
+    C.memmove(C.byref(p), C.byref(struct), C.sizeof(OrcParams))
+    return p
+
+
+class OracleVolume:
+    def __init__(self, voxels: np.ndarray, block_size: int, padding: int = 1):
+        vox = np.ascontiguousarray(voxels)
+        dtype = {np.dtype(np.uint8): 0, np.dtype(np.float32): 1}[vox.dtype]
+        nz, ny, nx = vox.shape
+        dim = (C.c_int32 * 3)(nx, ny, nz)
+        self.h = lib().orc_volume_create(C.cast(dim, P), block_size, padding, dtype, _p(vox))
+        if not self.h:
+            raise RuntimeError("orc_volume_create failed")
+        self.block_size = block_size
+        self.padding = padding
+        g = (C.c_int32 * 3)()
+        ne = C.c_int32()
+        lib().orc_volume_grid(self.h, C.cast(g, P), C.byref(ne))
+        self.grid = (g[0], g[1], g[2])
+        self.nonempty = ne.value
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_volume_free(self.h)
+            self.h = None
+
+    def thumbnails(self):
+        n = self.grid[0] * self.grid[1] * self.grid[2]
+        cheb = np.zeros(n, np.int32)
+        mean = np.zeros(n, np.float32)
+        lib().orc_volume_thumbnails(self.h, _p(cheb), _p(mean))
+        shape = (self.grid[2], self.grid[1], self.grid[0])
+        return cheb.reshape(shape), mean.reshape(shape)
+
+    def brick(self, i: int) -> np.ndarray:
+        P_ = self.block_size + 2 * self.padding
+        out = np.zeros(P_ ** 3, np.float32)
+        lib().orc_volume_brick(self.h, i, _p(out))
+        return out.reshape(P_, P_, P_)
+
+    def set_present(self, mask: np.ndarray) -> None:
+        m = np.ascontiguousarray(mask.astype(np.uint8).ravel())
+        lib().orc_volume_set_present(self.h, _p(m))
+
+
+def camera_orbit(arm, center=(0.0, 0.0, 0.0), fovy=60.0) -> np.ndarray:
+    out = np.zeros(10, np.float32)
+    a = np.asarray(arm, np.float32)
+    c = np.asarray(center, np.float32)
+    lib().orc_camera_orbit(_p(a), _p(c), fovy, _p(out))
+    return out
+
+
+def camera_ptu(pos, target=(0.0, 0.0, 0.0), up=(0.0, 1.0, 0.0), fovy=60.0) -> np.ndarray:
+    out = np.zeros(10, np.float32)
+    arrs = [np.asarray(v, np.float32) for v in (pos, target, up)]
+    lib().orc_camera_ptu(_p(arrs[0]), _p(arrs[1]), _p(arrs[2]), fovy, _p(out))
+    return out
+
+
+def camera_view(vol: OracleVolume, cam: np.ndarray) -> np.ndarray:
+    out = np.zeros(20, np.float32)
+    c = np.ascontiguousarray(cam, np.float32)
+    lib().orc_camera_view(vol.h, _p(c), _p(out))
+    return out
+
+
+def iso_lighting(vol: OracleVolume, cam: np.ndarray, params: OrcParams) -> OrcParams:
+    c = np.ascontiguousarray(cam, np.float32)
+    lib().orc_iso_lighting(vol.h, _p(c), C.byref(params))
+    return params
+
+
+def render(vol: OracleVolume, tf, params: OrcParams, view: np.ndarray, width: int, height: int,
+           nthreads: int = 0, want_v=True, want_aux=True, want_film=False, rows=None):
+    tfa = np.ascontiguousarray(np.asarray(tf, np.float32).reshape(-1, 4))
+    v = np.zeros((height, width, 4), np.float32) if want_v else None
+    rgba = np.zeros((height, width, 4), np.uint8)
+    aux = np.zeros((height, width, 4), np.float32) if want_aux else None
+    fb = 48 if params.shader == 1 else 64
+    film = np.zeros((height, width, fb), np.uint8) if want_film else None
+    view = np.ascontiguousarray(view, np.float32)
+    if rows is None:
+        n = lib().orc_render(vol.h, _p(tfa), tfa.shape[0], C.byref(params), _p(view), width, height,
+                             nthreads, _p(v), _p(rgba), _p(aux), _p(film))
+    else:
+        n = lib().orc_render_rows(vol.h, _p(tfa), tfa.shape[0], C.byref(params), _p(view), width,
+                                  height, rows[0], rows[1], nthreads, _p(v), _p(rgba), _p(aux),
+                                  _p(film))
+    return dict(v=v, rgba=rgba, aux=aux, film=film, samples=int(n))
+
+
+def march_film(vol: OracleVolume, tf, params: OrcParams, film: np.ndarray, width: int, height: int,
+               nthreads: int = 0) -> int:
+    tfa = np.ascontiguousarray(np.asarray(tf, np.float32).reshape(-1, 4))
+    return int(lib().orc_march_film(vol.h, _p(tfa), tfa.shape[0], C.byref(params), width, height,
+                                    nthreads, _p(film)))

@@ -1,0 +1,216 @@
+"""GPU parity: the CUDA path (through the C ABI) against the oracle.
+
+Bar: <= 1 LSB per 8-bit RGBA channel, <= 1e-4 max abs on the
+pre-quantisation floats, and the same number of brick samples (which pins
+every skip / adaptive-step / termination decision of every ray).
+"""
+
+import numpy as np
+import pytest
+
+import hydrant_gb300 as hy
+from hydrant_gb300 import workloads as wl
+from oracle import oracle as orc
+from tests._harness import Case, assert_parity, camera, view_array
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def blobs64(ctx):
+    c = Case(ctx, hy.synth_blobs_u8(0, (64, 64, 64), 12), 64, 1)
+    yield c
+    c.close()
+
+
+@pytest.fixture(scope="module")
+def tubes128(ctx):
+    c = Case(ctx, hy.synth_tubes_u8(1, (128, 128, 128), 12), 32, 1)
+    yield c
+    c.close()
+
+
+@pytest.fixture(scope="module")
+def c0(ctx):
+    w = wl.volume_c0()
+    c = Case(ctx, w.voxels(), w.block_size, w.padding, w.tf)
+    yield c, w
+    c.close()
+
+
+def test_volume_c0_full(c0):
+    c, w = c0
+    v = w.views[0]
+    g, r, _, _ = c.render_both(wl.make_camera(v.camera), v.width, v.height, **w.params)
+    s = assert_parity(g, r, what="config 0")
+    assert r["samples"] > 1_000_000
+    print("config0", s)
+
+
+@pytest.mark.parametrize("density", [1.0, 1e-2, 0.3])
+def test_volume_density(blobs64, density):
+    g, r, _, _ = blobs64.render_both(camera(), 96, 80, shader="Volume", sample_rate=0.25,
+                                     density=density)
+    assert_parity(g, r, what=f"density {density}")
+
+
+@pytest.mark.parametrize("sample_rate", [1.0, 0.5, 2.0])
+def test_volume_sample_rate(blobs64, sample_rate):
+    g, r, _, _ = blobs64.render_both(camera(a=(10, 30, 2.0)), 64, 64, shader="Volume",
+                                     sample_rate=sample_rate, density=1.0)
+    assert_parity(g, r, what=f"sample_rate {sample_rate}")
+
+
+@pytest.mark.parametrize("mode", ["Partition", "Paging"])
+def test_volume_modes(blobs64, mode):
+    g, r, _, _ = blobs64.render_both(camera(), 64, 48, shader="Volume", mode=mode,
+                                     sample_rate=0.5, density=1.0, rank=0.25)
+    assert_parity(g, r, what=mode)
+
+
+def test_volume_multibrick(tubes128):
+    g, r, _, _ = tubes128.render_both(camera(a=(40, 20, 2.5)), 128, 128, shader="Volume",
+                                      sample_rate=0.5, density=0.5)
+    assert_parity(g, r, what="multi-brick volume")
+
+
+@pytest.mark.parametrize("mode", ["Volume", "Solid"])
+def test_blocks(tubes128, mode):
+    g, r, _, _ = tubes128.render_both(camera(), 128, 96, shader="Blocks", mode=mode,
+                                      density=1e-2)
+    assert_parity(g, r, what=f"blocks {mode}")
+
+
+@pytest.mark.parametrize("mode", ["Color", "Normal", "Position"])
+def test_isosurface(tubes128, mode):
+    g, r, _, _ = tubes128.render_both(camera(a=(30, 50, 2.4)), 128, 128, shader="Isosurface",
+                                      mode=mode, isovalue=0.5)
+    assert_parity(g, r, what=f"iso {mode}")
+
+
+@pytest.mark.parametrize("shader,mode", [("Volume", 0), ("Blocks", "Volume"), ("Blocks", "Solid"),
+                                         ("Isosurface", "Color")])
+def test_composite_per_brick(tubes128, shader, mode):
+    kw = dict(shader=shader, mode=mode, composite=True, density=0.5 if shader == "Volume" else 1e-2,
+              sample_rate=0.5)
+    g, r, _, _ = tubes128.render_both(camera(a=(-35, 25, 2.3)), 96, 96, **kw)
+    assert_parity(g, r, what=f"composite {shader}")
+
+
+def test_volume_composite_srgb(tubes128):
+    g, r, _, _ = tubes128.render_both(camera(), 64, 64, shader="Volume", composite=True, srgb=True,
+                                      density=0.5)
+    assert_parity(g, r, what="composite srgb")
+
+
+def test_f32_volume(ctx):
+    c = Case(ctx, hy.synth_blobs_f32(4, (48, 48, 48), 16), 16, 1)
+    try:
+        g, r, _, _ = c.render_both(camera(), 80, 64, shader="Volume", sample_rate=1.0, density=1.0)
+        assert_parity(g, r, what="f32 volume")
+        g, r, _, _ = c.render_both(camera(), 64, 64, shader="Isosurface", isovalue=0.3)
+        assert_parity(g, r, what="f32 iso")
+    finally:
+        c.close()
+
+
+@pytest.mark.parametrize("wh", [(1, 1), (37, 23), (17, 9), (300, 7)])
+def test_ragged_resolutions(blobs64, wh):
+    g, r, _, _ = blobs64.render_both(camera(), wh[0], wh[1], shader="Volume", density=1.0)
+    assert_parity(g, r, what=f"{wh}")
+
+
+def test_camera_inside_volume(tubes128):
+    cam = camera("ptu", a=(0.1, -0.2, 0.15), target=(1.0, 0.3, -0.4))
+    for shader in ("Volume", "Isosurface", "Blocks"):
+        g, r, _, _ = tubes128.render_both(cam, 64, 64, shader=shader, density=0.2, sample_rate=0.5)
+        assert_parity(g, r, what=f"inside {shader}")
+
+
+def test_empty_volume_clear_colour(ctx):
+    c = Case(ctx, np.zeros((40, 40, 40), np.uint8), 16, 1)
+    try:
+        g, r, _, _ = c.render_both(camera(), 32, 32, shader="Volume", clear_color=(0.2, 0.4, 0.6))
+        assert_parity(g, r, what="empty")
+        assert g.samples == 0
+        assert np.all(g.rgba[..., :3] == [51, 102, 153]) and np.all(g.rgba[..., 3] == 0)
+    finally:
+        c.close()
+
+
+def test_axis_aligned_rays(blobs64):
+    # a camera on the z axis gives direction components of exactly 0 near the centre
+    cam = camera("ptu", a=(0.0, 0.0, 2.0))
+    g, r, _, _ = blobs64.render_both(cam, 33, 33, shader="Volume", density=1.0)
+    assert_parity(g, r, what="axis aligned")
+
+
+def test_camera_helpers_match_oracle(blobs64):
+    for arm in [(25, 65, 2.2), (-120, 10, 3.0), (0, 0, 1.5)]:
+        cam = camera(a=arm)
+        o = orc.camera_orbit(arm)
+        got = np.array(list(cam.position) + list(cam.target) + list(cam.up) + [cam.ctg_fovy_2])
+        np.testing.assert_allclose(got, o, rtol=1e-6, atol=1e-6)
+        v = view_array(hy.camera_view(blobs64.vol, cam))
+        ov = orc.camera_view(blobs64.ov, o)
+        np.testing.assert_allclose(v, ov, rtol=1e-5, atol=1e-6)
+
+
+def _film_dtype(shader):
+    return 48 if shader == "Blocks" else 64
+
+
+@pytest.mark.parametrize("shader", ["Volume", "Blocks", "Isosurface"])
+def test_pass_level_film(tubes128, shader):
+    """hy_shade_pass RAY_EMIT / PIXEL / FETCH on a reference-layout film."""
+    torch = pytest.importorskip("torch")
+    W, H = 48, 40
+    cam = camera(a=(15, 35, 2.2))
+    p = hy.shader_params(shader=shader, density=0.4, sample_rate=0.5)
+    if shader == "Isosurface":
+        hy.iso_lighting(tubes128.vol, cam, p)
+    view = hy.camera_view(tubes128.vol, cam)
+    fb = _film_dtype(shader)
+    film = torch.zeros(H * W * fb, dtype=torch.uint8, device="cuda")
+    dst = torch.zeros(H * W * 32, dtype=torch.uint8, device="cuda")
+    ctx = tubes128.ctx
+    hy.shade_pass(ctx, tubes128.vol, p, hy._abi.PASS_RAY_EMIT, view, film.data_ptr(), W, H)
+    ctx.synchronize()
+    ref = orc.render(tubes128.ov, tubes128.tf, orc.params_from(p), view_array(view), W, H,
+                     want_film=True)
+    got = film.cpu().numpy().reshape(H, W, fb)
+    assert np.array_equal(got, ref["film"]), "emit film differs from the oracle"
+    hy.shade_pass(ctx, tubes128.vol, p, hy._abi.PASS_PIXEL, None, film.data_ptr(), W, H,
+                  dst.data_ptr(), clear_rgb=(0, 0, 0))
+    ctx.synchronize()
+    rgb = dst.cpu().numpy()[: H * W * 3].reshape(H, W, 3)
+    assert np.array_equal(rgb, ref["rgba"][..., :3])
+    if shader != "Blocks":
+        hy.shade_pass(ctx, tubes128.vol, p, hy._abi.PASS_FETCH, None, film.data_ptr(), W, H,
+                      dst.data_ptr())
+        ctx.synchronize()
+        fetched = dst.cpu().numpy()
+        if shader == "Volume":
+            f = fetched.view(np.float32)[: H * W * 8].reshape(H, W, 8)
+            np.testing.assert_array_equal(f[..., 0:4], ref["aux"])       # theta, phi
+            np.testing.assert_array_equal(f[..., 4:8], ref["v"])         # val
+        else:
+            f = fetched[: H * W * 8].reshape(H, W, 8)
+            np.testing.assert_array_equal(f[..., :3], ref["rgba"][..., :3])
+            depth = f[..., 4:8].copy().view(np.float32)[..., 0]
+            np.testing.assert_array_equal(depth, ref["aux"][..., 0])
+
+
+def test_tubes_c1_isosurface_full(ctx):
+    w = wl.tubes_c1()
+    c = Case(ctx, w.voxels(), w.block_size, w.padding)
+    try:
+        v = w.views[0]
+        g, r, _, _ = c.render_both(wl.make_camera(v.camera), v.width, v.height, **w.params)
+        assert_parity(g, r, what="config 1 isosurface")
+        for mode in ("Volume", "Solid"):
+            g, r, _, _ = c.render_both(wl.make_camera(v.camera), v.width, v.height,
+                                       shader="Blocks", mode=mode, density=1e-2, composite=True)
+            assert_parity(g, r, what=f"config 1 blocks {mode}")
+    finally:
+        c.close()
