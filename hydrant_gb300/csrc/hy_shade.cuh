@@ -21,6 +21,15 @@ __device__ __forceinline__ float gmax(float a, float b) { return (a < b) ? b : a
 __device__ __forceinline__ int iclamp(int x, int lo, int hi) { return min(max(x, lo), hi); }
 __device__ __forceinline__ float fclamp(float x, float lo, float hi) { return gmin(gmax(x, lo), hi); }
 __device__ __forceinline__ float fsign(float x) { return float((0.f < x) - (x < 0.f)); }
+// float -> int: truncation, saturating, NaN -> 0 (the hardware conversion;
+// the oracle defines the same, C++ leaves these cases undefined).
+__device__ __forceinline__ int f2i(float x) { return int(x); }
+// Steps skipped over empty bricks.  The reference's value is a small
+// non-negative integer; NaN / negative / huge (degenerate rays only) are
+// pinned to [0, 2^30] so nsteps can never overflow and the loop always ends.
+__device__ __forceinline__ int skip_count(float di) {
+    return (di >= 0.f) ? (di < 1073741824.f ? int(di) : 1073741824) : 0;
+}
 
 // IPixel + StdVec4Pixel + shader extras (shader.hpp:26-34,
 // pixel_template.hpp:11-20, volume_shader.hpp:11-15, isosurface_shader.hpp:11-15).
@@ -68,7 +77,7 @@ __device__ __forceinline__ int skip_nblock_steps(Px &p, float rx, float ry, floa
     p.ox = p.ox + (p.dx * di) * step;
     p.oy = p.oy + (p.dy * di) * step;
     p.oz = p.oz + (p.dz * di) * step;
-    return int(di);
+    return skip_count(di);
 }
 
 // A resident brick: BlockSampler {storage, mapping} (block_paging.hpp:24-36).

@@ -75,8 +75,9 @@ __global__ void brick_stats_kernel(const T *__restrict__ raw, int dx, int dy, in
 template <typename T>
 __global__ void brick_fill_kernel(const T *__restrict__ raw, int dx, int dy, int dz, int bs,
                                   int pad, int gx, int gy, const int *__restrict__ slot_brick,
-                                  unsigned char *__restrict__ pool, long long slot_stride) {
-    const int slot = blockIdx.y;
+                                  unsigned char *__restrict__ pool, long long slot_stride,
+                                  int slot0) {
+    const int slot = slot0 + blockIdx.y;
     const int bid = slot_brick[slot];
     const int bx = bid % gx, by = (bid / gx) % gy, bz = bid / (gx * gy);
     const int P = bs + 2 * pad;
@@ -204,11 +205,14 @@ int upload_impl(hy_volume *vol, const void *host) {
         HY_UP(cudaMemcpyAsync(slot_brick_dev, slot_brick.data(), slot_brick.size() * sizeof(int),
                               cudaMemcpyHostToDevice, ctx->stream));
         const long long P3 = (long long)vol->P * vol->P * vol->P;
-        dim3 grid(unsigned((P3 + 255) / 256 < 512 ? (P3 + 255) / 256 : 512), vol->resident);
-        brick_fill_kernel<T><<<grid, 256, 0, ctx->stream>>>(
-            raw, d.dim[0], d.dim[1], d.dim[2], d.block_size, d.padding, vol->grid[0],
-            vol->grid[1], slot_brick_dev, vol->pool, (long long)vol->slot_stride);
-        HY_UP(cudaGetLastError());
+        for (int s0 = 0; s0 < vol->resident; s0 += 65535) {
+            const int n = std::min(65535, vol->resident - s0);
+            dim3 grid(unsigned((P3 + 255) / 256 < 512 ? (P3 + 255) / 256 : 512), unsigned(n));
+            brick_fill_kernel<T><<<grid, 256, 0, ctx->stream>>>(
+                raw, d.dim[0], d.dim[1], d.dim[2], d.block_size, d.padding, vol->grid[0],
+                vol->grid[1], slot_brick_dev, vol->pool, (long long)vol->slot_stride, s0);
+            HY_UP(cudaGetLastError());
+        }
     }
     std::vector<int2> info(nb);
     for (int i = 0; i < nb; ++i) info[i] = make_int2(vol->cheb[i], vol->reg_of_brick[i]);

@@ -54,6 +54,21 @@ inline F3 cross(F3 a, F3 b) {
 inline float comp_max(F3 a) { return gmax(gmax(a.x, a.y), a.z); }
 inline float comp_min(F3 a) { return gmin(gmin(a.x, a.y), a.z); }
 inline float fsign(float x) { return float((0.f < x) - (x < 0.f)); }
+// float -> int conversion, defined for every input: truncation toward zero,
+// saturating at the int range, NaN -> 0.  C++ leaves NaN / out-of-range
+// undefined; this is what the GPU conversion instruction does.
+inline int f2i(float x) {
+    if (x != x) return 0;
+    if (x >= 2147483648.f) return 2147483647;
+    if (x <= -2147483648.f) return (-2147483647 - 1);
+    return int(x);
+}
+// Steps skipped over empty bricks: the reference's value is a small
+// non-negative integer; degenerate (NaN / negative / huge) values are pinned
+// to [0, 2^30] so nsteps cannot overflow.
+inline int skip_count(float di) {
+    return (di >= 0.f) ? (di < 1073741824.f ? int(di) : 1073741824) : 0;
+}
 
 // Column-major 4x4: m[c*4 + r].
 struct M4 {
@@ -473,9 +488,9 @@ inline int thumb_index(const orc_volume *v, F3 x) {
     float fx = fclamp(x.x, 0.f, float(v->grid[0]));
     float fy = fclamp(x.y, 0.f, float(v->grid[1]));
     float fz = fclamp(x.z, 0.f, float(v->grid[2]));
-    int ix = iclamp(int(std::floor(fx)), 0, v->grid[0] - 1);
-    int iy = iclamp(int(std::floor(fy)), 0, v->grid[1] - 1);
-    int iz = iclamp(int(std::floor(fz)), 0, v->grid[2] - 1);
+    int ix = iclamp(f2i(std::floor(fx)), 0, v->grid[0] - 1);
+    int iy = iclamp(f2i(std::floor(fy)), 0, v->grid[1] - 1);
+    int iz = iclamp(f2i(std::floor(fz)), 0, v->grid[2] - 1);
     return (iz * v->grid[1] + iy) * v->grid[0] + ix;
 }
 
@@ -496,10 +511,10 @@ float sample_brick(const orc_volume *v, int pgid, F3 x) {
     F3 u = f3(fx.x - .5f, fx.y - .5f, fx.z - .5f);
     F3 flr = floor3(u);
     F3 a = sub(u, flr);
-    int ix = iclamp(int(flr.x), 0, P - 1), iy = iclamp(int(flr.y), 0, P - 1),
-        iz = iclamp(int(flr.z), 0, P - 1);
-    int jx = iclamp(int(std::ceil(u.x)), 0, P - 1), jy = iclamp(int(std::ceil(u.y)), 0, P - 1),
-        jz = iclamp(int(std::ceil(u.z)), 0, P - 1);
+    int ix = iclamp(f2i(flr.x), 0, P - 1), iy = iclamp(f2i(flr.y), 0, P - 1),
+        iz = iclamp(f2i(flr.z), 0, P - 1);
+    int jx = iclamp(f2i(std::ceil(u.x)), 0, P - 1), jy = iclamp(f2i(std::ceil(u.y)), 0, P - 1),
+        jz = iclamp(f2i(std::ceil(u.z)), 0, P - 1);
     auto at = [&](int X, int Y, int Z) { return data[(size_t(Z) * P + Y) * P + X]; };
     float x0_0 = lerp(at(ix, iy, iz), at(jx, iy, iz), a.x);
     float x1_0 = lerp(at(ix, jy, iz), at(jx, jy, iz), a.x);
@@ -519,8 +534,8 @@ F4 sample_tf(const Ctx &c, float s) {
     float u = fx - .5f;
     float flr = std::floor(u);
     float a = u - flr;
-    int ix = iclamp(int(flr), 0, c.ntf - 1);
-    int jx = iclamp(int(std::ceil(u)), 0, c.ntf - 1);
+    int ix = iclamp(f2i(flr), 0, c.ntf - 1);
+    int jx = iclamp(f2i(std::ceil(u)), 0, c.ntf - 1);
     F4 x = c.tf[ix], y = c.tf[jx];
     return F4{lerp(x.x, y.x, a), lerp(x.y, y.y, a), lerp(x.z, y.z, a), lerp(x.w, y.w, a)};
 }
@@ -531,7 +546,7 @@ int skip_nblock_steps(Ray &ray, F3 ip, int nblocks, float cdu, float step) {
     intersect(ray, ip, adds(ip, 1.f), tnear, tfar);
     float di = std::ceil((tfar + float(nblocks - 1) * cdu) / step);
     ray.o = add(ray.o, muls(muls(ray.d, di), step));
-    return int(di);
+    return skip_count(di);
 }
 
 // VolumeShaderKernel::main (volume_shader.cu:32-81)
@@ -736,7 +751,7 @@ int64_t emit(const Ctx &c, const Ray &ray_in, F3 bmin, F3 bmax, Px &px) {
         if (tnear < 0) tnear = 0;
         if (tfar < 0) tfar = 0;
         px.ray.o = add(px.ray.o, muls(px.ray.d, tnear));
-        px.nsteps = imin(c.max_steps, int((tfar - tnear) / c.step));
+        px.nsteps = imin(c.max_steps, f2i((tfar - tnear) / c.step));
         px.step_size = 1;
         return run_main(c, px);
     }
@@ -865,9 +880,9 @@ void for_each_brick(const Ctx &c, const Ray &r, F &&fn) {
     if (!(t1 > t0)) return;
     const orc_volume *v = c.vol;
     F3 p = add(r.o, muls(r.d, t0));
-    int cell[3] = {iclamp(int(std::floor(p.x)), 0, v->grid[0] - 1),
-                   iclamp(int(std::floor(p.y)), 0, v->grid[1] - 1),
-                   iclamp(int(std::floor(p.z)), 0, v->grid[2] - 1)};
+    int cell[3] = {iclamp(f2i(std::floor(p.x)), 0, v->grid[0] - 1),
+                   iclamp(f2i(std::floor(p.y)), 0, v->grid[1] - 1),
+                   iclamp(f2i(std::floor(p.z)), 0, v->grid[2] - 1)};
     float d[3] = {r.d.x, r.d.y, r.d.z}, o[3] = {r.o.x, r.o.y, r.o.z};
     int stp[3];
     float tmax[3], tdelta[3];
