@@ -11,9 +11,11 @@ resolutions drawn from {256^2, 512^2, 1024^2, 2048^2}, Volume shader, the
 64 views.  Metric: Gsamples/s (brick trilinear samples per second); views/s
 is reported beside it.
 
---impl ours       the GB300 path: one hy_render_device launch per view;
-                  `e2e` goes through hy_render with host buffers (host ->
-                  device view/params, device -> host RGBA per view).
+--impl ours       the GB300 path: all views of a step in one persistent
+                  launch replayed from a CUDA graph (hy_batch); the plain
+                  per-view path (one hy_render_device launch per view) is
+                  timed beside it.  `e2e` goes through hy_batch_render with a
+                  host output buffer (device -> host images inside the timing).
 --impl reference  the reference's own CPU multi-thread backend for this path
                   (restated in oracle/, the reference cannot be built here)
                   on all host threads, on a bounded sample of the workload.
@@ -53,6 +55,8 @@ def parse_args():
     ap.add_argument("--res", type=int, default=0,
                     help="keep only the views of this resolution (profiling a small case)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="use the default batch launch shape (profiling)")
     ap.add_argument("--cpu-sample-rows", type=int, default=0,
                     help="rows of the CPU-baseline sample (0 = auto)")
     return ap.parse_args()
@@ -234,6 +238,21 @@ def main_reference(args):
     return 0
 
 
+def _timed_steps(torch, stream, steps, fn, flush=None):
+    """Run `steps` calls of fn, each bracketed by CUDA events on `stream`;
+    a flush buffer (if any) is written between steps outside the events."""
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(steps)]
+    for k in range(steps):
+        if flush is not None:
+            with torch.cuda.stream(stream):
+                flush.fill_(k & 0xFF)
+        evs[k][0].record(stream)
+        fn()
+        evs[k][1].record(stream)
+    return evs
+
+
 def main_ours(args):
     import numpy as np
     import torch
@@ -246,8 +265,10 @@ def main_ours(args):
     torch.cuda.set_device(local)
     build_all()
     import hydrant_gb300 as hy
+    from hydrant_gb300 import autotune
     from hydrant_gb300 import workloads as wl
 
+    dev = f"cuda:{local}"
     w = workload(args)
     t0 = time.perf_counter()
     vox = w.voxels()
@@ -259,7 +280,7 @@ def main_ours(args):
     ctx.set_transfer_fn(w.tf)
     info = vol.info
 
-    views, params, bufs = [], [], []
+    views, params, lighting, bufs = [], [], [], []
     for v in w.views:
         cam = wl.make_camera(v.camera)
         p = hy.shader_params(**w.params)
@@ -267,93 +288,97 @@ def main_ours(args):
             hy.iso_lighting(vol, cam, p)
         views.append((hy.camera_view(vol, cam), v.width, v.height))
         params.append(p)
-        bufs.append(torch.empty(v.height * v.width * 4, dtype=torch.uint8, device=f"cuda:{local}"))
+        lighting.append((list(p.eye_pos), list(p.light_pos)))
+        bufs.append(torch.empty(v.height * v.width * 4, dtype=torch.uint8, device=dev))
     npix = sum(W * H for _, W, H in views)
-
-    # brick samples per step (deterministic; counted once, outside the timed region)
-    samples = 0
-    for (view, W, H), p, b in zip(views, params, bufs):
-        pc = hy.shader_params(**w.params, count_samples=True)
-        if pc.shader == hy._abi.SHADER_ISOSURFACE:
-            pc = p
-            pc.count_samples = 1
-        hy.render_device(ctx, vol, pc, view, W, H, b.data_ptr())
-        samples += ctx.stats().samples
-        if pc is p:
-            p.count_samples = 0
-
     stream = torch.cuda.ExternalStream(ctx.stream)
-
-    def step(evs=None):
-        for i, ((view, W, H), p, b) in enumerate(zip(views, params, bufs)):
-            if evs is not None:
-                evs[i][0].record(stream)
-            hy.render_device(ctx, vol, p, view, W, H, b.data_ptr())
-            if evs is not None:
-                evs[i][1].record(stream)
-
-    for _ in range(args.warmup):
-        step()
-    ctx.synchronize()
-    torch.cuda.synchronize()
-    if ws > 1:
-        torch.distributed.barrier()
     # L2 is 129 MB: when the brick pool is smaller, a 512 MB buffer is written
     # between timed steps (outside the timed events) so every step starts cold.
     flush = None
     if info.pool_bytes < 256 * 2**20:
-        flush = torch.empty(512 * 2**20, dtype=torch.uint8, device=f"cuda:{local}")
+        flush = torch.empty(512 * 2**20, dtype=torch.uint8, device=dev)
+
+    # ---- plain per-view path: one fused launch per view -------------------
+    samples = 0
+    for (view, W, H), p, b in zip(views, params, bufs):
+        p.count_samples = 1
+        hy.render_device(ctx, vol, p, view, W, H, b.data_ptr())
+        samples += ctx.stats().samples
+        p.count_samples = 0
+
+    def plain_step():
+        for (view, W, H), p, b in zip(views, params, bufs):
+            hy.render_device(ctx, vol, p, view, W, H, b.data_ptr())
+
+    for _ in range(args.warmup):
+        plain_step()
+    ctx.synchronize()
+    evs = _timed_steps(torch, stream, args.steps, plain_step, flush)
+    ctx.synchronize()
+    t_plain = sum(a.elapsed_time(b) for a, b in evs) / 1e3
+
+    # ---- batched path: one persistent launch per step, graph replay -------
+    batch = hy.Batch(ctx, vol, params[0], views, lighting)
+    out = torch.empty(batch.nbytes, dtype=torch.uint8, device=dev)
+    key = autotune.signature(torch.cuda.get_device_name(local), params[0], vol.desc,
+                             [(W, H) for _, W, H in views])
+    if args.no_autotune:
+        c = batch.config
+        tuned = {"tile_w": c.tile_w, "grab": c.grab, "block_warps": c.block_warps,
+                 "blocks_per_sm": c.blocks_per_sm, "source": "default"}
+    else:
+        tuned = autotune.tuned_config(batch, key, out.data_ptr(), reps=1)
+    batch.set_counting(True)
+    batch.render_device(out.data_ptr())
+    samples_b = ctx.stats().samples
+    batch.set_counting(False)
+    # the batch reproduces the per-view images exactly
+    ref = np.concatenate([b.cpu().numpy() for b in bufs])
+    same = bool(np.array_equal(out.cpu().numpy()[: ref.size], ref))
+
+    for _ in range(args.warmup):
+        batch.render_device(out.data_ptr())
+    ctx.synchronize()
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
     clocks = Clocks(local)
     clocks.start()
-    launch_ev = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-                  for _ in views] for _ in range(args.steps)]
-    step_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-               for _ in range(args.steps)]
-    torch.cuda.synchronize()
-    for k in range(args.steps):
-        if flush is not None:
-            with torch.cuda.stream(stream):
-                flush.fill_(k & 0xFF)
-        step_ev[k][0].record(stream)
-        step(launch_ev[k])
-        step_ev[k][1].record(stream)
+    evs = _timed_steps(torch, stream, args.steps, lambda: batch.render_device(out.data_ptr()), flush)
     ctx.synchronize()
     torch.cuda.synchronize()
     ck = clocks.stop()
-    t = sum(a.elapsed_time(b) for a, b in step_ev) / 1e3
-    kernel_ms = [a.elapsed_time(b) for evs in launch_ev for a, b in evs]
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    t = sum(step_ms) / 1e3
     if ws > 1:
-        tt = torch.tensor([t], device=f"cuda:{local}")
+        tt = torch.tensor([t, t_plain], device=dev)
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t = float(tt.item())
+        t, t_plain = float(tt[0].item()), float(tt[1].item())
         torch.distributed.barrier()
 
-    # e2e through the host-buffer entry point
+    # ---- e2e: the host-buffer entry point (device -> host images per step) --
+    host = np.empty(batch.nbytes, np.uint8)
     for _ in range(max(1, args.warmup // 2)):
-        for (view, W, H), p in zip(views, params):
-            hy.render(ctx, vol, p, view, W, H)
+        batch.render()
     if ws > 1:
         torch.distributed.barrier()
     te = time.perf_counter()
     for _ in range(args.steps):
-        for (view, W, H), p in zip(views, params):
-            hy.render(ctx, vol, p, view, W, H)
+        hy.lib().hy_batch_render(batch.handle, host.ctypes.data_as(ctypes.c_void_p))
+    ctx.synchronize()
     t_e2e = time.perf_counter() - te
     if ws > 1:
-        tt = torch.tensor([t_e2e], device=f"cuda:{local}")
+        tt = torch.tensor([t_e2e], device=dev)
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
         t_e2e = float(tt.item())
 
     value = samples * ws * args.steps / t / 1e9
+    plain_value = samples * ws * args.steps / t_plain / 1e9
     e2e = samples * ws * args.steps / t_e2e / 1e9
-    views_per_s = len(views) * ws * args.steps / t
     hbm, peak_kind = measured_peaks()
-    # dominant kernel: the fused render kernel, one launch per view
-    mean_launch_s = (sum(kernel_ms) / len(kernel_ms)) / 1e3
-    bytes_per_launch = samples / len(views) * BYTES_PER_SAMPLE
-    achieved = bytes_per_launch / mean_launch_s / 1e9
+    mean_launch_s = t / args.steps  # one batch kernel per step
+    achieved = samples * BYTES_PER_SAMPLE / mean_launch_s / 1e9
     tps = profile_traffic_per_sample()
-    out = None
     if rank == 0:
         cpu = None
         if not args.no_cpu_baseline:
@@ -364,7 +389,7 @@ def main_ours(args):
             cpu = {"value": s / dt / 1e9, "unit": "Gsamples/s", "cores": nth, "kind": "port",
                    "sample": f"rows {y0}..{y1} of the {view.width}x{view.height} view, {s} samples, "
                              f"{dt:.2f} s"}
-        out = {
+        out_json = {
             "metric": "Gsamples/s",
             "value": value,
             "unit": "Gsamples/s",
@@ -382,27 +407,36 @@ def main_ours(args):
                 "volume": list(w.dim), "block_size": w.block_size, "padding": w.padding,
                 "views": len(views), "pixels_per_step": npix,
                 "samples_per_step": samples,
-                "path": "plain per-view (one fused launch per view)",
+                "path": "batched: one persistent launch per step from a CUDA graph",
+                "launch_shape": tuned,
                 "l2": ("inputs larger than L2 (brick pool %.2f GB)" % (info.pool_bytes / 1e9))
                       if flush is None else
                       ("L2 flushed between timed steps (brick pool %.1f MB)" % (info.pool_bytes / 1e6)),
             },
-            "views_per_s": views_per_s,
+            "views_per_s": len(views) * ws * args.steps / t,
+            "plain": {"value": plain_value, "unit": "Gsamples/s",
+                      "views_per_s": len(views) * ws * args.steps / t_plain,
+                      "ms_per_step": t_plain / args.steps * 1e3,
+                      "path": "one fused hy_render_device launch per view"},
+            "batched_over_plain": t_plain / t,
+            "batch_matches_plain": same and samples_b == samples,
             "e2e": {"value": e2e, "unit": "Gsamples/s",
-                    "h2d_bytes_per_step": len(views) * (ctypes.sizeof(hy._abi.HyView) + ctypes.sizeof(hy._abi.HyShaderParams)),
-                    "d2h_bytes_per_step": npix * 4},
+                    "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": batch.nbytes,
+                    "path": "hy_batch_render (host output buffer)"},
             "roofline": {
                 "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": achieved / hbm, "peak_kind": peak_kind,
-                "traffic": (tps * samples / len(views)) if tps else None,
-                "note": "8 B/sample algorithmic footprint; the kernel is L1/issue bound",
+                "traffic": (tps * samples) if tps else None,
+                "note": "8 B/sample algorithmic footprint; the kernel is issue bound",
             },
             "cpu_baseline": cpu,
-            "gpu_launches": args.steps * len(views),
+            "gpu_launches": args.steps,
             "clocks": ck,
             "setup_s": {"generate": t_gen, "upload_and_brick": t_up},
         }
-        print(json.dumps(out), flush=True)
+        print(json.dumps(out_json), flush=True)
+    batch.close()
     vol.close()
     ctx.close()
     if ws > 1:

@@ -7,6 +7,7 @@ tests, the benchmark and the renderer-interface mirror.
 
 from ._abi import HydrantError, lib  # noqa: F401
 from .api import (  # noqa: F401
+    Batch,
     Context,
     RenderResult,
     Volume,

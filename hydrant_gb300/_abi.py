@@ -78,6 +78,26 @@ class HyVolumeInfo(C.Structure):
     ]
 
 
+class HyBatchView(C.Structure):
+    _fields_ = [
+        ("view", HyView),
+        ("width", C.c_int32),
+        ("height", C.c_int32),
+        ("rgba_offset", C.c_int64),
+        ("eye_pos", f3),
+        ("light_pos", f3),
+    ]
+
+
+class HyBatchConfig(C.Structure):
+    _fields_ = [
+        ("tile_w", C.c_int32),
+        ("grab", C.c_int32),
+        ("block_warps", C.c_int32),
+        ("blocks_per_sm", C.c_int32),
+    ]
+
+
 class HyRenderStats(C.Structure):
     _fields_ = [("samples", C.c_int64), ("pixels", C.c_int64), ("ms", C.c_float)]
 
@@ -112,6 +132,18 @@ _PROTOS = {
         C.c_int,
         [P, P, C.POINTER(HyShaderParams), C.c_int32, C.POINTER(HyView), P, C.c_int32, C.c_int32, P, P],
     ),
+    "hy_batch_create": (
+        C.c_int,
+        [P, P, C.POINTER(HyShaderParams), C.POINTER(HyBatchView), C.c_int32, C.POINTER(P)],
+    ),
+    "hy_batch_destroy": (C.c_int, [P]),
+    "hy_batch_output_bytes": (C.c_int, [P, C.POINTER(C.c_int64)]),
+    "hy_batch_set_config": (C.c_int, [P, C.POINTER(HyBatchConfig)]),
+    "hy_batch_get_config": (C.c_int, [P, C.POINTER(HyBatchConfig)]),
+    "hy_batch_set_counting": (C.c_int, [P, C.c_int32]),
+    "hy_batch_render_device": (C.c_int, [P, P]),
+    "hy_batch_render": (C.c_int, [P, P]),
+    "hy_batch_autotune": (C.c_int, [P, P, C.c_int32, C.POINTER(HyBatchConfig)]),
     "hy_synth_blobs_u8": (C.c_int, [C.c_uint64, P, C.c_int32, P, C.c_int32]),
     "hy_synth_blobs_f32": (C.c_int, [C.c_uint64, P, C.c_int32, P, C.c_int32]),
     "hy_synth_tubes_u8": (C.c_int, [C.c_uint64, P, C.c_int32, P, C.c_int32]),

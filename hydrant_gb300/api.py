@@ -10,6 +10,8 @@ import numpy as np
 
 from . import _abi
 from ._abi import (
+    HyBatchConfig,
+    HyBatchView,
     HyCamera,
     HyRenderStats,
     HyShaderParams,
@@ -260,3 +262,68 @@ def synth_tubes_u8(seed: int, dim, ntubes: int, nthreads: int = 0) -> np.ndarray
     d = (C.c_int32 * 3)(nx, ny, nz)
     check(lib().hy_synth_tubes_u8(seed, C.cast(d, C.c_void_p), ntubes, _ptr(out), nthreads))
     return out
+
+
+class Batch:
+    """Many views in one persistent launch replayed from a CUDA graph (hy_batch)."""
+
+    def __init__(self, ctx: Context, vol: Volume, params: HyShaderParams, views, lighting=None):
+        """views: list of (HyView, width, height); lighting: optional list of
+        (eye_pos, light_pos) per view for the Isosurface shader."""
+        self.ctx = ctx
+        n = len(views)
+        arr = (HyBatchView * n)()
+        off = 0
+        self.offsets = []
+        self.sizes = []
+        for i, (v, W, H) in enumerate(views):
+            arr[i].view = v
+            arr[i].width = W
+            arr[i].height = H
+            arr[i].rgba_offset = off
+            if lighting is not None:
+                arr[i].eye_pos = (C.c_float * 3)(*lighting[i][0])
+                arr[i].light_pos = (C.c_float * 3)(*lighting[i][1])
+            self.offsets.append(off)
+            self.sizes.append((W, H))
+            off += W * H * 4
+        h = C.c_void_p()
+        ctx.check(lib().hy_batch_create(ctx.handle, vol.handle, C.byref(params), arr, n, C.byref(h)))
+        self.handle = h
+        nb = C.c_int64()
+        ctx.check(lib().hy_batch_output_bytes(self.handle, C.byref(nb)))
+        self.nbytes = int(nb.value)
+
+    def close(self) -> None:
+        if self.handle:
+            lib().hy_batch_destroy(self.handle)
+            self.handle = None
+
+    @property
+    def config(self) -> HyBatchConfig:
+        c = HyBatchConfig()
+        self.ctx.check(lib().hy_batch_get_config(self.handle, C.byref(c)))
+        return c
+
+    def set_config(self, tile_w=8, grab=2, block_warps=4, blocks_per_sm=0) -> None:
+        c = HyBatchConfig(tile_w, grab, block_warps, blocks_per_sm)
+        self.ctx.check(lib().hy_batch_set_config(self.handle, C.byref(c)))
+
+    def set_counting(self, on: bool) -> None:
+        self.ctx.check(lib().hy_batch_set_counting(self.handle, int(bool(on))))
+
+    def render_device(self, rgba_ptr: int) -> None:
+        self.ctx.check(lib().hy_batch_render_device(self.handle, C.c_void_p(rgba_ptr)))
+
+    def render(self) -> list:
+        out = np.empty(self.nbytes, np.uint8)
+        self.ctx.check(lib().hy_batch_render(self.handle, _ptr(out)))
+        return self.split(out)
+
+    def split(self, flat: np.ndarray) -> list:
+        return [flat[o:o + W * H * 4].reshape(H, W, 4) for o, (W, H) in zip(self.offsets, self.sizes)]
+
+    def autotune(self, rgba_ptr: int, reps: int = 3) -> HyBatchConfig:
+        c = HyBatchConfig()
+        self.ctx.check(lib().hy_batch_autotune(self.handle, C.c_void_p(rgba_ptr), reps, C.byref(c)))
+        return c

@@ -1,0 +1,431 @@
+// hy_batch.cu -- many views, one persistent launch, replayed from a CUDA graph.
+//
+// The reference renders one view per Raycaster pass (raycaster.hpp:32-54):
+// each view is its own launch, and small views leave most SMs idle while the
+// last wave of a big view drains.  Here every view of a batch is cut into
+// warp ray tiles (32 rays: 8x4, 4x8, 16x2 or 32x1 pixels), all tiles of all
+// views form one queue, and a persistent grid sized to the GPU takes tiles
+// from it (one atomicAdd per `grab` tiles per warp) until it is empty.  A
+// tile's rays are shaded exactly as in the single-view kernel, so images are
+// identical to the per-view path.  The queue head is the only scratch memory;
+// the {queue reset, kernel} pair is captured once into a CUDA graph and
+// replayed per batch.
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "hy_shade.cuh"
+
+using namespace hy;
+using namespace hy::dev;
+
+namespace {
+
+struct BatchView {
+    ViewArgs view;
+    long long out_off;  // byte offset of the view's RGBA8 image
+    int tiles_x;
+    int tile0;          // first queue index of this view
+};
+
+struct BatchArgs {
+    ShadeArgs A;
+    const BatchView *views;
+    const int *starts;  // tile0 of every view, ascending
+    int nviews;
+    int total_tiles;
+    int tile_w, tile_h, grab;
+    unsigned int *queue;
+    unsigned char *out;
+};
+
+constexpr int kMaxViews = 2048;
+constexpr int kMaxBlockThreads = 256;
+
+template <int SHADER, int PC, int DT, bool PADDED, int COMPOSITE>
+__global__ void __launch_bounds__(kMaxBlockThreads)
+    batch_kernel(const __grid_constant__ BatchArgs B) {
+    extern __shared__ float4 smem[];
+    const ShadeArgs &A = B.A;
+    float4 *tf = smem;
+    float *lut = reinterpret_cast<float *>(smem + A.ntf);
+    int *starts = reinterpret_cast<int *>(lut + 256);
+    for (int i = threadIdx.x; i < A.ntf; i += blockDim.x) tf[i] = A.tf[i];
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) lut[i] = float(i) / 255.f;
+    for (int i = threadIdx.x; i < B.nviews; i += blockDim.x) starts[i] = B.starts[i];
+    __syncthreads();
+    const Shared S{tf, A.ntf, float(A.ntf), lut};
+    const int lane = threadIdx.x & 31;
+    const int lx = lane % B.tile_w, ly = lane / B.tile_w;
+    long long samples = 0;
+    for (;;) {
+        unsigned int t0 = 0;
+        if (lane == 0) t0 = atomicAdd(B.queue, unsigned(B.grab));
+        t0 = __shfl_sync(0xffffffffu, t0, 0);
+        if (t0 >= unsigned(B.total_tiles)) break;
+        for (int g = 0; g < B.grab; ++g) {
+            const int t = int(t0) + g;
+            if (t >= B.total_tiles) break;
+            int lo = 0, hi = B.nviews - 1;  // last view with starts[v] <= t
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (starts[mid] <= t)
+                    lo = mid;
+                else
+                    hi = mid - 1;
+            }
+            const BatchView &bv = B.views[lo];
+            const int local = t - starts[lo];
+            const int ty = local / bv.tiles_x, tx = local - ty * bv.tiles_x;
+            const int x = tx * B.tile_w + lx, y = ty * B.tile_h + ly;
+            if (x < bv.view.W && y < bv.view.H) {
+                float ox, oy, oz, dx, dy, dz;
+                gen_ray(bv.view, x, y, ox, oy, oz, dx, dy, dz);
+                float4 v;
+                if (COMPOSITE) {
+                    float4 aux;
+                    samples += composite_ray<SHADER, PC, DT, PADDED>(A, bv.view, S, ox, oy, oz,
+                                                                     dx, dy, dz, v, aux);
+                } else {
+                    Px p;
+                    samples += emit<SHADER, PC, DT, PADDED>(p, A, bv.view, S, ox, oy, oz, dx, dy,
+                                                            dz, 0.f, 0.f, 0.f, A.bbox_max[0],
+                                                            A.bbox_max[1], A.bbox_max[2]);
+                    v = make_float4(p.vx, p.vy, p.vz, p.vw);
+                }
+                uchar4 q;
+                if (v.w != 0.f)
+                    q = make_uchar4(saturate_u8(v.x), saturate_u8(v.y), saturate_u8(v.z),
+                                    saturate_u8(v.w));
+                else
+                    q = make_uchar4(A.clear_u8[0], A.clear_u8[1], A.clear_u8[2], 0);
+                *reinterpret_cast<uchar4 *>(B.out + bv.out_off +
+                                            (size_t(y) * bv.view.W + x) * 4) = q;
+            }
+        }
+    }
+    if (A.count) {
+        unsigned long long s = (unsigned long long)samples;
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if (lane == 0 && s) atomicAdd(A.counter, s);
+    }
+}
+
+template <int SHADER, int PC, int DT, bool PADDED>
+const void *pick_c(int composite) {
+    if (composite) return reinterpret_cast<const void *>(&batch_kernel<SHADER, PC, DT, PADDED, 1>);
+    return reinterpret_cast<const void *>(&batch_kernel<SHADER, PC, DT, PADDED, 0>);
+}
+
+template <int SHADER>
+const void *pick_shader(const ShadeArgs &a) {
+    if constexpr (SHADER == HY_SHADER_BLOCKS) {
+        return pick_c<SHADER, 0, HY_DTYPE_U8, false>(a.composite);
+    } else {
+        const bool padded = a.vol.pad > 0;
+        if (a.vol.dtype == HY_DTYPE_F32)
+            return padded ? pick_c<SHADER, 0, HY_DTYPE_F32, true>(a.composite)
+                          : pick_c<SHADER, 0, HY_DTYPE_F32, false>(a.composite);
+        if (padded && a.vol.P == 66) return pick_c<SHADER, 66, HY_DTYPE_U8, true>(a.composite);
+        if (padded && a.vol.P == 130) return pick_c<SHADER, 130, HY_DTYPE_U8, true>(a.composite);
+        return padded ? pick_c<SHADER, 0, HY_DTYPE_U8, true>(a.composite)
+                      : pick_c<SHADER, 0, HY_DTYPE_U8, false>(a.composite);
+    }
+}
+
+const void *pick_kernel(const ShadeArgs &a) {
+    switch (a.shader) {
+        case HY_SHADER_VOLUME:
+            return pick_shader<HY_SHADER_VOLUME>(a);
+        case HY_SHADER_BLOCKS:
+            return pick_shader<HY_SHADER_BLOCKS>(a);
+        default:
+            return pick_shader<HY_SHADER_ISOSURFACE>(a);
+    }
+}
+
+}  // namespace
+
+struct hy_batch {
+    hy_ctx *ctx = nullptr;
+    const hy_volume *vol = nullptr;
+    hy_shader_params params{};
+    std::vector<hy_batch_view> in;
+    std::vector<BatchView> views;
+    std::vector<int> starts;
+    BatchView *views_dev = nullptr;
+    int *starts_dev = nullptr;
+    unsigned int *queue_dev = nullptr;
+    int total_tiles = 0;
+    int64_t out_bytes = 0;
+    hy_batch_config cfg{8, 2, 4, 0};
+    ShadeArgs base{};
+    const void *kernel = nullptr;
+    size_t smem = 0;
+    int grid = 0;
+    cudaGraphExec_t exec = nullptr;
+    uint8_t *graph_out = nullptr;
+    int graph_count = -1;
+};
+
+namespace {
+
+bool valid_config(const hy_batch_config &c) {
+    const bool tw = c.tile_w == 4 || c.tile_w == 8 || c.tile_w == 16 || c.tile_w == 32;
+    return tw && c.grab >= 1 && c.grab <= 16 && c.block_warps >= 1 &&
+           c.block_warps * 32 <= kMaxBlockThreads && c.blocks_per_sm >= 0 && c.blocks_per_sm <= 32;
+}
+
+void drop_graph(hy_batch *b) {
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+    b->graph_out = nullptr;
+    b->graph_count = -1;
+}
+
+// (Re)build the tile layout for the current config and the persistent grid.
+int layout(hy_batch *b) {
+    hy_ctx *ctx = b->ctx;
+    const int tw = b->cfg.tile_w, th = 32 / tw;
+    b->views.resize(b->in.size());
+    b->starts.resize(b->in.size());
+    long long tile = 0;
+    for (size_t i = 0; i < b->in.size(); ++i) {
+        const hy_batch_view &v = b->in[i];
+        BatchView &d = b->views[i];
+        std::memset(&d, 0, sizeof(d));
+        std::memcpy(d.view.trans, v.view.trans, sizeof(d.view.trans));
+        d.view.ctg = v.view.ctg_fovy_2;
+        for (int k = 0; k < 3; ++k) {
+            d.view.ray_o[k] = v.view.ray_o[k];
+            d.view.eye[k] = v.eye_pos[k];
+            d.view.light[k] = v.light_pos[k];
+        }
+        d.view.W = v.width;
+        d.view.H = v.height;
+        d.out_off = v.rgba_offset;
+        d.tiles_x = (v.width + tw - 1) / tw;
+        d.tile0 = int(tile);
+        b->starts[i] = int(tile);
+        tile += (long long)d.tiles_x * ((v.height + th - 1) / th);
+    }
+    if (tile >= (1ll << 31) - 64) return hy_fail(ctx, HY_ERR_INVALID, "batch: too many ray tiles");
+    b->total_tiles = int(tile);
+    HY_CUDA(ctx, cudaMemcpyAsync(b->views_dev, b->views.data(), b->views.size() * sizeof(BatchView),
+                                 cudaMemcpyHostToDevice, ctx->stream));
+    HY_CUDA(ctx, cudaMemcpyAsync(b->starts_dev, b->starts.data(), b->starts.size() * sizeof(int),
+                                 cudaMemcpyHostToDevice, ctx->stream));
+    HY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    b->smem = size_t(b->base.ntf) * sizeof(float4) + 256 * sizeof(float) + b->in.size() * sizeof(int);
+    const int threads = b->cfg.block_warps * 32;
+    int per_sm = b->cfg.blocks_per_sm;
+    if (per_sm == 0) {
+        HY_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, b->kernel, threads,
+                                                                   b->smem));
+        per_sm = std::max(per_sm, 1);
+    }
+    int sms = 0;
+    HY_CUDA(ctx, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+    b->grid = sms * per_sm;
+    drop_graph(b);
+    return HY_OK;
+}
+
+int launch(hy_batch *b, uint8_t *out) {
+    hy_ctx *ctx = b->ctx;
+    const int count = b->params.count_samples ? 1 : 0;
+    if (!b->exec || b->graph_out != out || b->graph_count != count) {
+        drop_graph(b);
+        BatchArgs args;
+        args.A = b->base;
+        args.A.count = count;
+        args.views = b->views_dev;
+        args.starts = b->starts_dev;
+        args.nviews = int(b->views.size());
+        args.total_tiles = b->total_tiles;
+        args.tile_w = b->cfg.tile_w;
+        args.tile_h = 32 / b->cfg.tile_w;
+        args.grab = b->cfg.grab;
+        args.queue = b->queue_dev;
+        args.out = out;
+        void *kargs[] = {&args};
+        cudaGraph_t graph = nullptr;
+        HY_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        cudaMemsetAsync(b->queue_dev, 0, sizeof(unsigned int), ctx->stream);
+        if (count) cudaMemsetAsync(ctx->counter_dev, 0, sizeof(unsigned long long), ctx->stream);
+        cudaError_t le = cudaLaunchKernel(b->kernel, dim3(b->grid), dim3(b->cfg.block_warps * 32),
+                                          kargs, b->smem, ctx->stream);
+        cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
+        if (le != cudaSuccess) {
+            if (graph) cudaGraphDestroy(graph);
+            return hy_cuda_fail(ctx, le, "batch: kernel launch during capture");
+        }
+        HY_CUDA(ctx, ce);
+        cudaError_t ie = cudaGraphInstantiate(&b->exec, graph, 0);
+        cudaGraphDestroy(graph);
+        HY_CUDA(ctx, ie);
+        b->graph_out = out;
+        b->graph_count = count;
+    }
+    HY_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
+    HY_CUDA(ctx, cudaGraphLaunch(b->exec, ctx->stream));
+    HY_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
+    ctx->stats_pending = true;
+    ctx->pend_count = count;
+    int64_t px = 0;
+    for (auto &v : b->in) px += (int64_t)v.width * v.height;
+    ctx->pend_pixels = px;
+    return HY_OK;
+}
+
+}  // namespace
+
+extern "C" int hy_batch_create(hy_ctx *ctx, const hy_volume *vol, const hy_shader_params *params,
+                               const hy_batch_view *views, int32_t nviews, hy_batch **out) {
+    if (!ctx || !out) return HY_ERR_INVALID;
+    *out = nullptr;
+    if (!views || nviews <= 0 || nviews > kMaxViews)
+        return hy_fail(ctx, HY_ERR_INVALID, "batch: need 1..2048 views");
+    if (params && params->composite && params->shader == HY_SHADER_VOLUME && params->srgb) {
+        // supported: sRGB is applied per ray after compositing
+    }
+    hy::ShadeArgs base;
+    int rc = hy_fill_args(ctx, vol, params, nullptr, 1, 1, &base);
+    if (rc) return rc;
+    for (int i = 0; i < nviews; ++i) {
+        const hy_batch_view &v = views[i];
+        if (v.width <= 0 || v.height <= 0 || v.rgba_offset < 0 || (v.rgba_offset & 3))
+            return hy_fail(ctx, HY_ERR_INVALID, "batch: bad view size or output offset");
+    }
+    HY_CUDA(ctx, cudaSetDevice(ctx->device));
+    hy_batch *b = new hy_batch();
+    b->ctx = ctx;
+    b->vol = vol;
+    b->params = *params;
+    b->in.assign(views, views + nviews);
+    b->base = base;
+    b->kernel = pick_kernel(base);
+    for (auto &v : b->in)
+        b->out_bytes = std::max<int64_t>(b->out_bytes, v.rgba_offset + (int64_t)v.width * v.height * 4);
+    cudaError_t e = cudaMalloc(&b->views_dev, sizeof(BatchView) * nviews);
+    if (e == cudaSuccess) e = cudaMalloc(&b->starts_dev, sizeof(int) * nviews);
+    if (e == cudaSuccess) e = cudaMalloc(&b->queue_dev, sizeof(unsigned int));
+    if (e != cudaSuccess) {
+        hy_batch_destroy(b);
+        return hy_cuda_fail(ctx, e, "batch: allocation");
+    }
+    rc = layout(b);
+    if (rc) {
+        hy_batch_destroy(b);
+        return rc;
+    }
+    *out = b;
+    return HY_OK;
+}
+
+extern "C" int hy_batch_destroy(hy_batch *b) {
+    if (!b) return HY_OK;
+    cudaSetDevice(b->ctx->device);
+    cudaStreamSynchronize(b->ctx->stream);
+    drop_graph(b);
+    if (b->views_dev) cudaFree(b->views_dev);
+    if (b->starts_dev) cudaFree(b->starts_dev);
+    if (b->queue_dev) cudaFree(b->queue_dev);
+    delete b;
+    return HY_OK;
+}
+
+extern "C" int hy_batch_output_bytes(const hy_batch *b, int64_t *bytes) {
+    if (!b || !bytes) return HY_ERR_INVALID;
+    *bytes = b->out_bytes;
+    return HY_OK;
+}
+
+extern "C" int hy_batch_set_config(hy_batch *b, const hy_batch_config *cfg) {
+    if (!b || !cfg) return HY_ERR_INVALID;
+    if (!valid_config(*cfg)) return hy_fail(b->ctx, HY_ERR_INVALID, "batch: bad config");
+    b->cfg = *cfg;
+    return layout(b);
+}
+
+extern "C" int hy_batch_get_config(const hy_batch *b, hy_batch_config *out) {
+    if (!b || !out) return HY_ERR_INVALID;
+    *out = b->cfg;
+    return HY_OK;
+}
+
+extern "C" int hy_batch_set_counting(hy_batch *b, int32_t count_samples) {
+    if (!b) return HY_ERR_INVALID;
+    b->params.count_samples = count_samples ? 1 : 0;
+    return HY_OK;
+}
+
+extern "C" int hy_batch_render_device(hy_batch *b, uint8_t *rgba_dev) {
+    if (!b) return HY_ERR_INVALID;
+    if (!rgba_dev) return hy_fail(b->ctx, HY_ERR_INVALID, "batch: null output");
+    return launch(b, rgba_dev);
+}
+
+extern "C" int hy_batch_render(hy_batch *b, uint8_t *rgba_host) {
+    if (!b) return HY_ERR_INVALID;
+    if (!rgba_host) return hy_fail(b->ctx, HY_ERR_INVALID, "batch: null output");
+    hy_ctx *ctx = b->ctx;
+    void *stage = nullptr;
+    int rc = hy_stage(ctx, size_t(b->out_bytes), &stage);
+    if (rc) return rc;
+    rc = launch(b, static_cast<uint8_t *>(stage));
+    if (rc) return rc;
+    HY_CUDA(ctx, cudaMemcpyAsync(rgba_host, stage, size_t(b->out_bytes), cudaMemcpyDeviceToHost,
+                                 ctx->stream));
+    return hy_finish_stats(ctx);
+}
+
+// Times every candidate launch shape on this batch and keeps the fastest.
+extern "C" int hy_batch_autotune(hy_batch *b, uint8_t *rgba_dev, int32_t reps,
+                                 hy_batch_config *best_out) {
+    if (!b || !rgba_dev) return HY_ERR_INVALID;
+    hy_ctx *ctx = b->ctx;
+    if (reps <= 0) reps = 3;
+    const int tws[] = {8, 4, 16};
+    const int grabs[] = {1, 2, 4};
+    const int warps[] = {2, 4, 8};
+    const int count = b->params.count_samples;
+    b->params.count_samples = 0;
+    hy_batch_config best = b->cfg;
+    float best_ms = 1e30f;
+    cudaEvent_t e0, e1;
+    HY_CUDA(ctx, cudaEventCreate(&e0));
+    HY_CUDA(ctx, cudaEventCreate(&e1));
+    int rc = HY_OK;
+    for (int tw : tws)
+        for (int g : grabs)
+            for (int w : warps) {
+                hy_batch_config c{tw, g, w, 0};
+                b->cfg = c;
+                if ((rc = layout(b))) goto done;
+                if ((rc = launch(b, rgba_dev))) goto done;  // warm-up and graph build
+                HY_CUDA(ctx, cudaEventRecord(e0, ctx->stream));
+                for (int r = 0; r < reps; ++r)
+                    if ((rc = launch(b, rgba_dev))) goto done;
+                HY_CUDA(ctx, cudaEventRecord(e1, ctx->stream));
+                HY_CUDA(ctx, cudaEventSynchronize(e1));
+                float ms = 0.f;
+                HY_CUDA(ctx, cudaEventElapsedTime(&ms, e0, e1));
+                if (ms < best_ms) {
+                    best_ms = ms;
+                    best = c;
+                }
+            }
+done:
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    b->params.count_samples = count;
+    ctx->stats_pending = false;
+    if (rc) return rc;
+    b->cfg = best;
+    rc = layout(b);
+    if (rc) return rc;
+    if (best_out) *best_out = best;
+    return HY_OK;
+}

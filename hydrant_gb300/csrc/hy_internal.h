@@ -31,7 +31,18 @@ struct DevVolume {
     int gx, gy, gz;
     int P;      // padded brick edge
     int dtype;  // HY_DTYPE_*
-    int pad_;
+    int pad;    // apron width
+};
+
+// Per-view inputs: ViewArgs (shader.hpp:63-68) plus the image size and the
+// camera-dependent isosurface lighting (isosurface.cc:108-113).
+struct ViewArgs {
+    float trans[16];
+    float ctg;
+    float ray_o[3];
+    float eye[3];
+    float light[3];
+    int W, H;
 };
 
 // Everything one shading launch reads; passed as a __grid_constant__ kernel
@@ -50,15 +61,9 @@ struct ShadeArgs {
     float rank;
     int lowest_blkcnt;
     float to_world[16];
-    float eye[3];
-    float light[3];
     int composite, srgb, count;
     unsigned char clear_u8[4];
-    // ViewArgs (shader.hpp:63-68)
-    float trans[16];
-    float ctg;
-    float ray_o[3];
-    int W, H;
+    ViewArgs view;
     const float4 *tf;
     int ntf;
     // outputs

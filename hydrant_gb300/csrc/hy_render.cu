@@ -48,7 +48,7 @@ __device__ __forceinline__ uchar4 quantise(const ShadeArgs &A, float4 v) {
     return make_uchar4(A.clear_u8[0], A.clear_u8[1], A.clear_u8[2], 0);
 }
 
-template <int SHADER, int PC, int DT, int COMPOSITE>
+template <int SHADER, int PC, int DT, bool PADDED, int COMPOSITE>
 __global__ void __launch_bounds__(kThreads) render_kernel(const __grid_constant__ ShadeArgs A) {
     extern __shared__ float4 smem[];
     float4 *tf = smem;
@@ -58,16 +58,16 @@ __global__ void __launch_bounds__(kThreads) render_kernel(const __grid_constant_
     int x, y;
     tile_xy(x, y);
     long long samples = 0;
-    if (x < A.W && y < A.H) {
+    if (x < A.view.W && y < A.view.H) {
         float ox, oy, oz, dx, dy, dz;
-        gen_ray(A, x, y, ox, oy, oz, dx, dy, dz);
+        gen_ray(A.view, x, y, ox, oy, oz, dx, dy, dz);
         float4 v, aux;
         if (COMPOSITE) {
-            samples = composite_ray<SHADER, PC, DT>(A, S, ox, oy, oz, dx, dy, dz, v, aux);
+            samples = composite_ray<SHADER, PC, DT, PADDED>(A, A.view, S, ox, oy, oz, dx, dy, dz, v, aux);
         } else {
             Px p;
-            samples = emit<SHADER, PC, DT>(p, A, S, ox, oy, oz, dx, dy, dz, 0.f, 0.f, 0.f,
-                                           A.bbox_max[0], A.bbox_max[1], A.bbox_max[2]);
+            samples = emit<SHADER, PC, DT, PADDED>(p, A, A.view, S, ox, oy, oz, dx, dy, dz, 0.f, 0.f, 0.f,
+                                                   A.bbox_max[0], A.bbox_max[1], A.bbox_max[2]);
             v = make_float4(p.vx, p.vy, p.vz, p.vw);
             if (SHADER == HY_SHADER_VOLUME)
                 aux = make_float4(p.e0, p.e1, p.e2, p.e3);
@@ -76,7 +76,7 @@ __global__ void __launch_bounds__(kThreads) render_kernel(const __grid_constant_
             else
                 aux = make_float4(0.f, 0.f, 0.f, 0.f);
         }
-        const size_t idx = size_t(y) * A.W + x;
+        const size_t idx = size_t(y) * A.view.W + x;
         A.rgba[idx] = quantise(A, v);
         if (A.vout) A.vout[idx] = v;
         if (A.aux) A.aux[idx] = aux;
@@ -141,13 +141,13 @@ __global__ void __launch_bounds__(kThreads) emit_pass_kernel(const __grid_consta
     int x, y;
     tile_xy(x, y);
     long long samples = 0;
-    if (x < A.W && y < A.H) {
+    if (x < A.view.W && y < A.view.H) {
         float ox, oy, oz, dx, dy, dz;
-        gen_ray(A, x, y, ox, oy, oz, dx, dy, dz);
+        gen_ray(A.view, x, y, ox, oy, oz, dx, dy, dz);
         Px p;
-        samples = emit<SHADER, 0, DT>(p, A, S, ox, oy, oz, dx, dy, dz, 0.f, 0.f, 0.f,
-                                      A.bbox_max[0], A.bbox_max[1], A.bbox_max[2]);
-        store_film<SHADER>(A.film, size_t(y) * A.W + x, p);
+        samples = emit<SHADER, 0, DT, false>(p, A, A.view, S, ox, oy, oz, dx, dy, dz, 0.f, 0.f, 0.f,
+                                             A.bbox_max[0], A.bbox_max[1], A.bbox_max[2]);
+        store_film<SHADER>(A.film, size_t(y) * A.view.W + x, p);
     }
     count_samples(A, samples);
 }
@@ -163,10 +163,10 @@ __global__ void __launch_bounds__(kThreads) march_pass_kernel(const __grid_const
     int x, y;
     tile_xy(x, y);
     long long samples = 0;
-    if (x < A.W && y < A.H) {
-        const size_t idx = size_t(y) * A.W + x;
+    if (x < A.view.W && y < A.view.H) {
+        const size_t idx = size_t(y) * A.view.W + x;
         Px p = load_film<SHADER>(A.film, idx);
-        samples = run_main<SHADER, 0, DT>(p, A, S);
+        samples = run_main<SHADER, 0, DT, false>(p, A, A.view, S);
         store_film<SHADER>(A.film, idx, p);
     }
     count_samples(A, samples);
@@ -177,8 +177,8 @@ template <int SHADER>
 __global__ void __launch_bounds__(kThreads) pixel_pass_kernel(const __grid_constant__ ShadeArgs A) {
     int x, y;
     tile_xy(x, y);
-    if (x >= A.W || y >= A.H) return;
-    const size_t idx = size_t(y) * A.W + x;
+    if (x >= A.view.W || y >= A.view.H) return;
+    const size_t idx = size_t(y) * A.view.W + x;
     Px p = load_film<SHADER>(A.film, idx);
     unsigned char *d = static_cast<unsigned char *>(A.dst) + idx * 3;
     if (p.vw != 0.f) {
@@ -199,8 +199,8 @@ template <int SHADER>
 __global__ void __launch_bounds__(kThreads) fetch_pass_kernel(const __grid_constant__ ShadeArgs A) {
     int x, y;
     tile_xy(x, y);
-    if (x >= A.W || y >= A.H) return;
-    const size_t idx = size_t(y) * A.W + x;
+    if (x >= A.view.W || y >= A.view.H) return;
+    const size_t idx = size_t(y) * A.view.W + x;
     Px p = load_film<SHADER>(A.film, idx);
     if (SHADER == HY_SHADER_VOLUME) {
         float4 *d = reinterpret_cast<float4 *>(static_cast<char *>(A.dst) + idx * 32);
@@ -219,31 +219,39 @@ __global__ void __launch_bounds__(kThreads) fetch_pass_kernel(const __grid_const
 size_t smem_bytes(const ShadeArgs &a) { return size_t(a.ntf) * sizeof(float4) + 256 * sizeof(float); }
 
 dim3 grid_of(const ShadeArgs &a) {
-    return dim3((a.W + kTileW - 1) / kTileW, (a.H + kTileH - 1) / kTileH);
+    return dim3((a.view.W + kTileW - 1) / kTileW, (a.view.H + kTileH - 1) / kTileH);
 }
 
-template <int SHADER, int PC, int DT>
+template <int SHADER, int PC, int DT, bool PADDED>
 void launch_fused(const ShadeArgs &a, cudaStream_t s) {
     if (a.composite)
-        render_kernel<SHADER, PC, DT, 1><<<grid_of(a), kThreads, smem_bytes(a), s>>>(a);
+        render_kernel<SHADER, PC, DT, PADDED, 1><<<grid_of(a), kThreads, smem_bytes(a), s>>>(a);
     else
-        render_kernel<SHADER, PC, DT, 0><<<grid_of(a), kThreads, smem_bytes(a), s>>>(a);
+        render_kernel<SHADER, PC, DT, PADDED, 0><<<grid_of(a), kThreads, smem_bytes(a), s>>>(a);
 }
 
+// Instantiations: Blocks reads no bricks; u8 volumes with a 1-voxel apron and
+// 64^3 or 128^3 bricks get a compile-time brick edge (immediate offsets).
 template <int SHADER>
 int dispatch_fused(const ShadeArgs &a, cudaStream_t s) {
-    if (SHADER == HY_SHADER_BLOCKS) {
-        launch_fused<SHADER, 0, HY_DTYPE_U8>(a, s);
-        return HY_OK;
-    }
-    if (a.vol.dtype == HY_DTYPE_F32) {
-        launch_fused<SHADER, 0, HY_DTYPE_F32>(a, s);
-    } else if (a.vol.P == 66) {
-        launch_fused<SHADER, 66, HY_DTYPE_U8>(a, s);
-    } else if (a.vol.P == 130) {
-        launch_fused<SHADER, 130, HY_DTYPE_U8>(a, s);
+    if constexpr (SHADER == HY_SHADER_BLOCKS) {
+        launch_fused<SHADER, 0, HY_DTYPE_U8, false>(a, s);
     } else {
-        launch_fused<SHADER, 0, HY_DTYPE_U8>(a, s);
+        const bool padded = a.vol.pad > 0;
+        if (a.vol.dtype == HY_DTYPE_F32) {
+            if (padded)
+                launch_fused<SHADER, 0, HY_DTYPE_F32, true>(a, s);
+            else
+                launch_fused<SHADER, 0, HY_DTYPE_F32, false>(a, s);
+        } else if (padded && a.vol.P == 66) {
+            launch_fused<SHADER, 66, HY_DTYPE_U8, true>(a, s);
+        } else if (padded && a.vol.P == 130) {
+            launch_fused<SHADER, 130, HY_DTYPE_U8, true>(a, s);
+        } else if (padded) {
+            launch_fused<SHADER, 0, HY_DTYPE_U8, true>(a, s);
+        } else {
+            launch_fused<SHADER, 0, HY_DTYPE_U8, false>(a, s);
+        }
     }
     return HY_OK;
 }
@@ -298,7 +306,7 @@ int hy_fill_args(hy_ctx *ctx, const hy_volume *vol, const hy_shader_params *p, c
         return hy_fail(ctx, HY_ERR_STATE, "render: Volume shader needs a transfer function");
     std::memset(a, 0, sizeof(*a));
     a->vol = DevVolume{vol->pool, vol->info_dev, vol->reg_dev, vol->mean_dev, vol->grid[0],
-                       vol->grid[1], vol->grid[2], vol->P, vol->desc.dtype, 0};
+                       vol->grid[1], vol->grid[2], vol->P, vol->desc.dtype, vol->desc.padding};
     for (int i = 0; i < 3; ++i) a->bbox_max[i] = vol->bbox_max[i];
     a->du = vol->du;
     a->step = vol->du / 4.f / p->sample_rate;  // basic_renderer.hpp:129
@@ -309,8 +317,8 @@ int hy_fill_args(hy_ctx *ctx, const hy_volume *vol, const hy_shader_params *p, c
     a->isovalue = p->isovalue;
     for (int i = 0; i < 3; ++i) {
         a->surface[i] = p->surface_color[i];
-        a->eye[i] = p->eye_pos[i];
-        a->light[i] = p->light_pos[i];
+        a->view.eye[i] = p->eye_pos[i];
+        a->view.light[i] = p->light_pos[i];
         a->clear_u8[i] = sat_host(p->clear_color[i]);  // raycaster.hpp:211
     }
     a->rank = p->rank;
@@ -320,12 +328,12 @@ int hy_fill_args(hy_ctx *ctx, const hy_volume *vol, const hy_shader_params *p, c
     a->srgb = p->srgb;
     a->count = p->count_samples;
     if (view) {
-        std::memcpy(a->trans, view->trans, sizeof(a->trans));
-        a->ctg = view->ctg_fovy_2;
-        for (int i = 0; i < 3; ++i) a->ray_o[i] = view->ray_o[i];
+        std::memcpy(a->view.trans, view->trans, sizeof(a->view.trans));
+        a->view.ctg = view->ctg_fovy_2;
+        for (int i = 0; i < 3; ++i) a->view.ray_o[i] = view->ray_o[i];
     }
-    a->W = W;
-    a->H = H;
+    a->view.W = W;
+    a->view.H = H;
     a->tf = ctx->tf_dev;
     a->ntf = ctx->ntf;
     a->counter = ctx->counter_dev;
@@ -350,7 +358,7 @@ int hy_launch_render(hy_ctx *ctx, const ShadeArgs &a) {
     HY_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
     ctx->stats_pending = true;
     ctx->pend_count = a.count;
-    ctx->pend_pixels = (int64_t)a.W * a.H;
+    ctx->pend_pixels = (int64_t)a.view.W * a.view.H;
     return HY_OK;
 }
 
@@ -373,7 +381,7 @@ int hy_launch_pass(hy_ctx *ctx, const ShadeArgs &a, int pass) {
     HY_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
     ctx->stats_pending = true;
     ctx->pend_count = a.count && pass <= HY_PASS_RAY_MARCH;
-    ctx->pend_pixels = (int64_t)a.W * a.H;
+    ctx->pend_pixels = (int64_t)a.view.W * a.view.H;
     return HY_OK;
 }
 

@@ -104,22 +104,31 @@ __device__ __forceinline__ BrickRef load_brick(const DevVolume &V, int reg) {
 //    gives the same float.  Offsets are then immediates when P is a
 //    compile-time constant.
 // U8 voxels are normalised with lut[u] = u / 255.f (texture_3d.hpp:78-86).
-template <int PC, int DT>
+//
+// INTERIOR: the caller guarantees brick-local coordinates in [0,1] (the main
+// loops sample at o - floor(o)) and an apron of at least one voxel.  Then
+// f = P*(k*x + b) lies in [pad, bs+pad] (up to rounding far below 0.5), so
+// Wrap is the identity and floor(f - 0.5) is in [pad-1, bs+pad-1] within
+// [0, P-2]: both range checks are known to pass and are left out.
+template <int PC, int DT, bool INTERIOR = false>
 __device__ __forceinline__ float sample_brick(const BrickRef &b, int Prt, float lx, float ly,
                                               float lz, const float *__restrict__ lut) {
     const int P = PC ? PC : Prt;
     const float fd = float(P);
     float mx = b.k * lx + b.bx, my = b.k * ly + b.by, mz = b.k * lz + b.bz;
     float fx = fd * mx, fy = fd * my, fz = fd * mz;
-    if (!(fx >= 0.f && fx < fd)) fx = fx - fd * floorf(fx / fd);
-    if (!(fy >= 0.f && fy < fd)) fy = fy - fd * floorf(fy / fd);
-    if (!(fz >= 0.f && fz < fd)) fz = fz - fd * floorf(fz / fd);
+    if (!INTERIOR) {
+        if (!(fx >= 0.f && fx < fd)) fx = fx - fd * floorf(fx / fd);
+        if (!(fy >= 0.f && fy < fd)) fy = fy - fd * floorf(fy / fd);
+        if (!(fz >= 0.f && fz < fd)) fz = fz - fd * floorf(fz / fd);
+    }
     float ux = fx - .5f, uy = fy - .5f, uz = fz - .5f;
     float flx = floorf(ux), fly = floorf(uy), flz = floorf(uz);
     float ax = ux - flx, ay = uy - fly, az = uz - flz;
     int ix = int(flx), iy = int(fly), iz = int(flz);
     float v000, v100, v010, v110, v001, v101, v011, v111;
-    if (ix >= 0 && ix <= P - 2 && iy >= 0 && iy <= P - 2 && iz >= 0 && iz <= P - 2) {
+    if (INTERIOR ||
+        (ix >= 0 && ix <= P - 2 && iy >= 0 && iy <= P - 2 && iz >= 0 && iz <= P - 2)) {
         const long long base = ((long long)iz * P + iy) * P + ix;
         if (DT == HY_DTYPE_U8) {
             const unsigned char *q = b.base + base;
@@ -188,11 +197,16 @@ __device__ __forceinline__ float4 sample_tf(const float4 *__restrict__ tf, int n
                                             float s) {
     float fx = fn * s;
     if (!(0.f <= fx && fx <= fn)) return make_float4(0.f, 0.f, 0.f, 0.f);
+    // fx in [0, n] so floor(fx - 0.5) is in [-1, n-1]: the lower index only
+    // needs the clamp at 0.  The upper one is ceil(u) = floor(u) + 1, or
+    // floor(u) when u is integral -- where a == 0 and the knot it picks is
+    // weighted by 0, so floor(u) + 1 (clamped at n-1) gives the same floats.
     float u = fx - .5f;
     float flr = floorf(u);
     float a = u - flr;
-    int i = iclamp(int(flr), 0, n - 1);
-    int j = iclamp(int(ceilf(u)), 0, n - 1);
+    const int fi = int(flr);
+    int i = max(fi, 0);
+    int j = min(fi + 1, n - 1);
     float4 x = tf[i], y = tf[j];
     float b = 1.f - a;
     return make_float4(x.x * b + y.x * a, x.y * b + y.y * a, x.z * b + y.z * a, x.w * b + y.w * a);
@@ -211,35 +225,64 @@ struct Shared {
 #define HY_T93 0.93f
 #define HY_T85 0.85f
 
-// VolumeShaderKernel::main (volume_shader.cu:32-81).  The brick lookup is
-// cached while floor(o) stays in the same brick (same texel, same result).
-template <int PC, int DT>
+// Tracks the brick of the current sample position.  floor(o) only changes
+// when o leaves [ip, ip+1) on some axis, so the texel lookups are redone only
+// then (same texel, same values); o == NaN fails the test and redoes them
+// every step, exactly like the reference.
+struct BrickCursor {
+    float ipx, ipy, ipz, hx, hy, hz;
+    int cur, cd, pg;
+    BrickRef br;
+    __device__ __forceinline__ void reset() {
+        ipx = ipy = ipz = __int_as_float(0x7f800000);
+        hx = hy = hz = -__int_as_float(0x7f800000);
+        cur = -1;
+        cd = 0;
+        pg = -1;
+        br = BrickRef{};
+    }
+    __device__ __forceinline__ void update(const DevVolume &V, float fgx, float fgy, float fgz,
+                                           float ox, float oy, float oz) {
+        if (ox >= ipx && ox < hx && oy >= ipy && oy < hy && oz >= ipz && oz < hz) return;
+        ipx = floorf(ox);
+        ipy = floorf(oy);
+        ipz = floorf(oz);
+        hx = ipx + 1.f;
+        hy = ipy + 1.f;
+        hz = ipz + 1.f;
+        const int bid = thumb_index(V, fgx, fgy, fgz, ipx, ipy, ipz);
+        if (bid != cur) {
+            cur = bid;
+            const int2 in = __ldg(&V.info[bid]);
+            cd = in.x;
+            pg = in.y;
+            if (cd == 0 && pg >= 0) br = load_brick(V, pg);
+        }
+    }
+};
+
+// VolumeShaderKernel::main (volume_shader.cu:32-81).
+// PADDED: the volume has an apron of >= 1 voxel, so the interior sampler applies.
+template <int PC, int DT, bool PADDED>
 __device__ __forceinline__ long long volume_main(Px &p, const ShadeArgs &A, const Shared &S) {
     const DevVolume &V = A.vol;
     long long samples = 0;
     const float cdu = 1.f / gmax(gmax(fabsf(p.dx), fabsf(p.dy)), fabsf(p.dz));
     const float rx = 1.f / p.dx, ry = 1.f / p.dy, rz = 1.f / p.dz;
     const float fgx = float(V.gx), fgy = float(V.gy), fgz = float(V.gz);
-    int cur = -1, cd = 0, pg = -1;
-    BrickRef br{};
+    BrickCursor c;
+    c.reset();
     int cur_ss = 0;
     float sx = 0.f, sy = 0.f, sz = 0.f;
     while (p.nsteps > 0) {
-        float ipx = floorf(p.ox), ipy = floorf(p.oy), ipz = floorf(p.oz);
-        int bid = thumb_index(V, fgx, fgy, fgz, ipx, ipy, ipz);
-        if (bid != cur) {
-            cur = bid;
-            int2 in = __ldg(&V.info[bid]);
-            cd = in.x;
-            pg = in.y;
-            if (cd == 0 && pg >= 0) br = load_brick(V, pg);
-        }
-        if (cd) {
-            p.nsteps -= skip_nblock_steps(p, rx, ry, rz, ipx, ipy, ipz, cd, cdu,
+        c.update(V, fgx, fgy, fgz, p.ox, p.oy, p.oz);
+        if (c.cd) {
+            p.nsteps -= skip_nblock_steps(p, rx, ry, rz, c.ipx, c.ipy, c.ipz, c.cd, cdu,
                                           A.step * float(p.step_size));
         } else {
-            if (pg == -1) break;
-            float s = sample_brick<PC, DT>(br, V.P, p.ox - ipx, p.oy - ipy, p.oz - ipz, S.lut);
+            if (c.pg == -1) break;
+            float s = sample_brick<PC, DT, PADDED>(c.br, V.P, p.ox - c.ipx, p.oy - c.ipy,
+                                                   p.oz - c.ipz, S.lut);
             ++samples;
             float4 ub = sample_tf(S.tf, S.ntf, S.fntf, s);
             if (A.mode == HY_VOLUME_PARTITION) {
@@ -249,8 +292,8 @@ __device__ __forceinline__ long long volume_main(Px &p, const ShadeArgs &A, cons
                 float len = sqrtf(ub.x * ub.x + ub.y * ub.y + ub.z * ub.z);
                 ub = make_float4(mr * len, mg * len, mb * len, ub.w);
             } else if (A.mode == HY_VOLUME_PAGING) {
-                ub = pg >= A.lowest_blkcnt ? make_float4(0.f, 1.f, 0.f, ub.w)
-                                           : make_float4(1.f, 0.f, 0.f, ub.w);
+                ub = c.pg >= A.lowest_blkcnt ? make_float4(0.f, 1.f, 0.f, ub.w)
+                                             : make_float4(1.f, 0.f, 0.f, ub.w);
             }
             ub.w = ub.w * A.density;  // opacity scale; exact identity at 1
             const float w = ub.w;
@@ -362,8 +405,9 @@ __device__ __forceinline__ void normalize3(float &x, float &y, float &z) {
 
 // IsosurfaceShaderKernel::main (isosurface_shader.cu:50-125).  prev_value
 // stays 0, as in the reference (it is never updated there).
-template <int PC, int DT>
-__device__ __forceinline__ long long iso_main(Px &p, const ShadeArgs &A, const Shared &S) {
+template <int PC, int DT, bool PADDED>
+__device__ __forceinline__ long long iso_main(Px &p, const ShadeArgs &A, const ViewArgs &Vw,
+                                             const Shared &S) {
     const DevVolume &V = A.vol;
     long long samples = 0;
     const float cdu = 1.f / gmax(gmax(fabsf(p.dx), fabsf(p.dy)), fabsf(p.dz));
@@ -373,23 +417,18 @@ __device__ __forceinline__ long long iso_main(Px &p, const ShadeArgs &A, const S
     const float iso = A.isovalue;
     const float prev_sign = fsign(prev_value - iso);
     const float sx = p.dx * A.step, sy = p.dy * A.step, sz = p.dz * A.step;
-    int cur = -1, cd = 0, pg = -1;
-    BrickRef br{};
+    BrickCursor c;
+    c.reset();
     while (p.nsteps > 0) {
-        float ipx = floorf(p.ox), ipy = floorf(p.oy), ipz = floorf(p.oz);
-        int bid = thumb_index(V, fgx, fgy, fgz, ipx, ipy, ipz);
-        if (bid != cur) {
-            cur = bid;
-            int2 in = __ldg(&V.info[bid]);
-            cd = in.x;
-            pg = in.y;
-            if (cd == 0 && pg >= 0) br = load_brick(V, pg);
-        }
-        if (cd) {
-            p.nsteps -= skip_nblock_steps(p, rx, ry, rz, ipx, ipy, ipz, cd, cdu, A.step);
+        c.update(V, fgx, fgy, fgz, p.ox, p.oy, p.oz);
+        const float ipx = c.ipx, ipy = c.ipy, ipz = c.ipz;
+        const BrickRef &br = c.br;
+        if (c.cd) {
+            p.nsteps -= skip_nblock_steps(p, rx, ry, rz, ipx, ipy, ipz, c.cd, cdu, A.step);
         } else {
-            if (pg == -1) break;  // page fault: resume in the next march pass
-            float value = sample_brick<PC, DT>(br, V.P, p.ox - ipx, p.oy - ipy, p.oz - ipz, S.lut);
+            if (c.pg == -1) break;  // page fault: resume in the next march pass
+            float value = sample_brick<PC, DT, PADDED>(br, V.P, p.ox - ipx, p.oy - ipy,
+                                                       p.oz - ipz, S.lut);
             ++samples;
             if (fsign(value - iso) != prev_sign) {
                 const float dt = A.step;
@@ -416,7 +455,7 @@ __device__ __forceinline__ long long iso_main(Px &p, const ShadeArgs &A, const S
                 mat_vec4(A.to_world, ipx2, ipy2, ipz2, 1.f, wx, wy, wz);
                 mat_vec4(A.to_world, nnx, nny, nnz, 0.f, nx, ny, nz);
                 normalize3(nx, ny, nz);
-                float lx2 = A.light[0] - wx, ly2 = A.light[1] - wy, lz2 = A.light[2] - wz;
+                float lx2 = Vw.light[0] - wx, ly2 = Vw.light[1] - wy, lz2 = Vw.light[2] - wz;
                 normalize3(lx2, ly2, lz2);
                 float hx = lx2 - wx, hy = ly2 - wy, hz = lz2 - wz;
                 normalize3(hx, hy, hz);
@@ -424,7 +463,7 @@ __device__ __forceinline__ long long iso_main(Px &p, const ShadeArgs &A, const S
                 const float diffuse = .6f * fclamp(lx2 * nx + ly2 * ny + lz2 * nz, 0.f, 1.f);
                 const float specular =
                     .2f * powf(fclamp(hx * nx + hy * ny + hz * nz, 0.f, 1.f), 100.f);
-                const float ex = wx - A.eye[0], ey = wy - A.eye[1], ez = wz - A.eye[2];
+                const float ex = wx - Vw.eye[0], ey = wy - Vw.eye[1], ez = wz - Vw.eye[2];
                 const float distance = sqrtf(ex * ex + ey * ey + ez * ez) / 2.f;
                 if (A.mode == HY_ISO_COLOR) {
                     const float f = ambient + (diffuse + specular) / distance;
@@ -457,25 +496,26 @@ __device__ __forceinline__ long long iso_main(Px &p, const ShadeArgs &A, const S
     return samples;
 }
 
-template <int SHADER, int PC, int DT>
-__device__ __forceinline__ long long run_main(Px &p, const ShadeArgs &A, const Shared &S) {
-    if (SHADER == HY_SHADER_VOLUME) return volume_main<PC, DT>(p, A, S);
+template <int SHADER, int PC, int DT, bool PADDED>
+__device__ __forceinline__ long long run_main(Px &p, const ShadeArgs &A, const ViewArgs &Vw,
+                                             const Shared &S) {
+    if (SHADER == HY_SHADER_VOLUME) return volume_main<PC, DT, PADDED>(p, A, S);
     if (SHADER == HY_SHADER_BLOCKS) return blocks_main(p, A);
-    return iso_main<PC, DT>(p, A, S);
+    return iso_main<PC, DT, PADDED>(p, A, Vw, S);
 }
 
 // Ray generation (cuda_shading.cu:24-29 == cpu_shading.cc:14-21).
-__device__ __forceinline__ void gen_ray(const ShadeArgs &A, int x, int y, float &ox, float &oy,
+__device__ __forceinline__ void gen_ray(const ViewArgs &Vw, int x, int y, float &ox, float &oy,
                                         float &oz, float &dx, float &dy, float &dz) {
-    const float ccx = float(A.W) / 2.f, ccy = float(A.H) / 2.f;
-    const float fh = float(A.H);
+    const float ccx = float(Vw.W) / 2.f, ccy = float(Vw.H) / 2.f;
+    const float fh = float(Vw.H);
     const float ux = (float(x) - ccx) * 2.f / fh;
     const float uy = (float(y) - ccy) * 2.f / fh;
     float px, py, pz;
-    mat_vec4(A.trans, ux, -uy, -A.ctg, 1.f, px, py, pz);
-    ox = A.ray_o[0];
-    oy = A.ray_o[1];
-    oz = A.ray_o[2];
+    mat_vec4(Vw.trans, ux, -uy, -Vw.ctg, 1.f, px, py, pz);
+    ox = Vw.ray_o[0];
+    oy = Vw.ray_o[1];
+    oz = Vw.ray_o[2];
     dx = px - ox;
     dy = py - oy;
     dz = pz - oz;
@@ -485,8 +525,9 @@ __device__ __forceinline__ void gen_ray(const ShadeArgs &A, int x, int y, float 
 // ray_emit_shader_impl (shader.hpp:113-137) against box [b0, b1]; init() of
 // the Volume (volume_shader.cu:16-21) and Isosurface (isosurface_shader.cu:34-39)
 // shaders.
-template <int SHADER, int PC, int DT>
-__device__ __forceinline__ long long emit(Px &p, const ShadeArgs &A, const Shared &S, float ox,
+template <int SHADER, int PC, int DT, bool PADDED>
+__device__ __forceinline__ long long emit(Px &p, const ShadeArgs &A, const ViewArgs &Vw,
+                                          const Shared &S, float ox,
                                           float oy, float oz, float dx, float dy, float dz,
                                           float x0, float y0, float z0, float x1, float y1,
                                           float z1) {
@@ -517,7 +558,7 @@ __device__ __forceinline__ long long emit(Px &p, const ShadeArgs &A, const Share
         p.oz = p.oz + p.dz * tnear;
         p.nsteps = min(A.max_steps, int((tfar - tnear) / A.step));
         p.step_size = 1;
-        return run_main<SHADER, PC, DT>(p, A, S);
+        return run_main<SHADER, PC, DT, PADDED>(p, A, Vw, S);
     }
     p.nsteps = 0;
     p.step_size = 1;
@@ -538,8 +579,9 @@ __device__ __forceinline__ float vol_linear_to_srgb(float x) {  // volume.cc:175
 // per-partition bbox of dbuf_renderer.hpp:38-40) and the partials are
 // composited front to back with volume.cc:267-280 (Volume),
 // isosurface.cc:272-290 (depth-min, Isosurface) or the over operator (Blocks).
-template <int SHADER, int PC, int DT>
-__device__ __forceinline__ long long composite_ray(const ShadeArgs &A, const Shared &S, float ox,
+template <int SHADER, int PC, int DT, bool PADDED>
+__device__ __forceinline__ long long composite_ray(const ShadeArgs &A, const ViewArgs &Vw,
+                                                   const Shared &S, float ox,
                                                    float oy, float oz, float dx, float dy,
                                                    float dz, float4 &acc, float4 &aux) {
     long long samples = 0;
@@ -587,7 +629,7 @@ __device__ __forceinline__ long long composite_ray(const ShadeArgs &A, const Sha
         if (__ldg(&V.info[bid].x) == 0) {
             const float bx = float(cell[0]), by = float(cell[1]), bz = float(cell[2]);
             Px p;
-            samples += emit<SHADER, PC, DT>(p, A, S, ox, oy, oz, dx, dy, dz, bx, by, bz, bx + 1.f,
+            samples += emit<SHADER, PC, DT, PADDED>(p, A, Vw, S, ox, oy, oz, dx, dy, dz, bx, by, bz, bx + 1.f,
                                             by + 1.f, bz + 1.f);
             if (SHADER == HY_SHADER_VOLUME) {
                 if (first) {

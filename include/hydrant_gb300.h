@@ -228,6 +228,46 @@ int hy_shade_pass(hy_ctx *ctx, const hy_volume *vol, const hy_shader_params *par
                   int32_t pass, const hy_view *view, void *film_dev, int32_t width,
                   int32_t height, void *dst_dev, const uint8_t clear_rgb[3]);
 
+/* ---- batched multi-view rendering -------------------------------------------
+ * Many views rendered by one persistent launch replayed from a CUDA graph.
+ * The reference renders one view per Raycaster pass (raycaster.hpp:32-54,
+ * called per frame from BasicRenderer::offline_render, basic_renderer.hpp:
+ * 134-142); a batch gives images identical to hy_render per view. */
+typedef struct hy_batch hy_batch;
+
+typedef struct hy_batch_view {
+    hy_view view;          /* ViewArgs of this camera */
+    int32_t width;
+    int32_t height;
+    int64_t rgba_offset;   /* byte offset of this view's RGBA8 image in the output (4-aligned) */
+    float eye_pos[3];      /* Isosurface lighting of this camera (see hy_iso_lighting) */
+    float light_pos[3];
+} hy_batch_view;
+
+typedef struct hy_batch_config {
+    int32_t tile_w;        /* warp ray tile width: 4, 8, 16 or 32 (height 32/tile_w) */
+    int32_t grab;          /* warp tiles taken per queue access, 1..16 */
+    int32_t block_warps;   /* warps per block, 1..8 */
+    int32_t blocks_per_sm; /* persistent blocks per SM; 0 = as many as fit */
+} hy_batch_config;
+
+int hy_batch_create(hy_ctx *ctx, const hy_volume *vol, const hy_shader_params *params,
+                    const hy_batch_view *views, int32_t nviews, hy_batch **out);
+int hy_batch_destroy(hy_batch *batch);
+/* Bytes the output buffer must hold (max over views of offset + W*H*4). */
+int hy_batch_output_bytes(const hy_batch *batch, int64_t *bytes);
+int hy_batch_set_config(hy_batch *batch, const hy_batch_config *cfg);
+int hy_batch_get_config(const hy_batch *batch, hy_batch_config *out);
+/* 1: count brick samples of each launch into hy_render_stats. */
+int hy_batch_set_counting(hy_batch *batch, int32_t count_samples);
+/* Device output, asynchronous on the context's stream. */
+int hy_batch_render_device(hy_batch *batch, uint8_t *rgba_dev);
+/* Host output; returns when the images are on the host. */
+int hy_batch_render(hy_batch *batch, uint8_t *rgba_host);
+/* Times every launch shape (tile 8x4/4x8/16x2, grab 1/2/4, 2/4/8 warps per
+ * block) on this batch and keeps the fastest; it is returned in *best. */
+int hy_batch_autotune(hy_batch *batch, uint8_t *rgba_dev, int32_t reps, hy_batch_config *best);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,110 @@
+"""Batched multi-view rendering: identical images to the per-view path."""
+
+import numpy as np
+import pytest
+
+import hydrant_gb300 as hy
+from hydrant_gb300 import workloads as wl
+from tests._harness import camera
+
+pytestmark = pytest.mark.gpu
+
+SIZES = [(64, 64), (37, 23), (128, 96), (16, 16), (96, 128), (1, 1), (200, 33)]
+
+
+def _views(vol, sizes, seed=11):
+    rng = wl.SplitMix64(seed)
+    out, cams = [], []
+    for W, H in sizes:
+        arm = (rng.uniform(-180, 180), rng.uniform(-60, 60), rng.uniform(1.8, 3.0))
+        cam = camera(a=arm)
+        cams.append(cam)
+        out.append((hy.camera_view(vol, cam), W, H))
+    return out, cams
+
+
+def _per_view(ctx, vol, kw, views, cams):
+    imgs, samples = [], 0
+    for (v, W, H), cam in zip(views, cams):
+        p = hy.shader_params(count_samples=True, **kw)
+        if p.shader == hy._abi.SHADER_ISOSURFACE:
+            hy.iso_lighting(vol, cam, p)
+        r = hy.render(ctx, vol, p, v, W, H)
+        imgs.append(r.rgba)
+        samples += r.samples
+    return imgs, samples
+
+
+def _lighting(vol, cams, kw):
+    out = []
+    for cam in cams:
+        p = hy.shader_params(**kw)
+        hy.iso_lighting(vol, cam, p)
+        out.append((list(p.eye_pos), list(p.light_pos)))
+    return out
+
+
+@pytest.fixture(scope="module")
+def tubes(ctx):
+    vol = hy.Volume(ctx, hy.synth_tubes_u8(1, (128, 128, 128), 12), 32, 1)
+    ctx.set_transfer_fn(wl.TF9)
+    yield vol
+    vol.close()
+
+
+@pytest.mark.parametrize("kw", [
+    dict(shader="Volume", density=0.5, sample_rate=0.5),
+    dict(shader="Isosurface", mode="Color", isovalue=0.5),
+    dict(shader="Blocks", mode="Volume", density=1e-2),
+    dict(shader="Volume", density=0.5, composite=True),
+    dict(shader="Isosurface", mode="Normal", composite=True),
+])
+def test_batch_equals_per_view(ctx, tubes, kw):
+    views, cams = _views(tubes, SIZES)
+    ref, ref_samples = _per_view(ctx, tubes, kw, views, cams)
+    p = hy.shader_params(**kw)
+    light = _lighting(tubes, cams, kw) if p.shader == hy._abi.SHADER_ISOSURFACE else None
+    b = hy.Batch(ctx, tubes, p, views, light)
+    try:
+        b.set_counting(True)
+        for cfg in [(8, 1, 4), (4, 2, 2), (16, 4, 8), (32, 3, 1)]:
+            b.set_config(*cfg)
+            got = b.render()
+            assert ctx.stats().samples == ref_samples
+            for i, (g, r) in enumerate(zip(got, ref)):
+                assert np.array_equal(g, r), f"view {i} differs with config {cfg}"
+    finally:
+        b.close()
+
+
+def test_batch_autotune_and_graph_replay(ctx, tubes):
+    torch = pytest.importorskip("torch")
+    views, cams = _views(tubes, SIZES * 3, seed=5)
+    kw = dict(shader="Volume", density=0.3, sample_rate=0.5)
+    ref, _ = _per_view(ctx, tubes, kw, views, cams)
+    b = hy.Batch(ctx, tubes, hy.shader_params(**kw), views)
+    try:
+        out = torch.empty(b.nbytes, dtype=torch.uint8, device="cuda")
+        cfg = b.autotune(out.data_ptr(), reps=1)
+        assert cfg.tile_w in (4, 8, 16) and cfg.grab in (1, 2, 4)
+        for _ in range(3):  # graph replays
+            out.zero_()
+            b.render_device(out.data_ptr())
+            ctx.synchronize()
+            got = b.split(out.cpu().numpy())
+            for g, r in zip(got, ref):
+                assert np.array_equal(g, r)
+    finally:
+        b.close()
+
+
+def test_batch_rejects_bad_input(ctx, tubes):
+    with pytest.raises(hy.HydrantError):
+        hy.Batch(ctx, tubes, hy.shader_params(shader="Volume"), [])
+    views, _ = _views(tubes, [(8, 8)])
+    b = hy.Batch(ctx, tubes, hy.shader_params(shader="Volume"), views)
+    try:
+        with pytest.raises(hy.HydrantError):
+            b.set_config(tile_w=5)
+    finally:
+        b.close()
