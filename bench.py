@@ -325,7 +325,8 @@ def main_ours(args):
     if args.no_autotune:
         c = batch.config
         tuned = {"tile_w": c.tile_w, "grab": c.grab, "block_warps": c.block_warps,
-                 "blocks_per_sm": c.blocks_per_sm, "source": "default"}
+                 "blocks_per_sm": c.blocks_per_sm, "block_queue": c.block_queue,
+                 "source": "default"}
     else:
         tuned = autotune.tuned_config(batch, key, out.data_ptr(), reps=1)
     batch.set_counting(True)

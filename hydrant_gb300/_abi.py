@@ -95,6 +95,7 @@ class HyBatchConfig(C.Structure):
         ("grab", C.c_int32),
         ("block_warps", C.c_int32),
         ("blocks_per_sm", C.c_int32),
+        ("block_queue", C.c_int32),
     ]
 
 

@@ -5,7 +5,8 @@
 // last wave of a big view drains.  Here every view of a batch is cut into
 // warp ray tiles (32 rays: 8x4, 4x8, 16x2 or 32x1 pixels), all tiles of all
 // views form one queue, and a persistent grid sized to the GPU takes tiles
-// from it (one atomicAdd per `grab` tiles per warp) until it is empty.  A
+// from it (one atomicAdd per `grab` units) until it is empty -- per warp, or
+// per block with the block's warps on neighbouring warp tiles.  A
 // tile's rays are shaded exactly as in the single-view kernel, so images are
 // identical to the per-view path.  The queue head is the only scratch memory;
 // the {queue reset, kernel} pair is captured once into a CUDA graph and
@@ -36,6 +37,7 @@ struct BatchArgs {
     int nviews;
     int total_tiles;
     int tile_w, tile_h, grab;
+    int block_queue, bx, by;  // per-block queue units of bx x by warp tiles
     unsigned int *queue;
     unsigned char *out;
 };
@@ -43,10 +45,56 @@ struct BatchArgs {
 constexpr int kMaxViews = 2048;
 constexpr int kMaxBlockThreads = 256;
 
+// Shades one pixel of a batch view and stores its RGBA8 value.
+template <int SHADER, int PC, int DT, bool PADDED, int COMPOSITE>
+__device__ __forceinline__ long long shade_batch_pixel(const BatchArgs &B, const Shared &S,
+                                                       const BatchView &bv, int x, int y) {
+    const ShadeArgs &A = B.A;
+    if (x >= bv.view.W || y >= bv.view.H) return 0;
+    long long samples;
+    float ox, oy, oz, dx, dy, dz;
+    gen_ray(bv.view, x, y, ox, oy, oz, dx, dy, dz);
+    float4 v;
+    if (COMPOSITE) {
+        float4 aux;
+        samples = composite_ray<SHADER, PC, DT, PADDED>(A, bv.view, S, ox, oy, oz, dx, dy, dz, v,
+                                                        aux);
+    } else {
+        Px p;
+        samples = emit<SHADER, PC, DT, PADDED>(p, A, bv.view, S, ox, oy, oz, dx, dy, dz, 0.f, 0.f,
+                                               0.f, A.bbox_max[0], A.bbox_max[1], A.bbox_max[2]);
+        v = make_float4(p.vx, p.vy, p.vz, p.vw);
+    }
+    uchar4 q;
+    if (v.w != 0.f)
+        q = make_uchar4(saturate_u8(v.x), saturate_u8(v.y), saturate_u8(v.z), saturate_u8(v.w));
+    else
+        q = make_uchar4(A.clear_u8[0], A.clear_u8[1], A.clear_u8[2], 0);
+    *reinterpret_cast<uchar4 *>(B.out + bv.out_off + (size_t(y) * bv.view.W + x) * 4) = q;
+    return samples;
+}
+
+__device__ __forceinline__ int find_view(const int *starts, int n, int t) {
+    int lo = 0, hi = n - 1;  // last view with starts[v] <= t
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (starts[mid] <= t)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
+// Queue units: one warp tile per unit (block_queue == 0, each warp takes its
+// own units), or one block tile of bx x by warp tiles per unit (block_queue
+// == 1, the block takes a unit and warp w shades its w-th warp tile, so the
+// warps of an SM work on neighbouring rays and share L1 lines).
 template <int SHADER, int PC, int DT, bool PADDED, int COMPOSITE>
 __global__ void __launch_bounds__(kMaxBlockThreads)
     batch_kernel(const __grid_constant__ BatchArgs B) {
     extern __shared__ float4 smem[];
+    __shared__ unsigned int s_t0;
     const ShadeArgs &A = B.A;
     float4 *tf = smem;
     float *lut = reinterpret_cast<float *>(smem + A.ntf);
@@ -56,52 +104,44 @@ __global__ void __launch_bounds__(kMaxBlockThreads)
     for (int i = threadIdx.x; i < B.nviews; i += blockDim.x) starts[i] = B.starts[i];
     __syncthreads();
     const Shared S{tf, A.ntf, float(A.ntf), lut};
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int lx = lane % B.tile_w, ly = lane / B.tile_w;
     long long samples = 0;
-    for (;;) {
-        unsigned int t0 = 0;
-        if (lane == 0) t0 = atomicAdd(B.queue, unsigned(B.grab));
-        t0 = __shfl_sync(0xffffffffu, t0, 0);
-        if (t0 >= unsigned(B.total_tiles)) break;
-        for (int g = 0; g < B.grab; ++g) {
-            const int t = int(t0) + g;
-            if (t >= B.total_tiles) break;
-            int lo = 0, hi = B.nviews - 1;  // last view with starts[v] <= t
-            while (lo < hi) {
-                const int mid = (lo + hi + 1) >> 1;
-                if (starts[mid] <= t)
-                    lo = mid;
-                else
-                    hi = mid - 1;
+    if (B.block_queue) {
+        const int wx = warp % B.bx, wy = warp / B.bx;
+        for (;;) {
+            if (threadIdx.x == 0) s_t0 = atomicAdd(B.queue, unsigned(B.grab));
+            __syncthreads();
+            const unsigned int t0 = s_t0;
+            __syncthreads();
+            if (t0 >= unsigned(B.total_tiles)) break;
+            for (int g = 0; g < B.grab; ++g) {
+                const int t = int(t0) + g;
+                if (t >= B.total_tiles) break;
+                const int vi = find_view(starts, B.nviews, t);
+                const BatchView &bv = B.views[vi];
+                const int local = t - starts[vi];
+                const int uy = local / bv.tiles_x, ux = local - uy * bv.tiles_x;
+                const int x = (ux * B.bx + wx) * B.tile_w + lx;
+                const int y = (uy * B.by + wy) * B.tile_h + ly;
+                samples += shade_batch_pixel<SHADER, PC, DT, PADDED, COMPOSITE>(B, S, bv, x, y);
             }
-            const BatchView &bv = B.views[lo];
-            const int local = t - starts[lo];
-            const int ty = local / bv.tiles_x, tx = local - ty * bv.tiles_x;
-            const int x = tx * B.tile_w + lx, y = ty * B.tile_h + ly;
-            if (x < bv.view.W && y < bv.view.H) {
-                float ox, oy, oz, dx, dy, dz;
-                gen_ray(bv.view, x, y, ox, oy, oz, dx, dy, dz);
-                float4 v;
-                if (COMPOSITE) {
-                    float4 aux;
-                    samples += composite_ray<SHADER, PC, DT, PADDED>(A, bv.view, S, ox, oy, oz,
-                                                                     dx, dy, dz, v, aux);
-                } else {
-                    Px p;
-                    samples += emit<SHADER, PC, DT, PADDED>(p, A, bv.view, S, ox, oy, oz, dx, dy,
-                                                            dz, 0.f, 0.f, 0.f, A.bbox_max[0],
-                                                            A.bbox_max[1], A.bbox_max[2]);
-                    v = make_float4(p.vx, p.vy, p.vz, p.vw);
-                }
-                uchar4 q;
-                if (v.w != 0.f)
-                    q = make_uchar4(saturate_u8(v.x), saturate_u8(v.y), saturate_u8(v.z),
-                                    saturate_u8(v.w));
-                else
-                    q = make_uchar4(A.clear_u8[0], A.clear_u8[1], A.clear_u8[2], 0);
-                *reinterpret_cast<uchar4 *>(B.out + bv.out_off +
-                                            (size_t(y) * bv.view.W + x) * 4) = q;
+        }
+    } else {
+        for (;;) {
+            unsigned int t0 = 0;
+            if (lane == 0) t0 = atomicAdd(B.queue, unsigned(B.grab));
+            t0 = __shfl_sync(0xffffffffu, t0, 0);
+            if (t0 >= unsigned(B.total_tiles)) break;
+            for (int g = 0; g < B.grab; ++g) {
+                const int t = int(t0) + g;
+                if (t >= B.total_tiles) break;
+                const int vi = find_view(starts, B.nviews, t);
+                const BatchView &bv = B.views[vi];
+                const int local = t - starts[vi];
+                const int ty = local / bv.tiles_x, tx = local - ty * bv.tiles_x;
+                samples += shade_batch_pixel<SHADER, PC, DT, PADDED, COMPOSITE>(
+                    B, S, bv, tx * B.tile_w + lx, ty * B.tile_h + ly);
             }
         }
     }
@@ -159,7 +199,7 @@ struct hy_batch {
     unsigned int *queue_dev = nullptr;
     int total_tiles = 0;
     int64_t out_bytes = 0;
-    hy_batch_config cfg{8, 2, 4, 0};
+    hy_batch_config cfg{8, 1, 4, 0, 1};
     ShadeArgs base{};
     const void *kernel = nullptr;
     size_t smem = 0;
@@ -174,7 +214,8 @@ namespace {
 bool valid_config(const hy_batch_config &c) {
     const bool tw = c.tile_w == 4 || c.tile_w == 8 || c.tile_w == 16 || c.tile_w == 32;
     return tw && c.grab >= 1 && c.grab <= 16 && c.block_warps >= 1 &&
-           c.block_warps * 32 <= kMaxBlockThreads && c.blocks_per_sm >= 0 && c.blocks_per_sm <= 32;
+           c.block_warps * 32 <= kMaxBlockThreads && c.blocks_per_sm >= 0 &&
+           c.blocks_per_sm <= 32 && (c.block_queue == 0 || c.block_queue == 1);
 }
 
 void drop_graph(hy_batch *b) {
@@ -184,10 +225,21 @@ void drop_graph(hy_batch *b) {
     b->graph_count = -1;
 }
 
+void unit_shape(const hy_batch_config &c, int &bx, int &by) {
+    if (!c.block_queue) {
+        bx = by = 1;
+        return;
+    }
+    bx = (c.block_warps >= 4 && c.block_warps % 2 == 0) ? 2 : c.block_warps;
+    by = c.block_warps / bx;
+}
+
 // (Re)build the tile layout for the current config and the persistent grid.
 int layout(hy_batch *b) {
     hy_ctx *ctx = b->ctx;
-    const int tw = b->cfg.tile_w, th = 32 / tw;
+    int bx, by;
+    unit_shape(b->cfg, bx, by);
+    const int tw = b->cfg.tile_w * bx, th = (32 / b->cfg.tile_w) * by;
     b->views.resize(b->in.size());
     b->starts.resize(b->in.size());
     long long tile = 0;
@@ -247,6 +299,8 @@ int launch(hy_batch *b, uint8_t *out) {
         args.tile_w = b->cfg.tile_w;
         args.tile_h = 32 / b->cfg.tile_w;
         args.grab = b->cfg.grab;
+        args.block_queue = b->cfg.block_queue;
+        unit_shape(b->cfg, args.bx, args.by);
         args.queue = b->queue_dev;
         args.out = out;
         void *kargs[] = {&args};
@@ -398,10 +452,11 @@ extern "C" int hy_batch_autotune(hy_batch *b, uint8_t *rgba_dev, int32_t reps,
     HY_CUDA(ctx, cudaEventCreate(&e0));
     HY_CUDA(ctx, cudaEventCreate(&e1));
     int rc = HY_OK;
+    for (int bq = 0; bq < 2; ++bq)
     for (int tw : tws)
         for (int g : grabs)
             for (int w : warps) {
-                hy_batch_config c{tw, g, w, 0};
+                hy_batch_config c{tw, g, w, 0, bq};
                 b->cfg = c;
                 if ((rc = layout(b))) goto done;
                 if ((rc = launch(b, rgba_dev))) goto done;  // warm-up and graph build

@@ -249,6 +249,8 @@ typedef struct hy_batch_config {
     int32_t grab;          /* warp tiles taken per queue access, 1..16 */
     int32_t block_warps;   /* warps per block, 1..8 */
     int32_t blocks_per_sm; /* persistent blocks per SM; 0 = as many as fit */
+    int32_t block_queue;   /* 0: each warp takes warp tiles; 1: each block takes a block
+                              tile and its warps shade neighbouring warp tiles */
 } hy_batch_config;
 
 int hy_batch_create(hy_ctx *ctx, const hy_volume *vol, const hy_shader_params *params,
@@ -264,8 +266,10 @@ int hy_batch_set_counting(hy_batch *batch, int32_t count_samples);
 int hy_batch_render_device(hy_batch *batch, uint8_t *rgba_dev);
 /* Host output; returns when the images are on the host. */
 int hy_batch_render(hy_batch *batch, uint8_t *rgba_host);
-/* Times every launch shape (tile 8x4/4x8/16x2, grab 1/2/4, 2/4/8 warps per
- * block) on this batch and keeps the fastest; it is returned in *best. */
+/* Times every launch shape (queue per warp or per block, tile 8x4/4x8/16x2,
+ * grab 1/2/4, 2/4/8 warps per block) on this batch and keeps the fastest;
+ * it is returned in *best.  For the Isosurface shader, params->to_world must
+ * be set (hy_iso_lighting) when the batch is created. */
 int hy_batch_autotune(hy_batch *batch, uint8_t *rgba_dev, int32_t reps, hy_batch_config *best);
 
 #ifdef __cplusplus

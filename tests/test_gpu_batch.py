@@ -63,11 +63,15 @@ def test_batch_equals_per_view(ctx, tubes, kw):
     views, cams = _views(tubes, SIZES)
     ref, ref_samples = _per_view(ctx, tubes, kw, views, cams)
     p = hy.shader_params(**kw)
-    light = _lighting(tubes, cams, kw) if p.shader == hy._abi.SHADER_ISOSURFACE else None
+    light = None
+    if p.shader == hy._abi.SHADER_ISOSURFACE:
+        light = _lighting(tubes, cams, kw)
+        hy.iso_lighting(tubes, cams[0], p)  # to_world of the volume
     b = hy.Batch(ctx, tubes, p, views, light)
     try:
         b.set_counting(True)
-        for cfg in [(8, 1, 4), (4, 2, 2), (16, 4, 8), (32, 3, 1)]:
+        for cfg in [(8, 1, 4, 0, 1), (4, 2, 2, 0, 0), (16, 4, 8, 0, 1), (32, 3, 1, 0, 0),
+                    (8, 2, 8, 2, 1), (4, 1, 6, 0, 1)]:
             b.set_config(*cfg)
             got = b.render()
             assert ctx.stats().samples == ref_samples
