@@ -91,13 +91,16 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def profile_traffic_per_sample():
-    """dram bytes per brick sample from the committed ncu summary, if any."""
-    p = ROOT / "profiles" / "render_kernel_multiview.txt"
+def profile_traffic_per_sample(block_queue: int):
+    """DRAM bytes per brick sample of the batch kernel, from the committed ncu
+    summary (one capture of 4 views of the same volume; traffic grows with
+    the samples processed, so it is scaled to a full launch by samples)."""
+    p = ROOT / "profiles" / "batch_kernel_multiview.txt"
     if not p.exists():
         return None
+    tag = f"dram_bytes_per_sample[block_queue={block_queue}]:"
     for line in p.read_text().splitlines():
-        if line.startswith("dram_bytes_per_sample:"):
+        if line.startswith(tag):
             try:
                 return float(line.split(":", 1)[1].split()[0])
             except ValueError:
@@ -379,7 +382,7 @@ def main_ours(args):
     hbm, peak_kind = measured_peaks()
     mean_launch_s = t / args.steps  # one batch kernel per step
     achieved = samples * BYTES_PER_SAMPLE / mean_launch_s / 1e9
-    tps = profile_traffic_per_sample()
+    tps = profile_traffic_per_sample(int(tuned.get("block_queue", 1)))
     if rank == 0:
         cpu = None
         if not args.no_cpu_baseline:
