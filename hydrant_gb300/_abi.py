@@ -145,6 +145,10 @@ _PROTOS = {
     "hy_batch_render_device": (C.c_int, [P, P]),
     "hy_batch_render": (C.c_int, [P, P]),
     "hy_batch_autotune": (C.c_int, [P, P, C.c_int32, C.POINTER(HyBatchConfig)]),
+    "hy_render_views_noalloc": (
+        C.c_int,
+        [P, P, C.POINTER(HyShaderParams), C.POINTER(HyBatchView), C.c_int32, P],
+    ),
     "hy_synth_blobs_u8": (C.c_int, [C.c_uint64, P, C.c_int32, P, C.c_int32]),
     "hy_synth_blobs_f32": (C.c_int, [C.c_uint64, P, C.c_int32, P, C.c_int32]),
     "hy_synth_tubes_u8": (C.c_int, [C.c_uint64, P, C.c_int32, P, C.c_int32]),

@@ -14,6 +14,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "hy_shade.cuh"
@@ -482,5 +483,150 @@ done:
     rc = layout(b);
     if (rc) return rc;
     if (best_out) *best_out = best;
+    return HY_OK;
+}
+
+// ---- rendering a batch of views without allocating ---------------------------
+//
+// hy_render_views_noalloc is for callers that may not allocate device memory
+// while they render: a host application that owns the GPU's memory budget and
+// only lends this library its inputs and outputs, or a real-time frame loop
+// that cannot afford the implicit synchronisation and fragmentation of
+// cudaMalloc/cudaFree in the middle of a frame.  It renders like
+// hy_batch_render_device with the default launch shape, but keeps its scratch
+// -- the work-queue head, the first tile of each view and the per-view
+// descriptors -- in the file-scope array below instead of device allocations.
+//
+// The array is a fixed kNoAllocScratchBytes (about 33 KiB) that every GPU
+// which loads this library holds until the process exits.  Its device address
+// is looked up once per device, on the first call made on that device (with
+// the device made current), so that first call should come before any stream
+// capture.  All calls share the array and it keeps the last call's contents:
+// each call rewrites the descriptors and clears the queue head on its stream
+// before launching, and calls whose work overlaps on the GPU (other streams,
+// other host threads, several contexts on one device) race on it.
+
+constexpr int kNoAllocMaxViews = 256;
+constexpr size_t kNoAllocQueueBytes = 256;
+constexpr size_t kNoAllocStartsBytes = (kNoAllocMaxViews * sizeof(int) + 255) / 256 * 256;
+constexpr size_t kNoAllocScratchBytes =
+    kNoAllocQueueBytes + kNoAllocStartsBytes + kNoAllocMaxViews * sizeof(BatchView);
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+namespace {
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+unsigned char *g_noalloc_addr[kNoAllocMaxDevices] = {};
+
+// Device address of g_noalloc_scratch on ctx's device (host code cannot use
+// the symbol itself: on the host it names a stand-in, not device memory).
+int noalloc_scratch(hy_ctx *ctx, unsigned char **out) {
+    if (ctx->device < 0 || ctx->device >= kNoAllocMaxDevices)
+        return hy_fail(ctx, HY_ERR_INVALID, "noalloc: device index out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_addr[ctx->device]) {
+        HY_CUDA(ctx, cudaSetDevice(ctx->device));
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return hy_cuda_fail(ctx, e, "noalloc: cudaGetSymbolAddress(scratch)");
+        g_noalloc_addr[ctx->device] = static_cast<unsigned char *>(p);
+    }
+    *out = g_noalloc_addr[ctx->device];
+    return HY_OK;
+}
+
+}  // namespace
+
+extern "C" int hy_render_views_noalloc(hy_ctx *ctx, const hy_volume *vol,
+                                       const hy_shader_params *params,
+                                       const hy_batch_view *views, int32_t nviews,
+                                       uint8_t *rgba_dev) {
+    if (!ctx) return HY_ERR_INVALID;
+    if (!views || !rgba_dev) return hy_fail(ctx, HY_ERR_INVALID, "noalloc: null views or output");
+    if (nviews <= 0 || nviews > kNoAllocMaxViews)
+        return hy_fail(ctx, HY_ERR_INVALID,
+                       "noalloc: nviews must be 1..256 (the static scratch holds 256 views)");
+    ShadeArgs base;
+    int rc = hy_fill_args(ctx, vol, params, nullptr, 1, 1, &base);
+    if (rc) return rc;
+    base.count = 0;  // sample counting is not available on this entry point
+    unsigned char *scratch = nullptr;
+    rc = noalloc_scratch(ctx, &scratch);
+    if (rc) return rc;
+    HY_CUDA(ctx, cudaSetDevice(ctx->device));
+
+    // default launch shape: 8x4 warp tiles, block tiles of 2x2 warp tiles,
+    // one block tile per queue access
+    const hy_batch_config cfg{8, 1, 4, 0, 1};
+    int bx, by;
+    unit_shape(cfg, bx, by);
+    const int uw = cfg.tile_w * bx, uh = (32 / cfg.tile_w) * by;
+    BatchView hv[kNoAllocMaxViews];
+    int hs[kNoAllocMaxViews];
+    long long tile = 0;
+    for (int i = 0; i < nviews; ++i) {
+        const hy_batch_view &v = views[i];
+        if (v.width <= 0 || v.height <= 0 || v.rgba_offset < 0 || (v.rgba_offset & 3))
+            return hy_fail(ctx, HY_ERR_INVALID, "noalloc: bad view size or output offset");
+        BatchView &d = hv[i];
+        std::memset(&d, 0, sizeof(d));
+        std::memcpy(d.view.trans, v.view.trans, sizeof(d.view.trans));
+        d.view.ctg = v.view.ctg_fovy_2;
+        for (int k = 0; k < 3; ++k) {
+            d.view.ray_o[k] = v.view.ray_o[k];
+            d.view.eye[k] = v.eye_pos[k];
+            d.view.light[k] = v.light_pos[k];
+        }
+        d.view.W = v.width;
+        d.view.H = v.height;
+        d.out_off = v.rgba_offset;
+        d.tiles_x = (v.width + uw - 1) / uw;
+        d.tile0 = int(tile);
+        hs[i] = int(tile);
+        tile += (long long)d.tiles_x * ((v.height + uh - 1) / uh);
+        if (tile >= (1ll << 31) - 64) return hy_fail(ctx, HY_ERR_INVALID, "noalloc: too many tiles");
+    }
+    unsigned int *queue = reinterpret_cast<unsigned int *>(scratch);
+    int *starts = reinterpret_cast<int *>(scratch + kNoAllocQueueBytes);
+    BatchView *vdev = reinterpret_cast<BatchView *>(scratch + kNoAllocQueueBytes + kNoAllocStartsBytes);
+    HY_CUDA(ctx, cudaMemcpyAsync(vdev, hv, size_t(nviews) * sizeof(BatchView),
+                                 cudaMemcpyHostToDevice, ctx->stream));
+    HY_CUDA(ctx, cudaMemcpyAsync(starts, hs, size_t(nviews) * sizeof(int), cudaMemcpyHostToDevice,
+                                 ctx->stream));
+    HY_CUDA(ctx, cudaMemsetAsync(queue, 0, sizeof(unsigned int), ctx->stream));
+
+    BatchArgs args;
+    args.A = base;
+    args.views = vdev;
+    args.starts = starts;
+    args.nviews = nviews;
+    args.total_tiles = int(tile);
+    args.tile_w = cfg.tile_w;
+    args.tile_h = 32 / cfg.tile_w;
+    args.grab = cfg.grab;
+    args.block_queue = cfg.block_queue;
+    args.bx = bx;
+    args.by = by;
+    args.queue = queue;
+    args.out = rgba_dev;
+    const void *kernel = pick_kernel(base);
+    const int threads = cfg.block_warps * 32;
+    const size_t smem = size_t(base.ntf) * sizeof(float4) + 256 * sizeof(float) +
+                        size_t(nviews) * sizeof(int);
+    int per_sm = 0, sms = 0;
+    HY_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem));
+    HY_CUDA(ctx, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+    void *kargs[] = {&args};
+    HY_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
+    HY_CUDA(ctx, cudaLaunchKernel(kernel, dim3(sms * std::max(per_sm, 1)), dim3(threads), kargs,
+                                  smem, ctx->stream));
+    HY_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
+    ctx->stats_pending = true;
+    ctx->pend_count = 0;
+    int64_t px = 0;
+    for (int i = 0; i < nviews; ++i) px += (int64_t)views[i].width * views[i].height;
+    ctx->pend_pixels = px;
     return HY_OK;
 }

@@ -272,6 +272,20 @@ int hy_batch_render(hy_batch *batch, uint8_t *rgba_host);
  * be set (hy_iso_lighting) when the batch is created. */
 int hy_batch_autotune(hy_batch *batch, uint8_t *rgba_dev, int32_t reps, hy_batch_config *best);
 
+/* Renders up to 256 views into rgba_dev like hy_batch_render_device (default
+ * launch shape, same images), allocating nothing.  No counterpart in the
+ * reference.  For callers that may not allocate device memory while they
+ * render -- a host application that owns the GPU memory budget and only
+ * lends its inputs and outputs, or a frame loop that cannot take the
+ * synchronisation cost of cudaMalloc/cudaFree mid-frame.  Scratch lives in a
+ * fixed ~33 KiB static device array that every GPU loading the library keeps
+ * until exit; the first call on a device looks up its address and should
+ * come before any stream capture.  Calls share that array: calls that overlap
+ * on the GPU race.  More than 256 views is rejected with HY_ERR_INVALID.
+ * Asynchronous on the context's stream; count_samples is ignored. */
+int hy_render_views_noalloc(hy_ctx *ctx, const hy_volume *vol, const hy_shader_params *params,
+                            const hy_batch_view *views, int32_t nviews, uint8_t *rgba_dev);
+
 #ifdef __cplusplus
 }
 #endif
