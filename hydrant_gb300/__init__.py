@@ -11,9 +11,12 @@ from .api import (  # noqa: F401
     Context,
     RenderResult,
     Volume,
+    Pager,
+    Store,
     camera_orbit,
     camera_ptu,
     camera_view,
+    cull,
     iso_lighting,
     render,
     render_device,

@@ -99,6 +99,18 @@ class HyBatchConfig(C.Structure):
     ]
 
 
+PAGER_LOSSLESS, PAGER_REALTIME = 0, 1
+
+
+class HyPagerDesc(C.Structure):
+    _fields_ = [("slots", C.c_int32), ("mode", C.c_int32), ("max_uploads_per_frame", C.c_int32)]
+
+
+class HyPagerStats(C.Structure):
+    _fields_ = [(n, C.c_int64) for n in ("frames", "passes", "uploads", "upload_bytes", "hits",
+                                         "misses", "evictions", "visible")]
+
+
 class HyRenderStats(C.Structure):
     _fields_ = [("samples", C.c_int64), ("pixels", C.c_int64), ("ms", C.c_float)]
 
@@ -149,6 +161,21 @@ _PROTOS = {
         C.c_int,
         [P, P, C.POINTER(HyShaderParams), C.POINTER(HyBatchView), C.c_int32, P],
     ),
+    "hy_store_from_volume": (C.c_int, [P, C.POINTER(P)]),
+    "hy_store_create_noise": (
+        C.c_int, [P, C.POINTER(HyVolumeDesc), C.c_uint64, C.c_float, C.c_float, C.POINTER(P)]),
+    "hy_store_destroy": (C.c_int, [P]),
+    "hy_store_get_info": (C.c_int, [P, C.POINTER(HyVolumeInfo)]),
+    "hy_store_thumbnails": (C.c_int, [P, P, P]),
+    "hy_store_brick": (C.c_int, [P, C.c_int32, P]),
+    "hy_cull": (C.c_int, [P, C.POINTER(HyView), P, C.c_int32, P, P, C.POINTER(C.c_int32)]),
+    "hy_pager_create": (C.c_int, [P, P, C.POINTER(HyPagerDesc), C.POINTER(P)]),
+    "hy_pager_destroy": (C.c_int, [P]),
+    "hy_pager_volume": (C.c_int, [P, C.POINTER(P)]),
+    "hy_pager_stats_get": (C.c_int, [P, C.POINTER(HyPagerStats)]),
+    "hy_pager_present": (C.c_int, [P, P]),
+    "hy_pager_render": (
+        C.c_int, [P, C.POINTER(HyShaderParams), C.POINTER(HyCamera), C.c_int32, C.c_int32, P]),
     "hy_synth_blobs_u8": (C.c_int, [C.c_uint64, P, C.c_int32, P, C.c_int32]),
     "hy_synth_blobs_f32": (C.c_int, [C.c_uint64, P, C.c_int32, P, C.c_int32]),
     "hy_synth_tubes_u8": (C.c_int, [C.c_uint64, P, C.c_int32, P, C.c_int32]),

@@ -327,3 +327,112 @@ class Batch:
         c = HyBatchConfig()
         self.ctx.check(lib().hy_batch_autotune(self.handle, C.c_void_p(rgba_ptr), reps, C.byref(c)))
         return c
+
+
+def cull(vol, view: HyView, limit: int = -1, rect=None):
+    """hy_cull: visible non-empty bricks (ids in index order, squared distances)."""
+    n = vol.info.nbricks
+    ids = np.zeros(n, np.int32)
+    d2 = np.zeros(n, np.float32)
+    k = C.c_int32()
+    r = None if rect is None else np.ascontiguousarray(rect, np.float32)
+    vol.ctx.check(lib().hy_cull(vol.handle, C.byref(view), _ptr(r), limit, _ptr(ids), _ptr(d2),
+                                C.byref(k)))
+    return ids[: k.value].copy(), d2[: k.value].copy()
+
+
+class Store:
+    """Pinned host brick store (hy_store)."""
+
+    def __init__(self, ctx: Context, handle):
+        self.ctx = ctx
+        self.handle = handle
+
+    @classmethod
+    def from_volume(cls, vol: Volume) -> "Store":
+        h = C.c_void_p()
+        vol.ctx.check(lib().hy_store_from_volume(vol.handle, C.byref(h)))
+        return cls(vol.ctx, h)
+
+    @classmethod
+    def noise(cls, ctx: Context, dim, block_size: int, padding: int, seed: int,
+              cell_voxels: float, occupancy: float) -> "Store":
+        desc = HyVolumeDesc(tuple(dim), block_size, padding, _abi.DTYPE_U8)
+        h = C.c_void_p()
+        ctx.check(lib().hy_store_create_noise(ctx.handle, C.byref(desc), seed, cell_voxels,
+                                              occupancy, C.byref(h)))
+        return cls(ctx, h)
+
+    def close(self) -> None:
+        if self.handle:
+            lib().hy_store_destroy(self.handle)
+            self.handle = None
+
+    @property
+    def info(self) -> HyVolumeInfo:
+        i = HyVolumeInfo()
+        self.ctx.check(lib().hy_store_get_info(self.handle, C.byref(i)))
+        return i
+
+    def thumbnails(self):
+        i = self.info
+        cheb = np.zeros(i.nbricks, np.int32)
+        mean = np.zeros(i.nbricks, np.float32)
+        self.ctx.check(lib().hy_store_thumbnails(self.handle, _ptr(cheb), _ptr(mean)))
+        return cheb, mean
+
+    def brick(self, b: int, dtype=np.uint8) -> np.ndarray:
+        P = self.info.padded
+        out = np.zeros(P ** 3, dtype)
+        self.ctx.check(lib().hy_store_brick(self.handle, b, _ptr(out)))
+        return out.reshape(P, P, P)
+
+
+class _PagedVolume:
+    """Non-owning view of a pager's volume, usable wherever a Volume is."""
+
+    def __init__(self, ctx, handle):
+        self.ctx = ctx
+        self.handle = handle
+
+    @property
+    def info(self) -> HyVolumeInfo:
+        i = HyVolumeInfo()
+        self.ctx.check(lib().hy_volume_get_info(self.handle, C.byref(i)))
+        return i
+
+
+class Pager:
+    """Brick cache kept filled from a Store (hy_pager)."""
+
+    def __init__(self, ctx: Context, store: Store, slots: int, mode: int = _abi.PAGER_REALTIME,
+                 max_uploads_per_frame: int = 0):
+        self.ctx = ctx
+        d = _abi.HyPagerDesc(slots, mode, max_uploads_per_frame)
+        h = C.c_void_p()
+        ctx.check(lib().hy_pager_create(ctx.handle, store.handle, C.byref(d), C.byref(h)))
+        self.handle = h
+        vh = C.c_void_p()
+        ctx.check(lib().hy_pager_volume(self.handle, C.byref(vh)))
+        self.volume = _PagedVolume(ctx, vh)
+
+    def close(self) -> None:
+        if self.handle:
+            lib().hy_pager_destroy(self.handle)
+            self.handle = None
+
+    def render(self, params: HyShaderParams, cam: HyCamera, width: int, height: int,
+               rgba_ptr: int) -> None:
+        self.ctx.check(lib().hy_pager_render(self.handle, C.byref(params), C.byref(cam), width,
+                                             height, C.c_void_p(rgba_ptr)))
+
+    def stats(self) -> dict:
+        s = _abi.HyPagerStats()
+        self.ctx.check(lib().hy_pager_stats_get(self.handle, C.byref(s)))
+        return {n: int(getattr(s, n)) for n, _ in _abi.HyPagerStats._fields_}
+
+    def present(self) -> np.ndarray:
+        n = self.volume.info.nbricks
+        m = np.zeros(n, np.uint8)
+        self.ctx.check(lib().hy_pager_present(self.handle, _ptr(m)))
+        return m

@@ -117,7 +117,10 @@ struct hy_volume {
     float bbox_max[3] = {0, 0, 0};
     float du = 0.f;
     bool uploaded = false;
+    bool paged = false;       // pool is a brick cache owned by a hy_pager
 };
+
+int hy_volume_init(hy_ctx *ctx, const hy_volume_desc *desc, hy_volume *v);
 
 // error helpers (hy_api.cc)
 int hy_fail(hy_ctx *ctx, int code, const std::string &msg);

@@ -1,0 +1,930 @@
+// hy_page.cu -- out-of-core volumes: a pinned host brick store, visible-brick
+// culling on the GPU, and a pager that keeps a fixed HBM brick cache filled.
+//
+// Reference: LosslessBlockPagingServer (src/slave/paging/
+// lossless_block_paging.cc:116-174) renders a frame in batches of resident
+// bricks, nearest first, re-emitting nothing: rays that reach an absent brick
+// stop (volume_shader.cu:49-50) and the next batch's march pass resumes them.
+// RtBlockPagingServer (src/slave/paging/rt_block_paging.cc:249-326) keeps the
+// nearest visible bricks resident across frames, replacing bricks that left
+// the visible set.  Both take the visible set from OctreeCuller::cull
+// (include/hydrant/octree_culler.hpp:121-161).
+//
+// Here the bricks live in one pinned host allocation (the "store"), laid out
+// exactly like device slots, so a brick upload is a single DMA
+// (cudaMemcpyAsync) on a copy stream; the page table (int2 per brick) is
+// rewritten on the render stream after an event says the bricks arrived.  In
+// lossless mode the cache is double-buffered: batch k+1 uploads into the
+// other half while batch k marches.
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#include "hy_shade.cuh"
+
+using namespace hy;
+using namespace hy::dev;
+
+// ---------------------------------------------------------------------------
+// Brick store
+// ---------------------------------------------------------------------------
+struct hy_store {
+    hy_ctx *ctx = nullptr;
+    hy_volume_desc desc{};
+    int grid[3] = {0, 0, 0};
+    int nbricks = 0;
+    int P = 0;
+    size_t slot_stride = 0;
+    std::vector<int> cheb;
+    std::vector<float> mean;
+    std::vector<long long> offset;  // brick -> byte offset in `host`, -1 if empty
+    unsigned char *host = nullptr;  // pinned
+    size_t host_bytes = 0;
+    int nonempty = 0;
+};
+
+namespace {
+
+int store_alloc(hy_store *s, int nonempty) {
+    s->nonempty = nonempty;
+    s->host_bytes = std::max<size_t>(1, size_t(nonempty)) * s->slot_stride;
+    HY_CUDA(s->ctx, cudaHostAlloc(reinterpret_cast<void **>(&s->host), s->host_bytes,
+                                  cudaHostAllocDefault));
+    return HY_OK;
+}
+
+// ---- procedural value noise (the 32 GiB paging workload) --------------------
+
+__device__ __forceinline__ unsigned int mix32(unsigned int h) {
+    h ^= h >> 16;
+    h *= 0x7feb352dU;
+    h ^= h >> 15;
+    h *= 0x846ca68bU;
+    h ^= h >> 16;
+    return h;
+}
+
+__device__ __forceinline__ float lattice(unsigned int seed, int o, int x, int y, int z) {
+    unsigned int h = mix32(seed ^ mix32(unsigned(o) * 0x9E3779B9U ^ mix32(unsigned(x) ^
+                                         mix32(unsigned(y) * 0x85EBCA6BU ^ mix32(unsigned(z))))));
+    return float(h >> 8) * (1.f / 16777216.f);
+}
+
+// one octave of lattice value noise with smoothstep weights at p (cells)
+__device__ __forceinline__ float value_noise(unsigned int seed, int o, float px, float py, float pz) {
+    const float fx = floorf(px), fy = floorf(py), fz = floorf(pz);
+    const int ix = int(fx), iy = int(fy), iz = int(fz);
+    float tx = px - fx, ty = py - fy, tz = pz - fz;
+    tx = tx * tx * (3.f - 2.f * tx);
+    ty = ty * ty * (3.f - 2.f * ty);
+    tz = tz * tz * (3.f - 2.f * tz);
+    float c[2][2];
+    for (int k = 0; k < 2; ++k)
+        for (int j = 0; j < 2; ++j) {
+            const float a = lattice(seed, o, ix, iy + j, iz + k);
+            const float b = lattice(seed, o, ix + 1, iy + j, iz + k);
+            c[k][j] = a + (b - a) * tx;
+        }
+    const float y0 = c[0][0] + (c[0][1] - c[0][0]) * ty;
+    const float y1 = c[1][0] + (c[1][1] - c[1][0]) * ty;
+    return y0 + (y1 - y0) * tz;
+}
+
+// 3 octaves (cell, cell/2, cell/4; amplitudes 1, 1/2, 1/4), normalised to [0,1)
+__device__ __forceinline__ float noise3(unsigned int seed, float inv_cell, int x, int y, int z) {
+    const float px = (float(x) + 0.5f) * inv_cell, py = (float(y) + 0.5f) * inv_cell,
+                pz = (float(z) + 0.5f) * inv_cell;
+    float n = value_noise(seed, 0, px, py, pz);
+    n += 0.5f * value_noise(seed, 1, 2.f * px, 2.f * py, 2.f * pz);
+    n += 0.25f * value_noise(seed, 2, 4.f * px, 4.f * py, 4.f * pz);
+    return n * (1.f / 1.75f);
+}
+
+__device__ __forceinline__ unsigned char noise_voxel(unsigned int seed, float inv_cell, float thr,
+                                                     int x, int y, int z) {
+    const float n = noise3(seed, inv_cell, x, y, z);
+    if (!(n > thr)) return 0;
+    const float v = 1.f + floorf(254.f * (n - thr) / (1.f - thr));
+    return (unsigned char)fminf(255.f, v);
+}
+
+// noise at hashed sample positions, for the occupancy threshold
+__global__ void noise_sample_kernel(unsigned int seed, float inv_cell, int dx, int dy, int dz,
+                                    int n, float *out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const unsigned int h1 = mix32(unsigned(i) * 2654435761U ^ 0x1234567U);
+    const unsigned int h2 = mix32(h1 ^ 0x9E3779B9U), h3 = mix32(h2 ^ 0x7F4A7C15U);
+    out[i] = noise3(seed, inv_cell, int(h1 % unsigned(dx)), int(h2 % unsigned(dy)),
+                    int(h3 % unsigned(dz)));
+}
+
+struct NoiseChunk {
+    unsigned int seed;
+    float inv_cell, thr;
+    int dx, dy, dz, bs, pad, gx, gy;
+    int brick0;
+    long long slot_stride;
+    unsigned char *out;         // chunk of padded bricks (nullptr: flags only)
+    unsigned int *nonempty;     // per brick of the chunk
+    unsigned long long *sum;    // per brick: sum of core voxels
+};
+
+// One block per brick of the chunk: padded voxels (apron clamped at the
+// volume border), emptiness and the core sum.
+__global__ void noise_brick_kernel(const __grid_constant__ NoiseChunk a) {
+    const int bid = a.brick0 + blockIdx.x;
+    const int bx = bid % a.gx, by = (bid / a.gx) % a.gy, bz = bid / (a.gx * a.gy);
+    const int P = a.bs + 2 * a.pad;
+    const long long P3 = (long long)P * P * P;
+    unsigned int any = 0;
+    unsigned long long sum = 0;
+    unsigned char *dst = a.out ? a.out + (long long)blockIdx.x * a.slot_stride : nullptr;
+    for (long long i = threadIdx.x; i < P3; i += blockDim.x) {
+        const int x = int(i % P), y = int((i / P) % P), z = int(i / ((long long)P * P));
+        const int X = min(max(bx * a.bs + x - a.pad, 0), a.dx - 1);
+        const int Y = min(max(by * a.bs + y - a.pad, 0), a.dy - 1);
+        const int Z = min(max(bz * a.bs + z - a.pad, 0), a.dz - 1);
+        const unsigned char v = noise_voxel(a.seed, a.inv_cell, a.thr, X, Y, Z);
+        if (dst) dst[i] = v;
+        any |= v != 0;
+        const bool core = x >= a.pad && x < a.pad + a.bs && y >= a.pad && y < a.pad + a.bs &&
+                          z >= a.pad && z < a.pad + a.bs;
+        if (core) sum += v;
+    }
+    __shared__ unsigned long long ssum[32];
+    __shared__ unsigned int sany[32];
+    for (int o = 16; o > 0; o >>= 1) {
+        sum += __shfl_down_sync(0xffffffffu, sum, o);
+        any |= __shfl_down_sync(0xffffffffu, any, o);
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+        ssum[warp] = sum;
+        sany[warp] = any;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long s = 0;
+        unsigned int an = 0;
+        for (int w = 0; w < int(blockDim.x >> 5); ++w) {
+            s += ssum[w];
+            an |= sany[w];
+        }
+        a.nonempty[blockIdx.x] = an;
+        a.sum[blockIdx.x] = s;
+    }
+}
+
+// Chebyshev distance transform over the brick grid (26-neighbour dilation).
+void cheb_transform(const std::vector<unsigned char> &ne, const int g[3], std::vector<int> &out) {
+    const int n = g[0] * g[1] * g[2];
+    const int cap = std::max(g[0], std::max(g[1], g[2]));
+    out.assign(n, -1);
+    std::vector<int> frontier;
+    for (int i = 0; i < n; ++i)
+        if (ne[i]) {
+            out[i] = 0;
+            frontier.push_back(i);
+        }
+    for (int r = 1; r <= cap && !frontier.empty(); ++r) {
+        std::vector<int> next;
+        for (int id : frontier) {
+            const int x = id % g[0], y = (id / g[0]) % g[1], z = id / (g[0] * g[1]);
+            for (int k = 0; k < 27; ++k) {
+                const int X = x + k % 3 - 1, Y = y + (k / 3) % 3 - 1, Z = z + k / 9 - 1;
+                if (X < 0 || Y < 0 || Z < 0 || X >= g[0] || Y >= g[1] || Z >= g[2]) continue;
+                const int j = (Z * g[1] + Y) * g[0] + X;
+                if (out[j] < 0) {
+                    out[j] = r;
+                    next.push_back(j);
+                }
+            }
+        }
+        frontier.swap(next);
+    }
+    for (int i = 0; i < n; ++i)
+        if (out[i] < 0) out[i] = cap;
+}
+
+void store_geometry(hy_store *s, const hy_volume_desc &d) {
+    s->desc = d;
+    for (int i = 0; i < 3; ++i) s->grid[i] = (d.dim[i] + d.block_size - 1) / d.block_size;
+    s->nbricks = s->grid[0] * s->grid[1] * s->grid[2];
+    s->P = d.block_size + 2 * d.padding;
+    const size_t elem = d.dtype == HY_DTYPE_U8 ? 1 : 4;
+    s->slot_stride = (size_t(s->P) * s->P * s->P * elem + 255) / 256 * 256;
+}
+
+}  // namespace
+
+extern "C" int hy_store_from_volume(const hy_volume *vol, hy_store **out) {
+    if (!vol || !out) return HY_ERR_INVALID;
+    *out = nullptr;
+    hy_ctx *ctx = vol->ctx;
+    if (!vol->uploaded || vol->paged)
+        return hy_fail(ctx, HY_ERR_STATE, "store: needs a resident, uploaded volume");
+    hy_store *s = new hy_store();
+    s->ctx = ctx;
+    store_geometry(s, vol->desc);
+    s->cheb = vol->cheb;
+    s->mean = vol->mean;
+    s->offset.assign(s->nbricks, -1);
+    int rc = store_alloc(s, vol->resident);
+    if (rc) {
+        delete s;
+        return rc;
+    }
+    for (int b = 0; b < s->nbricks; ++b)
+        if (vol->reg_of_brick[b] >= 0) s->offset[b] = (long long)vol->reg_of_brick[b] * s->slot_stride;
+    cudaError_t e = cudaMemcpyAsync(s->host, vol->pool, size_t(vol->resident) * s->slot_stride,
+                                    cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) {
+        hy_store_destroy(s);
+        return hy_cuda_fail(ctx, e, "store: copy bricks to host");
+    }
+    *out = s;
+    return HY_OK;
+}
+
+extern "C" int hy_store_create_noise(hy_ctx *ctx, const hy_volume_desc *desc, uint64_t seed,
+                                     float cell_voxels, float occupancy, hy_store **out) {
+    if (!ctx || !desc || !out) return HY_ERR_INVALID;
+    *out = nullptr;
+    if (desc->dtype != HY_DTYPE_U8) return hy_fail(ctx, HY_ERR_INVALID, "noise store: u8 only");
+    if (!(cell_voxels >= 1.f) || !(occupancy > 0.f && occupancy < 1.f))
+        return hy_fail(ctx, HY_ERR_INVALID, "noise store: bad cell size or occupancy");
+    hy_volume tmp;
+    int rc = hy_volume_init(ctx, desc, &tmp);
+    if (rc) return rc;
+    HY_CUDA(ctx, cudaSetDevice(ctx->device));
+    hy_store *s = new hy_store();
+    s->ctx = ctx;
+    store_geometry(s, *desc);
+    const unsigned int sd = unsigned(seed ^ (seed >> 32));
+    const float inv_cell = 1.f / cell_voxels;
+    // occupancy threshold: the (1 - occupancy) quantile of 2^22 sampled voxels
+    const int ns = 1 << 22;
+    float *samp = nullptr;
+    unsigned char *chunk = nullptr;
+    unsigned int *ne_dev = nullptr;
+    unsigned long long *sum_dev = nullptr;
+    const int CH = 512;
+    auto fail = [&](cudaError_t e, const char *what) {
+        if (samp) cudaFree(samp);
+        if (chunk) cudaFree(chunk);
+        if (ne_dev) cudaFree(ne_dev);
+        if (sum_dev) cudaFree(sum_dev);
+        hy_store_destroy(s);
+        return hy_cuda_fail(ctx, e, what);
+    };
+    cudaError_t e = cudaMalloc(&samp, ns * sizeof(float));
+    if (e != cudaSuccess) return fail(e, "noise store: sample buffer");
+    noise_sample_kernel<<<(ns + 255) / 256, 256, 0, ctx->stream>>>(sd, inv_cell, desc->dim[0],
+                                                                   desc->dim[1], desc->dim[2], ns,
+                                                                   samp);
+    std::vector<float> hs(ns);
+    e = cudaMemcpyAsync(hs.data(), samp, ns * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return fail(e, "noise store: threshold samples");
+    const size_t q = size_t(double(ns) * (1.0 - double(occupancy)));
+    std::nth_element(hs.begin(), hs.begin() + q, hs.end());
+    const float thr = hs[q];
+    e = cudaMalloc(&chunk, size_t(CH) * s->slot_stride);
+    if (e == cudaSuccess) e = cudaMalloc(&ne_dev, CH * sizeof(unsigned int));
+    if (e == cudaSuccess) e = cudaMalloc(&sum_dev, CH * sizeof(unsigned long long));
+    if (e != cudaSuccess) return fail(e, "noise store: chunk buffers");
+    NoiseChunk a{sd, inv_cell, thr, desc->dim[0], desc->dim[1], desc->dim[2], desc->block_size,
+                 desc->padding, s->grid[0], s->grid[1], 0, (long long)s->slot_stride, nullptr,
+                 ne_dev, sum_dev};
+    // pass 1: emptiness and means
+    std::vector<unsigned char> ne(s->nbricks);
+    std::vector<unsigned long long> sums(s->nbricks);
+    std::vector<unsigned int> nb(CH);
+    for (int b0 = 0; b0 < s->nbricks; b0 += CH) {
+        const int n = std::min(CH, s->nbricks - b0);
+        a.brick0 = b0;
+        a.out = nullptr;
+        noise_brick_kernel<<<n, 256, 0, ctx->stream>>>(a);
+        e = cudaMemcpyAsync(nb.data(), ne_dev, n * sizeof(unsigned int), cudaMemcpyDeviceToHost,
+                            ctx->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(&sums[b0], sum_dev, n * sizeof(unsigned long long),
+                                cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) return fail(e, "noise store: emptiness pass");
+        for (int i = 0; i < n; ++i) ne[b0 + i] = nb[i] ? 1 : 0;
+    }
+    cheb_transform(ne, s->grid, s->cheb);
+    const double ncore = double(desc->block_size) * desc->block_size * desc->block_size;
+    s->mean.resize(s->nbricks);
+    s->offset.assign(s->nbricks, -1);
+    int nonempty = 0;
+    for (int b = 0; b < s->nbricks; ++b) {
+        s->mean[b] = float(double(sums[b]) / 255.0 / ncore);
+        if (ne[b]) s->offset[b] = (long long)(nonempty++) * s->slot_stride;
+    }
+    rc = store_alloc(s, nonempty);
+    if (rc) {
+        cudaFree(samp);
+        cudaFree(chunk);
+        cudaFree(ne_dev);
+        cudaFree(sum_dev);
+        hy_store_destroy(s);
+        return rc;
+    }
+    // pass 2: generate and copy the non-empty bricks into the pinned store
+    for (int b0 = 0; b0 < s->nbricks; b0 += CH) {
+        const int n = std::min(CH, s->nbricks - b0);
+        bool any = false;
+        for (int i = 0; i < n; ++i) any |= ne[b0 + i] != 0;
+        if (!any) continue;
+        a.brick0 = b0;
+        a.out = chunk;
+        noise_brick_kernel<<<n, 256, 0, ctx->stream>>>(a);
+        for (int i = 0; i < n; ++i)
+            if (ne[b0 + i]) {
+                e = cudaMemcpyAsync(s->host + s->offset[b0 + i], chunk + size_t(i) * s->slot_stride,
+                                    s->slot_stride, cudaMemcpyDeviceToHost, ctx->stream);
+                if (e != cudaSuccess) return fail(e, "noise store: brick copy");
+            }
+        e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) return fail(e, "noise store: generation pass");
+    }
+    cudaFree(samp);
+    cudaFree(chunk);
+    cudaFree(ne_dev);
+    cudaFree(sum_dev);
+    *out = s;
+    return HY_OK;
+}
+
+extern "C" int hy_store_destroy(hy_store *s) {
+    if (!s) return HY_OK;
+    if (s->host) cudaFreeHost(s->host);
+    delete s;
+    return HY_OK;
+}
+
+extern "C" int hy_store_get_info(const hy_store *s, hy_volume_info *out) {
+    if (!s || !out) return HY_ERR_INVALID;
+    for (int i = 0; i < 3; ++i) {
+        out->grid[i] = s->grid[i];
+        out->bbox_max[i] = float(s->desc.dim[i]) / float(s->desc.block_size);
+    }
+    out->nbricks = s->nbricks;
+    out->nonempty = s->nonempty;
+    out->resident = 0;
+    out->padded = s->P;
+    out->slot_bytes = (int64_t)s->slot_stride;
+    out->pool_bytes = (int64_t)s->host_bytes;
+    return HY_OK;
+}
+
+extern "C" int hy_store_thumbnails(const hy_store *s, int32_t *chebyshev, float *mean) {
+    if (!s) return HY_ERR_INVALID;
+    for (int i = 0; i < s->nbricks; ++i) {
+        if (chebyshev) chebyshev[i] = s->cheb[i];
+        if (mean) mean[i] = s->mean[i];
+    }
+    return HY_OK;
+}
+
+extern "C" int hy_store_brick(const hy_store *s, int32_t brick, void *out) {
+    if (!s || !out || brick < 0 || brick >= s->nbricks) return HY_ERR_INVALID;
+    const size_t bytes = size_t(s->P) * s->P * s->P * (s->desc.dtype == HY_DTYPE_U8 ? 1 : 4);
+    if (s->offset[brick] < 0)
+        std::memset(out, 0, bytes);
+    else
+        std::memcpy(out, s->host + s->offset[brick], bytes);
+    return HY_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Visible-brick culling (OctreeCuller::cull, octree_culler.hpp:121-161).
+// Frustum: border rays at (+-1, +-1, -ctg) in camera space; plane normals
+// cross(border[i], border[i+1]) and the origin are taken to object space, the
+// border directions are used untransformed (octree_culler.hpp:324-345, as in
+// the reference).  A brick is visible if it is non-empty and contains_fast()
+// accepts its box: a corner inside all four planes, or a border ray from the
+// origin that hits the box with tfar > 0 (octree_culler.hpp:162-183).
+// ---------------------------------------------------------------------------
+namespace {
+
+struct CullArgs {
+    float norm[4][3];
+    float rdir[4][3];  // 1 / normalize(border[i])
+    float orig[3];
+    const int2 *info;
+    int gx, gy, gz;
+    int *ids;
+    float *d2;
+    unsigned int *count;
+};
+
+__device__ __forceinline__ bool frustum_contains(const CullArgs &a, float x, float y, float z) {
+    const float px = x - a.orig[0], py = y - a.orig[1], pz = z - a.orig[2];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+        if (!(a.norm[i][0] * px + a.norm[i][1] * py + a.norm[i][2] * pz > 0.f)) return false;
+    return true;
+}
+
+__global__ void cull_kernel(const __grid_constant__ CullArgs a) {
+    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= a.gx * a.gy * a.gz) return;
+    if (a.info[id].x != 0) return;
+    const int x = id % a.gx, y = (id / a.gx) % a.gy, z = id / (a.gx * a.gy);
+    const float x0 = float(x), y0 = float(y), z0 = float(z);
+    const float x1 = float(x + 1), y1 = float(y + 1), z1 = float(z + 1);
+    const float vx[2] = {x0, x1}, vy[2] = {y0, y1}, vz[2] = {z0, z1};
+    bool hit = false;
+    for (int i = 0; i < 2 && !hit; ++i)
+        for (int j = 0; j < 2 && !hit; ++j)
+            for (int k = 0; k < 2 && !hit; ++k) hit = frustum_contains(a, vx[i], vy[j], vz[k]);
+    for (int i = 0; i < 4 && !hit; ++i) {
+        float tnear, tfar;
+        if (intersect(a.orig[0], a.orig[1], a.orig[2], a.rdir[i][0], a.rdir[i][1], a.rdir[i][2], x0,
+                      y0, z0, x1, y1, z1, tnear, tfar) &&
+            tfar > 0.f)
+            hit = true;
+    }
+    if (!hit) return;
+    const float cx = x0 + .5f - a.orig[0], cy = y0 + .5f - a.orig[1], cz = z0 + .5f - a.orig[2];
+    const unsigned int slot = atomicAdd(a.count, 1u);
+    a.ids[slot] = id;
+    a.d2[slot] = cx * cx + cy * cy + cz * cz;
+}
+
+void hcross(const float a[3], const float b[3], float o[3]) {
+    o[0] = a[1] * b[2] - b[1] * a[2];
+    o[1] = a[2] * b[0] - b[2] * a[0];
+    o[2] = a[0] * b[1] - b[0] * a[1];
+}
+
+void host_frustum(const hy_view &v, const float rect[4], CullArgs &a) {
+    const float ctg = v.ctg_fovy_2;
+    const float border[4][3] = {{rect[2], rect[3], -ctg},
+                                {rect[2], rect[1], -ctg},
+                                {rect[0], rect[1], -ctg},
+                                {rect[0], rect[3], -ctg}};
+    const float *m = v.trans;
+    for (int i = 0; i < 4; ++i) {
+        float n[3];
+        hcross(border[i], border[(i + 1) % 4], n);
+        for (int r = 0; r < 3; ++r)
+            a.norm[i][r] = m[r] * n[0] + m[4 + r] * n[1] + m[8 + r] * n[2] + m[12 + r] * 0.f;
+        const float s = 1.f / std::sqrt(border[i][0] * border[i][0] + border[i][1] * border[i][1] +
+                                        border[i][2] * border[i][2]);
+        for (int r = 0; r < 3; ++r) a.rdir[i][r] = 1.f / (border[i][r] * s);
+    }
+    for (int r = 0; r < 3; ++r)
+        a.orig[r] = m[r] * 0.f + m[4 + r] * 0.f + m[8 + r] * 0.f + m[12 + r] * 1.f;
+}
+
+struct CullScratch {
+    int *ids = nullptr;
+    float *d2 = nullptr;
+    unsigned int *count = nullptr;
+    int cap = 0;
+};
+
+int run_cull(hy_ctx *ctx, const hy_volume *vol, const hy_view &view, const float rect_in[4],
+             int limit, CullScratch &cs, std::vector<int> &ids, std::vector<float> &d2) {
+    const float def_rect[4] = {-1.f, -1.f, 1.f, 1.f};
+    const float *rect = rect_in ? rect_in : def_rect;
+    if (cs.cap < vol->nbricks) {
+        if (cs.ids) cudaFree(cs.ids);
+        if (cs.d2) cudaFree(cs.d2);
+        if (cs.count) cudaFree(cs.count);
+        cs = CullScratch{};
+        HY_CUDA(ctx, cudaMalloc(&cs.ids, vol->nbricks * sizeof(int)));
+        HY_CUDA(ctx, cudaMalloc(&cs.d2, vol->nbricks * sizeof(float)));
+        HY_CUDA(ctx, cudaMalloc(&cs.count, sizeof(unsigned int)));
+        cs.cap = vol->nbricks;
+    }
+    CullArgs a;
+    host_frustum(view, rect, a);
+    a.info = vol->info_dev;
+    a.gx = vol->grid[0];
+    a.gy = vol->grid[1];
+    a.gz = vol->grid[2];
+    a.ids = cs.ids;
+    a.d2 = cs.d2;
+    a.count = cs.count;
+    HY_CUDA(ctx, cudaMemsetAsync(cs.count, 0, sizeof(unsigned int), ctx->stream));
+    cull_kernel<<<(vol->nbricks + 255) / 256, 256, 0, ctx->stream>>>(a);
+    HY_CUDA(ctx, cudaGetLastError());
+    unsigned int n = 0;
+    HY_CUDA(ctx, cudaMemcpyAsync(&n, cs.count, sizeof(n), cudaMemcpyDeviceToHost, ctx->stream));
+    HY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    std::vector<int> hid(n);
+    std::vector<float> hd(n);
+    if (n) {
+        HY_CUDA(ctx, cudaMemcpyAsync(hid.data(), cs.ids, n * sizeof(int), cudaMemcpyDeviceToHost,
+                                     ctx->stream));
+        HY_CUDA(ctx, cudaMemcpyAsync(hd.data(), cs.d2, n * sizeof(float), cudaMemcpyDeviceToHost,
+                                     ctx->stream));
+        HY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    std::vector<int> idx(n);
+    std::iota(idx.begin(), idx.end(), 0);
+    size_t keep = n;
+    if (limit >= 0 && size_t(limit) < n) {
+        // nearest `limit` by (distance^2, index)
+        std::nth_element(idx.begin(), idx.begin() + limit, idx.end(), [&](int x, int y) {
+            return hd[x] < hd[y] || (hd[x] == hd[y] && hid[x] < hid[y]);
+        });
+        keep = size_t(limit);
+        idx.resize(keep);
+    }
+    std::sort(idx.begin(), idx.end(), [&](int x, int y) { return hid[x] < hid[y]; });
+    ids.resize(keep);
+    d2.resize(keep);
+    for (size_t i = 0; i < keep; ++i) {
+        ids[i] = hid[idx[i]];
+        d2[i] = hd[idx[i]];
+    }
+    return HY_OK;
+}
+
+}  // namespace
+
+extern "C" int hy_cull(const hy_volume *vol, const hy_view *view, const float rect[4],
+                       int32_t limit, int32_t *ids_out, float *dist2_out, int32_t *n_out) {
+    if (!vol || !view || !n_out) return HY_ERR_INVALID;
+    hy_ctx *ctx = vol->ctx;
+    if (!vol->info_dev) return hy_fail(ctx, HY_ERR_STATE, "cull: volume has no page table");
+    CullScratch cs;
+    std::vector<int> ids;
+    std::vector<float> d2;
+    int rc = run_cull(ctx, vol, *view, rect, limit, cs, ids, d2);
+    if (cs.ids) cudaFree(cs.ids);
+    if (cs.d2) cudaFree(cs.d2);
+    if (cs.count) cudaFree(cs.count);
+    if (rc) return rc;
+    for (size_t i = 0; i < ids.size(); ++i) {
+        if (ids_out) ids_out[i] = ids[i];
+        if (dist2_out) dist2_out[i] = d2[i];
+    }
+    *n_out = int32_t(ids.size());
+    return HY_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Pager
+// ---------------------------------------------------------------------------
+struct hy_pager {
+    hy_ctx *ctx = nullptr;
+    hy_store *store = nullptr;
+    hy_volume *vol = nullptr;    // paged volume: pool = cache slots
+    hy_pager_desc desc{};
+    int nslots = 0;              // device slots (2 x batch in lossless mode)
+    cudaStream_t copy = nullptr;
+    cudaEvent_t copied = nullptr;
+    cudaEvent_t marched[2] = {nullptr, nullptr};  // last pass that used each cache half
+    cudaEvent_t staged[2] = {nullptr, nullptr};   // page-table copy out of each staging buffer
+    std::vector<int> page;       // brick -> slot, -1 absent
+    std::vector<int> owner;      // slot -> brick, -1 free
+    int next_free = 0;           // realtime: slots never used yet
+    int2 *info_stage[2] = {nullptr, nullptr};  // pinned staging of the page table
+    CullScratch cs;
+    void *film = nullptr;
+    size_t film_bytes = 0;
+    hy_pager_stats stats{};
+};
+
+namespace {
+
+// film -> RGBA8 with the write_to rule (pixel_template.hpp:11-20)
+__global__ void film_rgba_kernel(const float4 *__restrict__ film, int stride_f4, int n,
+                                 uchar4 *__restrict__ out, uchar4 clear) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 v = film[size_t(i) * stride_f4 + 2];
+    out[i] = v.w != 0.f ? make_uchar4(saturate_u8(v.x), saturate_u8(v.y), saturate_u8(v.z),
+                                      saturate_u8(v.w))
+                        : clear;
+}
+
+// Rewrites the device page table on the render stream from staging buffer
+// `buf` (0 or 1); the buffer is reused only after its previous copy ran.
+int upload_page_table(hy_pager *pg, int buf = 0) {
+    hy_ctx *ctx = pg->ctx;
+    hy_volume *v = pg->vol;
+    HY_CUDA(ctx, cudaEventSynchronize(pg->staged[buf]));
+    int2 *st = pg->info_stage[buf];
+    for (int b = 0; b < v->nbricks; ++b) st[b] = make_int2(v->cheb[b], pg->page[b]);
+    HY_CUDA(ctx, cudaMemcpyAsync(v->info_dev, st, v->nbricks * sizeof(int2),
+                                 cudaMemcpyHostToDevice, ctx->stream));
+    HY_CUDA(ctx, cudaEventRecord(pg->staged[buf], ctx->stream));
+    return HY_OK;
+}
+
+// Upload bricks into slots on the copy stream; returns after queuing.
+int upload_bricks(hy_pager *pg, const int *bricks, const int *slots, int n) {
+    hy_ctx *ctx = pg->ctx;
+    for (int i = 0; i < n; ++i) {
+        const long long off = pg->store->offset[bricks[i]];
+        if (off < 0) return hy_fail(ctx, HY_ERR_INVALID, "pager: empty brick requested");
+        HY_CUDA(ctx, cudaMemcpyAsync(pg->vol->pool + size_t(slots[i]) * pg->vol->slot_stride,
+                                     pg->store->host + off, pg->store->slot_stride,
+                                     cudaMemcpyHostToDevice, pg->copy));
+    }
+    pg->stats.uploads += n;
+    pg->stats.upload_bytes += (int64_t)n * (int64_t)pg->store->slot_stride;
+    return HY_OK;
+}
+
+}  // namespace
+
+extern "C" int hy_pager_create(hy_ctx *ctx, hy_store *store, const hy_pager_desc *desc,
+                               hy_pager **out) {
+    if (!ctx || !store || !desc || !out) return HY_ERR_INVALID;
+    *out = nullptr;
+    if (store->ctx != ctx) return hy_fail(ctx, HY_ERR_INVALID, "pager: store of another context");
+    if (desc->slots <= 0) return hy_fail(ctx, HY_ERR_INVALID, "pager: slots must be > 0");
+    if (desc->mode != HY_PAGER_LOSSLESS && desc->mode != HY_PAGER_REALTIME)
+        return hy_fail(ctx, HY_ERR_INVALID, "pager: unknown mode");
+    HY_CUDA(ctx, cudaSetDevice(ctx->device));
+    hy_pager *pg = new hy_pager();
+    pg->ctx = ctx;
+    pg->store = store;
+    pg->desc = *desc;
+    pg->nslots = desc->mode == HY_PAGER_LOSSLESS ? 2 * desc->slots : desc->slots;
+    hy_volume *v = new hy_volume();
+    pg->vol = v;
+    int rc = hy_volume_init(ctx, &store->desc, v);
+    auto fail = [&](int code) {
+        hy_pager_destroy(pg);
+        return code;
+    };
+    if (rc) return fail(rc);
+    v->paged = true;
+    v->cheb = store->cheb;
+    v->mean = store->mean;
+    v->nonempty = store->nonempty;
+    v->resident = 0;
+    v->reg_of_brick.assign(v->nbricks, -1);
+    v->pool_bytes = size_t(pg->nslots) * v->slot_stride;
+    cudaError_t e = cudaMalloc(&v->pool, v->pool_bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&v->info_dev, v->nbricks * sizeof(int2));
+    if (e == cudaSuccess) e = cudaMalloc(&v->reg_dev, pg->nslots * sizeof(RegEntry));
+    if (e == cudaSuccess) e = cudaMalloc(&v->mean_dev, v->nbricks * sizeof(float));
+    for (int i = 0; i < 2 && e == cudaSuccess; ++i) {
+        e = cudaHostAlloc(reinterpret_cast<void **>(&pg->info_stage[i]), v->nbricks * sizeof(int2),
+                          cudaHostAllocDefault);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&pg->marched[i], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&pg->staged[i], cudaEventDisableTiming);
+    }
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&pg->copy, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&pg->copied, cudaEventDisableTiming);
+    if (e != cudaSuccess) return fail(hy_cuda_fail(ctx, e, "pager: allocation"));
+    std::vector<RegEntry> reg(pg->nslots);
+    for (int s = 0; s < pg->nslots; ++s)
+        reg[s] = RegEntry{v->k, v->b, v->b, v->b, (long long)s * (long long)v->slot_stride, {0, 0}};
+    e = cudaMemcpyAsync(v->reg_dev, reg.data(), reg.size() * sizeof(RegEntry),
+                        cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(v->mean_dev, v->mean.data(), v->nbricks * sizeof(float),
+                            cudaMemcpyHostToDevice, ctx->stream);
+    if (e != cudaSuccess) return fail(hy_cuda_fail(ctx, e, "pager: registry upload"));
+    pg->page.assign(v->nbricks, -1);
+    pg->owner.assign(pg->nslots, -1);
+    rc = upload_page_table(pg);
+    if (rc) return fail(rc);
+    v->uploaded = true;
+    *out = pg;
+    return HY_OK;
+}
+
+extern "C" int hy_pager_destroy(hy_pager *pg) {
+    if (!pg) return HY_OK;
+    hy_ctx *ctx = pg->ctx;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    if (pg->copy) {
+        cudaStreamSynchronize(pg->copy);
+        cudaStreamDestroy(pg->copy);
+    }
+    if (pg->copied) cudaEventDestroy(pg->copied);
+    for (int i = 0; i < 2; ++i) {
+        if (pg->marched[i]) cudaEventDestroy(pg->marched[i]);
+        if (pg->staged[i]) cudaEventDestroy(pg->staged[i]);
+        if (pg->info_stage[i]) cudaFreeHost(pg->info_stage[i]);
+    }
+    if (pg->cs.ids) cudaFree(pg->cs.ids);
+    if (pg->cs.d2) cudaFree(pg->cs.d2);
+    if (pg->cs.count) cudaFree(pg->cs.count);
+    if (pg->film) cudaFree(pg->film);
+    if (pg->vol) {
+        hy_volume *v = pg->vol;
+        if (v->pool) cudaFree(v->pool);
+        if (v->info_dev) cudaFree(v->info_dev);
+        if (v->reg_dev) cudaFree(v->reg_dev);
+        if (v->mean_dev) cudaFree(v->mean_dev);
+        delete v;
+    }
+    delete pg;
+    return HY_OK;
+}
+
+extern "C" int hy_pager_volume(hy_pager *pg, hy_volume **out) {
+    if (!pg || !out) return HY_ERR_INVALID;
+    *out = pg->vol;
+    return HY_OK;
+}
+
+extern "C" int hy_pager_stats_get(const hy_pager *pg, hy_pager_stats *out) {
+    if (!pg || !out) return HY_ERR_INVALID;
+    *out = pg->stats;
+    return HY_OK;
+}
+
+namespace {
+
+// LosslessBlockPagingServer::start + next (lossless_block_paging.cc:116-174):
+// visible bricks by distance to inverse(iet) * eye, in batches of
+// desc.slots; batch k marches while batch k+1 uploads into the other half.
+int render_lossless(hy_pager *pg, const hy_shader_params *p, const hy_camera *cam,
+                    const hy_view &view, int W, int H, uint8_t *rgba_dev) {
+    hy_ctx *ctx = pg->ctx;
+    hy_volume *v = pg->vol;
+    std::vector<int> ids;
+    std::vector<float> d2;
+    int rc = run_cull(ctx, v, view, nullptr, -1, pg->cs, ids, d2);
+    if (rc) return rc;
+    // order: distance of brick centres to cp = inverse(iet) * eye, ties by
+    // index; inverse(iet) is the to_world matrix of hy_iso_lighting
+    hy_shader_params tmp;
+    std::memset(&tmp, 0, sizeof(tmp));
+    rc = hy_iso_lighting(v, cam, &tmp);
+    if (rc) return rc;
+    const float *et = tmp.to_world;
+    float cp[3];
+    for (int r = 0; r < 3; ++r)
+        cp[r] = et[r] * cam->position[0] + et[4 + r] * cam->position[1] +
+                et[8 + r] * cam->position[2] + et[12 + r] * 1.f;
+    std::vector<std::pair<float, int>> order(ids.size());
+    for (size_t i = 0; i < ids.size(); ++i) {
+        const int id = ids[i];
+        const int x = id % v->grid[0], y = (id / v->grid[0]) % v->grid[1],
+                  z = id / (v->grid[0] * v->grid[1]);
+        const float dx = cp[0] - (float(x) + 0.5f), dy = cp[1] - (float(y) + 0.5f),
+                    dz = cp[2] - (float(z) + 0.5f);
+        order[i] = {std::sqrt(dx * dx + dy * dy + dz * dz), id};
+    }
+    std::sort(order.begin(), order.end());
+    const int B = pg->desc.slots;
+    const int nbatch = std::max(1, int((order.size() + B - 1) / B));
+    const size_t need = size_t(W) * H * 64;
+    if (need > pg->film_bytes) {
+        if (pg->film) cudaFree(pg->film);
+        pg->film = nullptr;
+        pg->film_bytes = 0;
+        HY_CUDA(ctx, cudaMalloc(&pg->film, need));
+        pg->film_bytes = need;
+    }
+    ShadeArgs a;
+    rc = hy_fill_args(ctx, v, p, &view, W, H, &a);
+    if (rc) return rc;
+    a.film = pg->film;
+    a.count = 0;
+    std::vector<int> bricks, slots;
+    auto queue_batch = [&](int k) -> int {
+        bricks.clear();
+        slots.clear();
+        const int half = k & 1;
+        for (int j = k * B; j < std::min<int>((k + 1) * B, int(order.size())); ++j) {
+            bricks.push_back(order[j].second);
+            slots.push_back(half * B + (j - k * B));
+        }
+        // this half of the cache is free once the pass of batch k-2 has run
+        HY_CUDA(ctx, cudaStreamWaitEvent(pg->copy, pg->marched[half], 0));
+        int r = upload_bricks(pg, bricks.data(), slots.data(), int(bricks.size()));
+        if (r) return r;
+        HY_CUDA(ctx, cudaEventRecord(pg->copied, pg->copy));
+        return HY_OK;
+    };
+    HY_CUDA(ctx, cudaEventRecord(pg->marched[0], ctx->stream));
+    HY_CUDA(ctx, cudaEventRecord(pg->marched[1], ctx->stream));
+    std::vector<int> prev;
+    rc = queue_batch(0);
+    if (rc) return rc;
+    for (int k = 0; k < nbatch; ++k) {
+        const std::vector<int> cur = bricks, cur_slots = slots;
+        HY_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, pg->copied, 0));
+        // page table: only batch k present (lossless_block_paging.cc:147, 163)
+        for (int b : prev) pg->page[b] = -1;
+        for (size_t i = 0; i < cur.size(); ++i) pg->page[cur[i]] = cur_slots[i];
+        rc = upload_page_table(pg, k & 1);
+        if (rc) return rc;
+        rc = hy_launch_pass(ctx, a, k == 0 ? HY_PASS_RAY_EMIT : HY_PASS_RAY_MARCH);
+        if (rc) return rc;
+        HY_CUDA(ctx, cudaEventRecord(pg->marched[k & 1], ctx->stream));
+        ++pg->stats.passes;
+        prev = cur;
+        if (k + 1 < nbatch) {
+            rc = queue_batch(k + 1);
+            if (rc) return rc;
+        }
+    }
+    for (int b : prev) pg->page[b] = -1;
+    uchar4 clear = make_uchar4(a.clear_u8[0], a.clear_u8[1], a.clear_u8[2], 0);
+    const int stride = p->shader == HY_SHADER_BLOCKS ? 3 : 4;
+    film_rgba_kernel<<<(W * H + 255) / 256, 256, 0, ctx->stream>>>(
+        static_cast<const float4 *>(pg->film), stride, W * H, reinterpret_cast<uchar4 *>(rgba_dev),
+        clear);
+    HY_CUDA(ctx, cudaGetLastError());
+    pg->stats.visible = int64_t(order.size());
+    v->resident = 0;
+    return HY_OK;
+}
+
+// RtBlockPagingServer::update (rt_block_paging.cc:296-326) and the brick
+// arrival handler (rt_block_paging.cc:246-291): the nearest `slots` visible
+// bricks are required; missing ones (nearest first, at most
+// max_uploads_per_frame) go to never-used slots, then to slots of bricks that
+// are no longer required (the highest brick index first); then one frame.
+int render_realtime(hy_pager *pg, const hy_shader_params *p, const hy_view &view, int W, int H,
+                    uint8_t *rgba_dev) {
+    hy_ctx *ctx = pg->ctx;
+    hy_volume *v = pg->vol;
+    std::vector<int> req;
+    std::vector<float> d2;
+    int rc = run_cull(ctx, v, view, nullptr, pg->nslots, pg->cs, req, d2);
+    if (rc) return rc;
+    std::vector<char> required(v->nbricks, 0);
+    for (int b : req) required[b] = 1;
+    std::vector<std::pair<float, int>> missing;
+    for (size_t i = 0; i < req.size(); ++i)
+        if (pg->page[req[i]] < 0) missing.push_back({d2[i], req[i]});
+        else ++pg->stats.hits;
+    std::sort(missing.begin(), missing.end());
+    std::vector<int> redundant;  // ascending brick index
+    for (int s = 0; s < pg->nslots; ++s)
+        if (pg->owner[s] >= 0 && !required[pg->owner[s]]) redundant.push_back(pg->owner[s]);
+    std::sort(redundant.begin(), redundant.end());
+    pg->stats.misses += int64_t(missing.size());
+    const int budget = pg->desc.max_uploads_per_frame > 0 ? pg->desc.max_uploads_per_frame
+                                                           : int(missing.size());
+    std::vector<int> bricks, slots;
+    for (int i = 0; i < int(missing.size()) && int(bricks.size()) < budget; ++i) {
+        const int b = missing[i].second;
+        int slot;
+        if (pg->next_free < pg->nslots) {
+            slot = pg->next_free++;
+        } else if (!redundant.empty()) {
+            const int old = redundant.back();
+            redundant.pop_back();
+            slot = pg->page[old];
+            pg->page[old] = -1;
+            ++pg->stats.evictions;
+        } else {
+            break;  // no slot: the brick stays absent this frame
+        }
+        pg->owner[slot] = b;
+        pg->page[b] = slot;
+        bricks.push_back(b);
+        slots.push_back(slot);
+    }
+    rc = upload_bricks(pg, bricks.data(), slots.data(), int(bricks.size()));
+    if (rc) return rc;
+    HY_CUDA(ctx, cudaEventRecord(pg->copied, pg->copy));
+    HY_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, pg->copied, 0));
+    rc = upload_page_table(pg);
+    if (rc) return rc;
+    int resident = 0;
+    for (int s = 0; s < pg->nslots; ++s) resident += pg->owner[s] >= 0;
+    v->resident = resident;
+    pg->stats.visible = int64_t(req.size());
+    ++pg->stats.passes;
+    return hy_render_device(ctx, v, p, &view, W, H, rgba_dev, nullptr, nullptr);
+}
+
+}  // namespace
+
+extern "C" int hy_pager_render(hy_pager *pg, const hy_shader_params *p, const hy_camera *cam,
+                               int32_t W, int32_t H, uint8_t *rgba_dev) {
+    if (!pg || !p || !cam || !rgba_dev) return HY_ERR_INVALID;
+    hy_ctx *ctx = pg->ctx;
+    if (p->composite) return hy_fail(ctx, HY_ERR_UNSUPPORTED, "pager: composite not supported");
+    HY_CUDA(ctx, cudaSetDevice(ctx->device));
+    hy_view view;
+    int rc = hy_camera_view(pg->vol, cam, &view);
+    if (rc) return rc;
+    ++pg->stats.frames;
+    if (pg->desc.mode == HY_PAGER_LOSSLESS)
+        return render_lossless(pg, p, cam, view, W, H, rgba_dev);
+    return render_realtime(pg, p, view, W, H, rgba_dev);
+}
+
+extern "C" int hy_pager_present(const hy_pager *pg, uint8_t *mask) {
+    if (!pg || !mask) return HY_ERR_INVALID;
+    for (int b = 0; b < pg->vol->nbricks; ++b) mask[b] = pg->page[b] >= 0 ? 1 : 0;
+    return HY_OK;
+}

@@ -239,24 +239,18 @@ int upload_impl(hy_volume *vol, const void *host) {
 
 }  // namespace
 
-extern "C" int hy_volume_create(hy_ctx *ctx, const hy_volume_desc *desc, hy_volume **out) {
-    if (!ctx || !desc || !out) return HY_ERR_INVALID;
-    *out = nullptr;
+int hy_volume_init(hy_ctx *ctx, const hy_volume_desc *desc, hy_volume *v) {
     if (desc->dtype != HY_DTYPE_U8 && desc->dtype != HY_DTYPE_F32)
         return hy_fail(ctx, HY_ERR_INVALID, "volume: dtype must be u8 or f32");
     if (desc->block_size <= 0 || desc->padding < 0 || desc->padding > desc->block_size)
         return hy_fail(ctx, HY_ERR_INVALID, "volume: bad block_size/padding");
     for (int i = 0; i < 3; ++i)
         if (desc->dim[i] <= 0) return hy_fail(ctx, HY_ERR_INVALID, "volume: bad dims");
-    hy_volume *v = new hy_volume();
     v->ctx = ctx;
     v->desc = *desc;
     for (int i = 0; i < 3; ++i) v->grid[i] = (desc->dim[i] + desc->block_size - 1) / desc->block_size;
     long long nb = (long long)v->grid[0] * v->grid[1] * v->grid[2];
-    if (nb > (1 << 24)) {
-        delete v;
-        return hy_fail(ctx, HY_ERR_INVALID, "volume: more than 2^24 bricks");
-    }
+    if (nb > (1 << 24)) return hy_fail(ctx, HY_ERR_INVALID, "volume: more than 2^24 bricks");
     v->nbricks = int(nb);
     v->P = desc->block_size + 2 * desc->padding;
     v->elem = desc->dtype == HY_DTYPE_U8 ? 1 : 4;
@@ -269,6 +263,18 @@ extern "C" int hy_volume_create(hy_ctx *ctx, const hy_volume_desc *desc, hy_volu
     float blksz = float(desc->block_size);
     for (int i = 0; i < 3; ++i) v->bbox_max[i] = float(desc->dim[i]) / blksz;
     v->du = 1.f / blksz;
+    return HY_OK;
+}
+
+extern "C" int hy_volume_create(hy_ctx *ctx, const hy_volume_desc *desc, hy_volume **out) {
+    if (!ctx || !desc || !out) return HY_ERR_INVALID;
+    *out = nullptr;
+    hy_volume *v = new hy_volume();
+    int rc = hy_volume_init(ctx, desc, v);
+    if (rc) {
+        delete v;
+        return rc;
+    }
     *out = v;
     return HY_OK;
 }

@@ -228,6 +228,70 @@ int hy_shade_pass(hy_ctx *ctx, const hy_volume *vol, const hy_shader_params *par
                   int32_t pass, const hy_view *view, void *film_dev, int32_t width,
                   int32_t height, void *dst_dev, const uint8_t clear_rgb[3]);
 
+/* ---- out-of-core volumes: brick store, culling, pager ------------------------
+ * A store keeps every non-empty padded brick of a dataset in pinned host
+ * memory (the decoded form of the varch archive the reference streams from,
+ * lossless_block_paging.cc:149-167).  A pager owns a paged volume whose brick
+ * pool is a fixed cache of `slots` device slots and keeps it filled from the
+ * store, with one of the reference's two policies. */
+typedef struct hy_store hy_store;
+typedef struct hy_pager hy_pager;
+
+enum { HY_PAGER_LOSSLESS = 0, HY_PAGER_REALTIME = 1 };
+
+typedef struct hy_pager_desc {
+    int32_t slots;                 /* bricks per batch (lossless) / cache size (realtime) */
+    int32_t mode;                  /* HY_PAGER_* */
+    int32_t max_uploads_per_frame; /* realtime: 0 = every missing brick */
+} hy_pager_desc;
+
+typedef struct hy_pager_stats {
+    int64_t frames, passes, uploads, upload_bytes, hits, misses, evictions, visible;
+} hy_pager_stats;
+
+/* Store of a resident volume's bricks (copies its pool to pinned host memory). */
+int hy_store_from_volume(const hy_volume *vol, hy_store **out);
+/* Store of a procedural u8 volume: 3 octaves of lattice value noise (cell,
+ * cell/2, cell/4 voxels; amplitudes 1, 1/2, 1/4), thresholded so that
+ * `occupancy` of the voxels are non-zero, those rescaled to 1..255; generated
+ * on the device brick by brick. */
+int hy_store_create_noise(hy_ctx *ctx, const hy_volume_desc *desc, uint64_t seed,
+                          float cell_voxels, float occupancy, hy_store **out);
+int hy_store_destroy(hy_store *store);
+int hy_store_get_info(const hy_store *store, hy_volume_info *out);
+int hy_store_thumbnails(const hy_store *store, int32_t *chebyshev, float *mean);
+/* Copy one padded brick (P^3 voxels; zeros for an empty brick). */
+int hy_store_brick(const hy_store *store, int32_t brick, void *out);
+
+/* OctreeCuller::cull (octree_culler.hpp:121-161) on the device: non-empty
+ * bricks whose box meets the frustum, the nearest `limit` (< 0: all) by
+ * squared distance of the brick centre to the eye (ties by index), returned in
+ * index order.  rect = {min.x, min.y, max.x, max.y} (NULL: [-1,1]^2).
+ * ids / dist2 must hold nbricks entries. */
+int hy_cull(const hy_volume *vol, const hy_view *view, const float rect[4], int32_t limit,
+            int32_t *ids_out, float *dist2_out, int32_t *n_out);
+
+int hy_pager_create(hy_ctx *ctx, hy_store *store, const hy_pager_desc *desc, hy_pager **out);
+int hy_pager_destroy(hy_pager *pager);
+/* The paged volume (for hy_cull / hy_render); owned by the pager. */
+int hy_pager_volume(hy_pager *pager, hy_volume **out);
+int hy_pager_stats_get(const hy_pager *pager, hy_pager_stats *out);
+/* Bricks resident after the last frame, one byte per brick. */
+int hy_pager_present(const hy_pager *pager, uint8_t *mask);
+/* One frame into a device RGBA8 image.
+ *  LOSSLESS: LosslessBlockPagingServer::start/next (lossless_block_paging.cc:
+ *    116-174) + Volume/Isosurface/Blocks passes: visible bricks ordered by the
+ *    distance of their centres to inverse(iet) * eye (as the reference
+ *    computes it), uploaded in batches of `slots`; the first batch's pass
+ *    emits, later ones resume (ray_march); only the current batch is in the
+ *    page table.  Uploads of batch k+1 overlap the march of batch k.
+ *  REALTIME: RtBlockPagingServer::update (rt_block_paging.cc:296-326): the
+ *    nearest `slots` visible bricks are required; missing ones, nearest first,
+ *    go to never-used slots and then to slots of bricks no longer required
+ *    (highest index first); one emit pass renders with what is resident. */
+int hy_pager_render(hy_pager *pager, const hy_shader_params *params, const hy_camera *cam,
+                    int32_t width, int32_t height, uint8_t *rgba_dev);
+
 /* ---- batched multi-view rendering -------------------------------------------
  * Many views rendered by one persistent launch replayed from a CUDA graph.
  * The reference renders one view per Raycaster pass (raycaster.hpp:32-54,

@@ -1065,3 +1065,124 @@ extern "C" int64_t orc_march_film(const orc_volume *v, const float *tf, int32_t 
     for (auto n : counts) total += n;
     return total;
 }
+
+// ---------------------------------------------------------------------------
+// Visible-brick culling: OctreeCuller::cull (octree_culler.hpp:121-161) with
+// get_frustrum (324-345) and Frustum::contains / contains_fast (18-74).
+// Reproduced as written, including that the frustum's border directions stay
+// in camera space while its plane normals and origin are transformed to
+// object space (octree_culler.hpp:329-343).  The selection of the nearest
+// `limit` bricks breaks distance ties by brick index (std::nth_element leaves
+// them unspecified), and the result is ordered by brick index (x fastest).
+// ---------------------------------------------------------------------------
+namespace {
+
+struct Frustum {
+    F3 norm[4];
+    F3 border[4];
+    F3 orig;
+    bool contains(F3 p) const {
+        return dot(norm[0], sub(p, orig)) > 0.f && dot(norm[1], sub(p, orig)) > 0.f &&
+               dot(norm[2], sub(p, orig)) > 0.f && dot(norm[3], sub(p, orig)) > 0.f;
+    }
+    bool contains_fast(F3 mn, F3 mx) const {
+        const F3 vp[2] = {mn, mx};
+        for (int i = 0; i != 2; ++i)
+            for (int j = 0; j != 2; ++j)
+                for (int k = 0; k != 2; ++k)
+                    if (contains(f3(vp[i].x, vp[j].y, vp[k].z))) return true;
+        for (int i = 0; i != 4; ++i) {
+            Ray r;
+            r.o = orig;
+            r.d = normalize(border[i]);
+            float tnear, tfar;
+            if (intersect(r, mn, mx, tnear, tfar) && tfar > 0.f) return true;
+        }
+        return false;
+    }
+};
+
+Frustum make_frustum(const float view[20], const float rect[4]) {
+    // rect = {min.x, min.y, max.x, max.y}
+    Frustum f;
+    const float ctg = view[16];
+    f.border[0] = f3(rect[2], rect[3], -ctg);
+    f.border[1] = f3(rect[2], rect[1], -ctg);
+    f.border[2] = f3(rect[0], rect[1], -ctg);
+    f.border[3] = f3(rect[0], rect[3], -ctg);
+    f.orig = f3(0, 0, 0);
+    f.norm[0] = cross(f.border[0], f.border[1]);
+    f.norm[1] = cross(f.border[1], f.border[2]);
+    f.norm[2] = cross(f.border[2], f.border[3]);
+    f.norm[3] = cross(f.border[3], f.border[0]);
+    M4 t;
+    std::memcpy(t.m, view, sizeof(t.m));
+    F4 o = mulv(t, F4{f.orig.x, f.orig.y, f.orig.z, 1.f});
+    f.orig = f3(o.x, o.y, o.z);
+    for (auto &n : f.norm) {
+        F4 m = mulv(t, F4{n.x, n.y, n.z, 0.f});
+        n = f3(m.x, m.y, m.z);
+    }
+    return f;
+}
+
+}  // namespace
+
+extern "C" int32_t orc_cull(const orc_volume *v, const float view[20], const float rect_in[4],
+                            int32_t limit, int32_t *ids_out, float *dist2_out) {
+    const float def_rect[4] = {-1.f, -1.f, 1.f, 1.f};
+    const float *rect = rect_in ? rect_in : def_rect;
+    Frustum f = make_frustum(view, rect);
+    struct Item {
+        float d2;
+        int id;
+    };
+    std::vector<Item> buf;
+    for (int z = 0; z < v->grid[2]; ++z)
+        for (int y = 0; y < v->grid[1]; ++y)
+            for (int x = 0; x < v->grid[0]; ++x) {
+                int id = (z * v->grid[1] + y) * v->grid[0] + x;
+                if (v->cheb[id] != 0) continue;
+                F3 mn = f3(float(x), float(y), float(z));
+                F3 mx = f3(float(x + 1), float(y + 1), float(z + 1));
+                if (f.contains_fast(mn, mx)) {
+                    F3 c = f3(float(x) + .5f, float(y) + .5f, float(z) + .5f);
+                    F3 d = sub(c, f.orig);
+                    buf.push_back(Item{dot(d, d), id});
+                }
+            }
+    size_t n = buf.size();
+    if (limit >= 0 && size_t(limit) < n) {
+        std::nth_element(buf.begin(), buf.begin() + limit, buf.end(), [](const Item &a, const Item &b) {
+            return a.d2 < b.d2 || (a.d2 == b.d2 && a.id < b.id);
+        });
+        n = size_t(limit);
+        buf.resize(n);
+    }
+    std::sort(buf.begin(), buf.end(), [](const Item &a, const Item &b) { return a.id < b.id; });
+    for (size_t i = 0; i < n; ++i) {
+        if (ids_out) ids_out[i] = buf[i].id;
+        if (dist2_out) dist2_out[i] = buf[i].d2;
+    }
+    return int32_t(n);
+}
+
+// LosslessBlockPagingServer::start (lossless_block_paging.cc:116-135): the
+// visible bricks ordered by the distance of their centres to
+// cp = inverse(iet) * camera position -- the inverse exhibit transform, as
+// the reference writes it -- with ties broken by brick index.
+extern "C" void orc_lossless_order(const orc_volume *v, const float cam[10], const int32_t *ids,
+                                   int32_t n, int32_t *order_out) {
+    M4 et = inverse(exhibit_iet(v));
+    F4 c4 = mulv(et, F4{cam[0], cam[1], cam[2], 1.f});
+    F3 cp = f3(c4.x, c4.y, c4.z);
+    std::vector<std::pair<float, int>> d(n);
+    for (int i = 0; i < n; ++i) {
+        int id = ids[i];
+        int x = id % v->grid[0], y = (id / v->grid[0]) % v->grid[1], z = id / (v->grid[0] * v->grid[1]);
+        F3 c = f3(float(x) + 0.5f, float(y) + 0.5f, float(z) + 0.5f);
+        d[i] = {length(sub(c, cp)), id};
+    }
+    std::sort(d.begin(), d.end());
+    for (int i = 0; i < n; ++i) order_out[i] = d[i].second;
+}

@@ -84,6 +84,16 @@ int64_t orc_render_rows(const orc_volume *v, const float *tf_rgba, int32_t ntf,
                         int32_t height, int32_t y0, int32_t y1, int32_t nthreads,
                         float *v_out, uint8_t *rgba_out, float *aux_out, void *film_out);
 
+/* Visible non-empty bricks (OctreeCuller::cull): the nearest `limit` (< 0:
+ * all) by squared distance of the brick centre to the frustum origin, ties by
+ * index, returned in index order.  rect = {min.x, min.y, max.x, max.y} or NULL
+ * for [-1,1]^2.  Returns the count. */
+int32_t orc_cull(const orc_volume *v, const float view[20], const float rect[4], int32_t limit,
+                 int32_t *ids_out, float *dist2_out);
+/* LosslessBlockPagingServer::start ordering of brick ids. */
+void orc_lossless_order(const orc_volume *v, const float cam[10], const int32_t *ids, int32_t n,
+                        int32_t *order_out);
+
 /* Resume a film (RAY_MARCH pass) with the current page table. */
 int64_t orc_march_film(const orc_volume *v, const float *tf_rgba, int32_t ntf,
                        const orc_params *p, int32_t width, int32_t height, int32_t nthreads,

@@ -68,6 +68,8 @@ def lib() -> C.CDLL:
                                             C.c_int32, C.c_int32, C.c_int32, C.c_int32, P, P, P, P]),
             "orc_march_film": (C.c_int64, [P, P, C.c_int32, C.POINTER(OrcParams), C.c_int32,
                                            C.c_int32, C.c_int32, P]),
+            "orc_cull": (C.c_int32, [P, P, P, C.c_int32, P, P]),
+            "orc_lossless_order": (None, [P, P, P, C.c_int32, P]),
         }
         for name, (res, args) in protos.items():
             fn = getattr(l, name)
@@ -181,3 +183,28 @@ def march_film(vol: OracleVolume, tf, params: OrcParams, film: np.ndarray, width
     tfa = np.ascontiguousarray(np.asarray(tf, np.float32).reshape(-1, 4))
     return int(lib().orc_march_film(vol.h, _p(tfa), tfa.shape[0], C.byref(params), width, height,
                                     nthreads, _p(film)))
+
+
+def cull(vol: OracleVolume, view: np.ndarray, limit: int = -1, rect=None):
+    """OctreeCuller::cull restated: (ids in index order, squared distances)."""
+    n = vol.grid[0] * vol.grid[1] * vol.grid[2]
+    ids = np.zeros(n, np.int32)
+    d2 = np.zeros(n, np.float32)
+    v = np.ascontiguousarray(view, np.float32)
+    r = None if rect is None else np.ascontiguousarray(rect, np.float32)
+    k = lib().orc_cull(vol.h, _p(v), _p(r), limit, _p(ids), _p(d2))
+    return ids[:k].copy(), d2[:k].copy()
+
+
+def lossless_order(vol: OracleVolume, cam: np.ndarray, ids: np.ndarray) -> np.ndarray:
+    ids = np.ascontiguousarray(ids, np.int32)
+    out = np.zeros_like(ids)
+    c = np.ascontiguousarray(cam, np.float32)
+    lib().orc_lossless_order(vol.h, _p(c), _p(ids), len(ids), _p(out))
+    return out
+
+
+def present_mask(vol: OracleVolume, ids) -> np.ndarray:
+    m = np.zeros(vol.grid[0] * vol.grid[1] * vol.grid[2], np.uint8)
+    m[np.asarray(ids, np.int64)] = 1
+    return m

@@ -1,0 +1,188 @@
+"""Out-of-core path: brick store, visible-brick culling, lossless and realtime pagers.
+
+Culling must give exactly the oracle's visible set and distances; the
+lossless pager must reproduce the oracle replaying the same batches with
+emit + march passes (holes included); the realtime pager must follow the
+reference's replacement policy, simulated here on the host with the oracle's
+culling, and render what the oracle renders with that resident set.
+"""
+
+import numpy as np
+import pytest
+
+import hydrant_gb300 as hy
+from hydrant_gb300 import _abi
+from hydrant_gb300 import workloads as wl
+from oracle import oracle as orc
+from tests._harness import view_array
+
+pytestmark = pytest.mark.gpu
+
+
+def cam10(c):
+    return np.array(list(c.position) + list(c.target) + list(c.up) + [c.ctg_fovy_2], np.float32)
+
+
+def write_to(v, clear=(0, 0, 0)):
+    out = np.zeros(v.shape[:-1] + (4,), np.uint8)
+    sat = lambda x: np.clip(x.astype(np.float32) * np.float32(255), 0, 255).astype(np.uint8)
+    hit = v[..., 3] != 0
+    for c in range(4):
+        out[..., c] = np.where(hit, sat(v[..., c]), clear[c] if c < 3 else 0)
+    return out
+
+
+@pytest.fixture(scope="module")
+def tubes(ctx):
+    vox = hy.synth_tubes_u8(1, (128, 128, 128), 14)
+    vol = hy.Volume(ctx, vox, 16, 1)
+    ov = orc.OracleVolume(vox, 16, 1)
+    ctx.set_transfer_fn(wl.TF9)
+    store = hy.Store.from_volume(vol)
+    yield vol, ov, store
+    store.close()
+    vol.close()
+
+
+CAMS = [("orbit", (25, 65, 2.2)), ("orbit", (-110, 20, 1.8)), ("orbit", (60, -40, 3.0)),
+        ("ptu", (0.2, 0.1, 0.3))]
+
+
+@pytest.mark.parametrize("cam", CAMS)
+@pytest.mark.parametrize("limit", [-1, 7, 60])
+def test_cull_matches_oracle(tubes, cam, limit):
+    vol, ov, _ = tubes
+    c = wl.make_camera(wl.Camera(cam[0], cam[1]))
+    view = hy.camera_view(vol, c)
+    ids, d2 = hy.cull(vol, view, limit)
+    oids, od2 = orc.cull(ov, view_array(view), limit)
+    assert np.array_equal(ids, oids)
+    assert np.array_equal(d2, od2)
+    if limit < 0:
+        assert len(ids) > 0
+
+
+def test_store_holds_the_bricks(tubes):
+    vol, ov, store = tubes
+    cheb, mean = store.thumbnails()
+    ocheb, omean = ov.thumbnails()
+    assert np.array_equal(cheb, ocheb.ravel()) and np.array_equal(mean, omean.ravel())
+    for b in [0, 7, 100, 511]:
+        got = store.brick(b).astype(np.float32) / np.float32(255)
+        if cheb[b] == 0:
+            np.testing.assert_array_equal(got, ov.brick(b))
+        else:
+            assert not got.any()
+
+
+def _oracle_lossless(ov, tf, op, c10, v20, W, H, B):
+    ids, _ = orc.cull(ov, v20)
+    order = orc.lossless_order(ov, c10, ids)
+    batches = [order[i:i + B] for i in range(0, len(order), B)] or [order[:0]]
+    film = None
+    for k, batch in enumerate(batches):
+        ov.set_present(orc.present_mask(ov, batch))
+        if k == 0:
+            film = orc.render(ov, tf, op, v20, W, H, want_film=True)["film"]
+        else:
+            orc.march_film(ov, tf, op, film, W, H)
+    ov.set_present(np.ones(ov.grid[0] * ov.grid[1] * ov.grid[2], np.uint8))
+    fb = film.shape[-1] // 4
+    v = film.view(np.float32).reshape(H, W, fb)[..., 8:12]
+    return write_to(v), len(batches)
+
+
+@pytest.mark.parametrize("shader", ["Volume", "Isosurface", "Blocks"])
+@pytest.mark.parametrize("slots", [25, 1000])
+def test_lossless_pager_matches_oracle(ctx, tubes, shader, slots):
+    torch = pytest.importorskip("torch")
+    vol, ov, store = tubes
+    pg = hy.Pager(ctx, store, slots, _abi.PAGER_LOSSLESS)
+    try:
+        W, H = 72, 56
+        for cam in CAMS[:3]:
+            c = wl.make_camera(wl.Camera(cam[0], cam[1]))
+            p = hy.shader_params(shader=shader, density=0.4, sample_rate=0.5, isovalue=0.5)
+            if shader == "Isosurface":
+                hy.iso_lighting(vol, c, p)
+            out = torch.zeros(W * H * 4, dtype=torch.uint8, device="cuda")
+            pg.render(p, c, W, H, out.data_ptr())
+            ctx.synchronize()
+            got = out.cpu().numpy().reshape(H, W, 4)
+            view = view_array(hy.camera_view(vol, c))
+            ref, nb = _oracle_lossless(ov, wl.TF9, orc.params_from(p), cam10(c), view, W, H, slots)
+            d = np.abs(got.astype(int) - ref.astype(int))
+            assert d.max() <= 1, f"{shader} {cam}: {d.max()} LSB"
+        st = pg.stats()
+        if slots == 25:
+            assert st["passes"] > st["frames"]  # several batches per frame
+        assert st["uploads"] > 0
+    finally:
+        pg.close()
+
+
+@pytest.mark.parametrize("budget", [0, 9])
+def test_realtime_pager_follows_reference_policy(ctx, tubes, budget):
+    torch = pytest.importorskip("torch")
+    vol, ov, store = tubes
+    slots = 40
+    pg = hy.Pager(ctx, store, slots, _abi.PAGER_REALTIME, budget)
+    page, owner, next_free = {}, {}, 0
+    try:
+        W, H = 64, 48
+        for f in range(6):
+            c = wl.make_camera(wl.Camera("orbit", (25 + 25 * f, 40, 2.2)))
+            p = hy.shader_params(shader="Volume", density=0.4, sample_rate=0.5)
+            out = torch.zeros(W * H * 4, dtype=torch.uint8, device="cuda")
+            pg.render(p, c, W, H, out.data_ptr())
+            ctx.synchronize()
+            # host simulation of the replacement policy with the oracle's cull
+            view = view_array(hy.camera_view(vol, c))
+            ids, d2 = orc.cull(ov, view, slots)
+            req = set(ids.tolist())
+            missing = sorted((float(d), int(b)) for b, d in zip(ids, d2) if int(b) not in page)
+            redundant = sorted(b for b in page if b not in req)
+            n = 0
+            for _, b in missing:
+                if budget and n >= budget:
+                    break
+                if next_free < slots:
+                    slot = next_free
+                    next_free += 1
+                elif redundant:
+                    old = redundant.pop()
+                    slot = page.pop(old)
+                else:
+                    break
+                page[b] = slot
+                owner[slot] = b
+                n += 1
+            mask = orc.present_mask(ov, list(page))
+            assert np.array_equal(pg.present(), mask), f"frame {f}: resident sets differ"
+            ov.set_present(mask)
+            ref = orc.render(ov, wl.TF9, orc.params_from(p), view, W, H)["rgba"]
+            got = out.cpu().numpy().reshape(H, W, 4)
+            assert np.abs(got.astype(int) - ref.astype(int)).max() <= 1, f"frame {f}"
+        st = pg.stats()
+        assert st["evictions"] > 0 and st["hits"] > 0
+    finally:
+        ov.set_present(np.ones(ov.grid[0] * ov.grid[1] * ov.grid[2], np.uint8))
+        pg.close()
+
+
+def test_noise_store(ctx):
+    store = hy.Store.noise(ctx, (128, 128, 64), 32, 1, seed=2, cell_voxels=32.0, occupancy=0.15)
+    try:
+        info = store.info
+        assert tuple(info.grid) == (4, 4, 2)
+        cheb, mean = store.thumbnails()
+        occ = []
+        for b in range(info.nbricks):
+            br = store.brick(b)
+            core = br[1:33, 1:33, 1:33]
+            assert (cheb[b] == 0) == bool(br.any())
+            assert mean[b] == np.float32(core.astype(np.float64).sum() / 255.0 / 32 ** 3)
+            occ.append((core > 0).mean())
+        assert 0.08 < float(np.mean(occ)) < 0.25
+    finally:
+        store.close()
