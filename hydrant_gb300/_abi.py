@@ -111,6 +111,17 @@ class HyPagerStats(C.Structure):
                                          "misses", "evictions", "visible")]
 
 
+class HyDiffParams(C.Structure):
+    _fields_ = [
+        ("n", C.c_int32),
+        ("sample_rate", C.c_float),
+        ("max_steps", C.c_int32),
+        ("density", C.c_float),
+        ("ntf", C.c_int32),
+        ("ckpt_k", C.c_int32),
+    ]
+
+
 class HyRenderStats(C.Structure):
     _fields_ = [("samples", C.c_int64), ("pixels", C.c_int64), ("ms", C.c_float)]
 
@@ -176,6 +187,16 @@ _PROTOS = {
     "hy_pager_present": (C.c_int, [P, P]),
     "hy_pager_render": (
         C.c_int, [P, C.POINTER(HyShaderParams), C.POINTER(HyCamera), C.c_int32, C.c_int32, P]),
+    "hy_diff_ckpt_bytes": (
+        C.c_int, [C.POINTER(HyDiffParams), C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_int64)]),
+    "hy_diff_forward": (
+        C.c_int,
+        [P, C.POINTER(HyDiffParams), P, P, C.POINTER(HyView), C.c_int32, C.c_int32, C.c_int32, P,
+         P, P]),
+    "hy_diff_backward": (
+        C.c_int,
+        [P, C.POINTER(HyDiffParams), P, P, C.POINTER(HyView), C.c_int32, C.c_int32, C.c_int32, P,
+         P, P, P, P]),
     "hy_synth_blobs_u8": (C.c_int, [C.c_uint64, P, C.c_int32, P, C.c_int32]),
     "hy_synth_blobs_f32": (C.c_int, [C.c_uint64, P, C.c_int32, P, C.c_int32]),
     "hy_synth_tubes_u8": (C.c_int, [C.c_uint64, P, C.c_int32, P, C.c_int32]),

@@ -20,7 +20,7 @@ CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libhydrant_gb300.so"
 
-SOURCES = ["hy_api.cc", "hy_volume.cu", "hy_render.cu", "hy_batch.cu", "hy_page.cu", "hy_synth.cc"]
+SOURCES = ["hy_api.cc", "hy_volume.cu", "hy_render.cu", "hy_batch.cu", "hy_page.cu", "hy_diff.cu", "hy_synth.cc"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_COMMON = [

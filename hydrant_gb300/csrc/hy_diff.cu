@@ -1,0 +1,412 @@
+// hy_diff.cu -- differentiable Volume rendering: forward with per-ray
+// checkpoints and the adjoint ray march.
+//
+// The forward is the Volume shader's march (volume_shader.cu:32-81) over one
+// dense f32 brick with a 1-voxel replicate apron, in the reference's float
+// operations, with the discontinuous parts fixed: step_size stays 1 (no
+// adaptive stepping) and there is no empty-space skipping.  Sampling the
+// padded brick at index i is sampling the raw volume at clamp(i-1, 0, n-1),
+// so the kernels read the caller's raw n^3 volume directly and the gradient
+// of an apron voxel lands on the voxel it replicates.
+//
+// Every K steps the forward stores the ray state (position, v.w) in a
+// checkpoint buffer.  The adjoint walks a ray's segments back to front: it
+// restores a checkpoint, recomputes the K samples of that segment (positions,
+// values, transmittance) into a local array, and back-propagates through
+// front-to-back compositing, the transfer-function lookup and the trilinear
+// weights.  With c_n = (r a, g a, b a, a), T_n = 1 - v.w before sample n and
+// R_n = c_n + (1 - a_n) R_{n+1} the colour composited behind sample n:
+//   dL/dc_n = T_n g,   dL/da_n += -T_n (g . R_{n+1}),
+// with g = dL/dv of the pixel.  Knot gradients are summed per block in shared
+// memory before one global atomic per knot channel; voxel gradients are eight
+// atomics per sample.
+
+#include <algorithm>
+#include <cstring>
+
+#include "hy_shade.cuh"
+
+using namespace hy;
+using namespace hy::dev;
+
+namespace {
+
+constexpr int kMaxDiffViews = 64;
+constexpr int kMaxK = 64;
+constexpr int kMaxKnots = 256;
+
+struct DiffView {
+    float trans[16];
+    float ctg;
+    float ray_o[3];
+};
+
+struct DiffArgs {
+    const float *vol;  // raw n^3, x fastest
+    int n;             // edge (brick = whole volume)
+    float k, b;        // BlockSamplerMapping of the padded brick
+    float step;
+    int max_steps;
+    float density;
+    const float4 *tf;
+    int ntf;
+    int K;             // checkpoint interval
+    int max_ckpt;      // checkpoints per ray
+    int W, H, nviews;
+    DiffView views[kMaxDiffViews];
+    float4 *image;     // nviews * H * W
+    float4 *ckpt;      // nviews * H * W * max_ckpt (position.xyz, v.w)
+    int *nsteps_out;   // steps taken per ray (for the adjoint)
+    const float4 *dimage;
+    float *dvol;
+    float *dtf;        // ntf * 4
+};
+
+// Trilinear sample of the padded brick at brick-local x in [0,1] (the
+// interior case of sample_brick: apron >= 1, no wrap, no clamps), returning
+// the eight raw-volume indices and weights for the adjoint.
+struct Tap {
+    int idx[8];
+    float w[8];
+};
+
+__device__ __forceinline__ float diff_sample(const DiffArgs &a, float lx, float ly, float lz,
+                                             Tap *tap) {
+    const int P = a.n + 2;
+    const float fd = float(P);
+    const float fx = fd * (a.k * lx + a.b), fy = fd * (a.k * ly + a.b), fz = fd * (a.k * lz + a.b);
+    const float ux = fx - .5f, uy = fy - .5f, uz = fz - .5f;
+    const float flx = floorf(ux), fly = floorf(uy), flz = floorf(uz);
+    const float ax = ux - flx, ay = uy - fly, az = uz - flz;
+    const int ix = int(flx), iy = int(fly), iz = int(flz);
+    // padded index i -> raw clamp(i - 1, 0, n - 1)
+    const int x0 = iclamp(ix - 1, 0, a.n - 1), x1 = iclamp(ix, 0, a.n - 1);
+    const int y0 = iclamp(iy - 1, 0, a.n - 1), y1 = iclamp(iy, 0, a.n - 1);
+    const int z0 = iclamp(iz - 1, 0, a.n - 1), z1 = iclamp(iz, 0, a.n - 1);
+    const long long n = a.n;
+    const long long r00 = (z0 * n + y0) * n, r10 = (z0 * n + y1) * n, r01 = (z1 * n + y0) * n,
+                    r11 = (z1 * n + y1) * n;
+    const float v000 = __ldg(a.vol + r00 + x0), v100 = __ldg(a.vol + r00 + x1);
+    const float v010 = __ldg(a.vol + r10 + x0), v110 = __ldg(a.vol + r10 + x1);
+    const float v001 = __ldg(a.vol + r01 + x0), v101 = __ldg(a.vol + r01 + x1);
+    const float v011 = __ldg(a.vol + r11 + x0), v111 = __ldg(a.vol + r11 + x1);
+    const float bx = 1.f - ax, by = 1.f - ay, bz = 1.f - az;
+    const float x0_0 = v000 * bx + v100 * ax;
+    const float x1_0 = v010 * bx + v110 * ax;
+    const float x0_1 = v001 * bx + v101 * ax;
+    const float x1_1 = v011 * bx + v111 * ax;
+    const float yy0 = x0_0 * by + x1_0 * ay;
+    const float yy1 = x0_1 * by + x1_1 * ay;
+    if (tap) {
+        tap->idx[0] = int(r00 + x0);
+        tap->idx[1] = int(r00 + x1);
+        tap->idx[2] = int(r10 + x0);
+        tap->idx[3] = int(r10 + x1);
+        tap->idx[4] = int(r01 + x0);
+        tap->idx[5] = int(r01 + x1);
+        tap->idx[6] = int(r11 + x0);
+        tap->idx[7] = int(r11 + x1);
+        tap->w[0] = bx * by * bz;
+        tap->w[1] = ax * by * bz;
+        tap->w[2] = bx * ay * bz;
+        tap->w[3] = ax * ay * bz;
+        tap->w[4] = bx * by * az;
+        tap->w[5] = ax * by * az;
+        tap->w[6] = bx * ay * az;
+        tap->w[7] = ax * ay * az;
+    }
+    return yy0 * bz + yy1 * az;
+}
+
+// emit against the unit box; returns nsteps, sets o and d
+__device__ __forceinline__ int diff_emit(const DiffArgs &a, int view, int x, int y, float &ox,
+                                         float &oy, float &oz, float &dx, float &dy, float &dz) {
+    const DiffView &vw = a.views[view];
+    ViewArgs va;
+    // gen_ray reads trans / ctg / ray_o / W / H only
+    for (int i = 0; i < 16; ++i) va.trans[i] = vw.trans[i];
+    va.ctg = vw.ctg;
+    va.ray_o[0] = vw.ray_o[0];
+    va.ray_o[1] = vw.ray_o[1];
+    va.ray_o[2] = vw.ray_o[2];
+    va.W = a.W;
+    va.H = a.H;
+    gen_ray(va, x, y, ox, oy, oz, dx, dy, dz);
+    float tnear, tfar;
+    if (!intersect(ox, oy, oz, 1.f / dx, 1.f / dy, 1.f / dz, 0.f, 0.f, 0.f, 1.f, 1.f, 1.f, tnear,
+                   tfar))
+        return 0;
+    if (tnear < 0) tnear = 0;
+    if (tfar < 0) tfar = 0;
+    ox = ox + dx * tnear;
+    oy = oy + dy * tnear;
+    oz = oz + dz * tnear;
+    return min(a.max_steps, int((tfar - tnear) / a.step));
+}
+
+// transfer function value and its derivative in s
+__device__ __forceinline__ float4 tf_eval(const float4 *tf, int n, float s, int &i, int &j,
+                                          float &al, bool &inb) {
+    const float fn = float(n);
+    const float fx = fn * s;
+    inb = (0.f <= fx && fx <= fn);
+    if (!inb) {
+        i = j = 0;
+        al = 0.f;
+        return make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    const float u = fx - .5f;
+    const float flr = floorf(u);
+    al = u - flr;
+    const int fi = int(flr);
+    i = max(fi, 0);
+    j = min(fi + 1, n - 1);
+    const float4 p = tf[i], q = tf[j];
+    const float bb = 1.f - al;
+    return make_float4(p.x * bb + q.x * al, p.y * bb + q.y * al, p.z * bb + q.z * al,
+                       p.w * bb + q.w * al);
+}
+
+__device__ __forceinline__ void pixel_of(const DiffArgs &a, int &x, int &y, int &view) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    x = blockIdx.x * 16 + (warp & 1) * 8 + (lane & 7);
+    y = blockIdx.y * 8 + (warp >> 1) * 4 + (lane >> 3);
+    view = blockIdx.z;
+}
+
+__global__ void __launch_bounds__(128) diff_forward_kernel(const __grid_constant__ DiffArgs a) {
+    __shared__ float4 tf[kMaxKnots];
+    for (int i = threadIdx.x; i < a.ntf; i += blockDim.x) tf[i] = a.tf[i];
+    __syncthreads();
+    int x, y, view;
+    pixel_of(a, x, y, view);
+    if (x >= a.W || y >= a.H) return;
+    const size_t ray = (size_t(view) * a.H + y) * a.W + x;
+    float ox, oy, oz, dx, dy, dz;
+    const int nsteps = diff_emit(a, view, x, y, ox, oy, oz, dx, dy, dz);
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float sx = dx * a.step, sy = dy * a.step, sz = dz * a.step;  // step_size 1
+    for (int s = 0; s < nsteps; ++s) {
+        if (a.ckpt && s % a.K == 0) a.ckpt[ray * a.max_ckpt + s / a.K] = make_float4(ox, oy, oz, v.w);
+        const float ipx = floorf(ox), ipy = floorf(oy), ipz = floorf(oz);
+        const float val = diff_sample(a, ox - ipx, oy - ipy, oz - ipz, nullptr);
+        int i, j;
+        float al;
+        bool inb;
+        float4 ub = tf_eval(tf, a.ntf, val, i, j, al, inb);
+        ub.w = ub.w * a.density;
+        const float w = ub.w;
+        ub.x = ub.x * w;
+        ub.y = ub.y * w;
+        ub.z = ub.z * w;
+        const float t = 1.f - v.w;
+        v.x = v.x + ub.x * t;
+        v.y = v.y + ub.y * t;
+        v.z = v.z + ub.z * t;
+        v.w = v.w + ub.w * t;
+        ox = ox + sx;
+        oy = oy + sy;
+        oz = oz + sz;
+    }
+    a.image[ray] = v;
+    if (a.nsteps_out) a.nsteps_out[ray] = nsteps;
+}
+
+__global__ void __launch_bounds__(128) diff_backward_kernel(const __grid_constant__ DiffArgs a) {
+    __shared__ float4 tf[kMaxKnots];
+    __shared__ float4 gtf[kMaxKnots];
+    for (int i = threadIdx.x; i < a.ntf; i += blockDim.x) {
+        tf[i] = a.tf[i];
+        gtf[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    __syncthreads();
+    int x, y, view;
+    pixel_of(a, x, y, view);
+    if (x < a.W && y < a.H) {
+        const size_t ray = (size_t(view) * a.H + y) * a.W + x;
+        const int nsteps = a.nsteps_out[ray];
+        const float4 g = a.dimage[ray];
+        float ox0, oy0, oz0, dx, dy, dz;
+        diff_emit(a, view, x, y, ox0, oy0, oz0, dx, dy, dz);
+        const float sx = dx * a.step, sy = dy * a.step, sz = dz * a.step;
+        float4 R = make_float4(0.f, 0.f, 0.f, 0.f);
+        float px[kMaxK], py[kMaxK], pz[kMaxK], pw[kMaxK];
+        const int nseg = (nsteps + a.K - 1) / a.K;
+        for (int seg = nseg - 1; seg >= 0; --seg) {
+            const float4 c = a.ckpt[ray * a.max_ckpt + seg];
+            float ox = c.x, oy = c.y, oz = c.z, vw = c.w;
+            const int s0 = seg * a.K, cnt = min(a.K, nsteps - s0);
+            // recompute the segment's positions and v.w before each sample
+            for (int s = 0; s < cnt; ++s) {
+                px[s] = ox;
+                py[s] = oy;
+                pz[s] = oz;
+                pw[s] = vw;
+                const float ipx = floorf(ox), ipy = floorf(oy), ipz = floorf(oz);
+                const float val = diff_sample(a, ox - ipx, oy - ipy, oz - ipz, nullptr);
+                int i, j;
+                float al;
+                bool inb;
+                float4 ub = tf_eval(tf, a.ntf, val, i, j, al, inb);
+                const float aa = ub.w * a.density;
+                vw = vw + aa * (1.f - vw);
+                ox = ox + sx;
+                oy = oy + sy;
+                oz = oz + sz;
+            }
+            for (int s = cnt - 1; s >= 0; --s) {
+                const float ipx = floorf(px[s]), ipy = floorf(py[s]), ipz = floorf(pz[s]);
+                Tap tap;
+                const float val = diff_sample(a, px[s] - ipx, py[s] - ipy, pz[s] - ipz, &tap);
+                int i, j;
+                float al;
+                bool inb;
+                const float4 q = tf_eval(tf, a.ntf, val, i, j, al, inb);
+                const float aa = q.w * a.density;
+                const float T = 1.f - pw[s];
+                // dL/dc = T g ; transmittance term through later samples
+                const float gcx = T * g.x, gcy = T * g.y, gcz = T * g.z, gcw = T * g.w;
+                const float gdot = g.x * R.x + g.y * R.y + g.z * R.z + g.w * R.w;
+                const float da = gcx * q.x + gcy * q.y + gcz * q.z + gcw - T * gdot;
+                // R_n = c_n + (1 - a_n) R_{n+1}
+                const float om = 1.f - aa;
+                R = make_float4(q.x * aa + om * R.x, q.y * aa + om * R.y, q.z * aa + om * R.z,
+                                aa + om * R.w);
+                if (!inb) continue;
+                // gradient of the TF output (r, g, b, A)
+                const float4 gq = make_float4(gcx * aa, gcy * aa, gcz * aa, da * a.density);
+                const float bb = 1.f - al;
+                atomicAdd(&gtf[i].x, gq.x * bb);
+                atomicAdd(&gtf[i].y, gq.y * bb);
+                atomicAdd(&gtf[i].z, gq.z * bb);
+                atomicAdd(&gtf[i].w, gq.w * bb);
+                atomicAdd(&gtf[j].x, gq.x * al);
+                atomicAdd(&gtf[j].y, gq.y * al);
+                atomicAdd(&gtf[j].z, gq.z * al);
+                atomicAdd(&gtf[j].w, gq.w * al);
+                // d TF / d s = (knot_j - knot_i) * n
+                const float4 kj = tf[j], ki = tf[i];
+                const float fn = float(a.ntf);
+                const float ds = (gq.x * (kj.x - ki.x) + gq.y * (kj.y - ki.y) +
+                                  gq.z * (kj.z - ki.z) + gq.w * (kj.w - ki.w)) * fn;
+                if (ds != 0.f)
+#pragma unroll
+                    for (int t = 0; t < 8; ++t)
+                        if (tap.w[t] != 0.f) atomicAdd(a.dvol + tap.idx[t], ds * tap.w[t]);
+            }
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < a.ntf; i += blockDim.x) {
+        const float4 v = gtf[i];
+        if (v.x != 0.f) atomicAdd(a.dtf + 4 * i + 0, v.x);
+        if (v.y != 0.f) atomicAdd(a.dtf + 4 * i + 1, v.y);
+        if (v.z != 0.f) atomicAdd(a.dtf + 4 * i + 2, v.z);
+        if (v.w != 0.f) atomicAdd(a.dtf + 4 * i + 3, v.w);
+    }
+}
+
+int fill_diff(hy_ctx *ctx, const hy_diff_params *p, const float *vol, const float *tf,
+              const hy_view *views, int nviews, int W, int H, DiffArgs &a) {
+    if (!p || !vol || !tf || !views) return hy_fail(ctx, HY_ERR_INVALID, "diff: null argument");
+    if (p->n <= 1) return hy_fail(ctx, HY_ERR_INVALID, "diff: volume edge must be > 1");
+    if (nviews <= 0 || nviews > kMaxDiffViews)
+        return hy_fail(ctx, HY_ERR_INVALID, "diff: 1..64 views");
+    if (W <= 0 || H <= 0) return hy_fail(ctx, HY_ERR_INVALID, "diff: bad resolution");
+    if (p->ntf <= 0 || p->ntf > kMaxKnots) return hy_fail(ctx, HY_ERR_INVALID, "diff: 1..256 knots");
+    if (p->ckpt_k <= 0 || p->ckpt_k > kMaxK)
+        return hy_fail(ctx, HY_ERR_INVALID, "diff: checkpoint interval 1..64");
+    if (!(p->sample_rate > 0.f)) return hy_fail(ctx, HY_ERR_INVALID, "diff: sample_rate <= 0");
+    std::memset(&a, 0, sizeof(a));
+    a.vol = vol;
+    a.n = p->n;
+    // one brick of edge n with a 1-voxel apron (lossless_block_paging.cc:20-22)
+    a.k = float(p->n) / float(p->n + 2);
+    a.b = float(1) / float(p->n) * a.k;
+    const float du = 1.f / float(p->n);
+    a.step = du / 4.f / p->sample_rate;
+    a.max_steps = p->max_steps;
+    a.density = p->density;
+    a.tf = reinterpret_cast<const float4 *>(tf);
+    a.ntf = p->ntf;
+    a.K = p->ckpt_k;
+    // the unit box's diagonal bounds every ray's step count
+    const long long maxn = std::min<long long>(p->max_steps, (long long)(1.7320509f / a.step) + 2);
+    a.max_ckpt = int((maxn + a.K - 1) / a.K) + 1;
+    a.W = W;
+    a.H = H;
+    a.nviews = nviews;
+    for (int v = 0; v < nviews; ++v) {
+        std::memcpy(a.views[v].trans, views[v].trans, sizeof(a.views[v].trans));
+        a.views[v].ctg = views[v].ctg_fovy_2;
+        for (int i = 0; i < 3; ++i) a.views[v].ray_o[i] = views[v].ray_o[i];
+    }
+    return HY_OK;
+}
+
+dim3 diff_grid(const DiffArgs &a) { return dim3((a.W + 15) / 16, (a.H + 7) / 8, a.nviews); }
+
+}  // namespace
+
+extern "C" int hy_diff_ckpt_bytes(const hy_diff_params *p, int32_t W, int32_t H, int32_t nviews,
+                                  int64_t *bytes) {
+    if (!p || !bytes || p->ckpt_k <= 0 || p->n <= 1 || !(p->sample_rate > 0.f))
+        return HY_ERR_INVALID;
+    const float step = 1.f / float(p->n) / 4.f / p->sample_rate;
+    const long long maxn = std::min<long long>(p->max_steps, (long long)(1.7320509f / step) + 2);
+    const long long per_ray = (maxn + p->ckpt_k - 1) / p->ckpt_k + 1;
+    *bytes = (int64_t)per_ray * 16 * W * H * nviews;
+    return HY_OK;
+}
+
+extern "C" int hy_diff_forward(hy_ctx *ctx, const hy_diff_params *p, const float *vol_dev,
+                               const float *tf_dev, const hy_view *views, int32_t nviews,
+                               int32_t W, int32_t H, float *image_dev, float *ckpt_dev,
+                               int32_t *nsteps_dev) {
+    if (!ctx) return HY_ERR_INVALID;
+    if (!image_dev) return hy_fail(ctx, HY_ERR_INVALID, "diff: null image");
+    DiffArgs a;
+    int rc = fill_diff(ctx, p, vol_dev, tf_dev, views, nviews, W, H, a);
+    if (rc) return rc;
+    if ((ckpt_dev == nullptr) != (nsteps_dev == nullptr))
+        return hy_fail(ctx, HY_ERR_INVALID, "diff: checkpoints and step counts go together");
+    a.image = reinterpret_cast<float4 *>(image_dev);
+    a.ckpt = reinterpret_cast<float4 *>(ckpt_dev);
+    a.nsteps_out = nsteps_dev;
+    HY_CUDA(ctx, cudaSetDevice(ctx->device));
+    HY_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
+    diff_forward_kernel<<<diff_grid(a), 128, 0, ctx->stream>>>(a);
+    HY_CUDA(ctx, cudaGetLastError());
+    HY_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
+    ctx->stats_pending = true;
+    ctx->pend_count = 0;
+    ctx->pend_pixels = (int64_t)W * H * nviews;
+    return HY_OK;
+}
+
+extern "C" int hy_diff_backward(hy_ctx *ctx, const hy_diff_params *p, const float *vol_dev,
+                                const float *tf_dev, const hy_view *views, int32_t nviews,
+                                int32_t W, int32_t H, const float *dimage_dev,
+                                const float *ckpt_dev, const int32_t *nsteps_dev,
+                                float *dvol_dev, float *dtf_dev) {
+    if (!ctx) return HY_ERR_INVALID;
+    if (!dimage_dev || !ckpt_dev || !nsteps_dev || !dvol_dev || !dtf_dev)
+        return hy_fail(ctx, HY_ERR_INVALID, "diff: null argument");
+    DiffArgs a;
+    int rc = fill_diff(ctx, p, vol_dev, tf_dev, views, nviews, W, H, a);
+    if (rc) return rc;
+    a.dimage = reinterpret_cast<const float4 *>(dimage_dev);
+    a.ckpt = const_cast<float4 *>(reinterpret_cast<const float4 *>(ckpt_dev));
+    a.nsteps_out = const_cast<int *>(nsteps_dev);
+    a.dvol = dvol_dev;
+    a.dtf = dtf_dev;
+    HY_CUDA(ctx, cudaSetDevice(ctx->device));
+    HY_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
+    diff_backward_kernel<<<diff_grid(a), 128, 0, ctx->stream>>>(a);
+    HY_CUDA(ctx, cudaGetLastError());
+    HY_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
+    ctx->stats_pending = true;
+    ctx->pend_count = 0;
+    ctx->pend_pixels = (int64_t)W * H * nviews;
+    return HY_OK;
+}

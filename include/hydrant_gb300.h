@@ -292,6 +292,38 @@ int hy_pager_present(const hy_pager *pager, uint8_t *mask);
 int hy_pager_render(hy_pager *pager, const hy_shader_params *params, const hy_camera *cam,
                     int32_t width, int32_t height, uint8_t *rgba_dev);
 
+/* ---- differentiable rendering (transfer function and voxel gradients) -------
+ * No counterpart in the reference (its shaders have no derivatives).  The
+ * forward is the Volume shader's march (volume_shader.cu:32-81) over one
+ * dense f32 brick of n^3 voxels with a 1-voxel replicate apron, with step_size
+ * held at 1 and no empty-space skipping (the two discontinuous parts); it
+ * stores the ray state every ckpt_k steps.  The backward recomputes each
+ * K-step segment from its checkpoint and back-propagates through compositing,
+ * the transfer function and the trilinear weights, accumulating into
+ * caller-zeroed gradient buffers.  All pointers are device pointers; views is
+ * a host array; both calls are asynchronous on the context's stream. */
+typedef struct hy_diff_params {
+    int32_t n;            /* volume edge (voxels); bbox = [0,1]^3 */
+    float sample_rate;    /* step = (1/n) / 4 / sample_rate */
+    int32_t max_steps;
+    float density;        /* opacity scale of the TF alpha */
+    int32_t ntf;          /* knots (<= 256) */
+    int32_t ckpt_k;       /* checkpoint interval, 1..64 */
+} hy_diff_params;
+
+/* Bytes of the checkpoint buffer for W x H x nviews rays. */
+int hy_diff_ckpt_bytes(const hy_diff_params *p, int32_t width, int32_t height, int32_t nviews,
+                       int64_t *bytes);
+/* image: nviews*H*W RGBA floats.  ckpt / nsteps may both be NULL (no backward). */
+int hy_diff_forward(hy_ctx *ctx, const hy_diff_params *p, const float *volume, const float *tf,
+                    const hy_view *views, int32_t nviews, int32_t width, int32_t height,
+                    float *image, float *ckpt, int32_t *nsteps);
+/* dL/dimage in, dL/dvolume (n^3) and dL/dtf (ntf*4) accumulated. */
+int hy_diff_backward(hy_ctx *ctx, const hy_diff_params *p, const float *volume, const float *tf,
+                     const hy_view *views, int32_t nviews, int32_t width, int32_t height,
+                     const float *dimage, const float *ckpt, const int32_t *nsteps,
+                     float *dvolume, float *dtf);
+
 /* ---- batched multi-view rendering -------------------------------------------
  * Many views rendered by one persistent launch replayed from a CUDA graph.
  * The reference renders one view per Raycaster pass (raycaster.hpp:32-54,

@@ -1186,3 +1186,270 @@ extern "C" void orc_lossless_order(const orc_volume *v, const float cam[10], con
     std::sort(d.begin(), d.end());
     for (int i = 0; i < n; ++i) order_out[i] = d[i].second;
 }
+
+// ---------------------------------------------------------------------------
+// Differentiable Volume march (one dense brick of n^3 voxels, 1-voxel
+// replicate apron; step_size fixed at 1, no empty-space skipping).  The float
+// version uses the reference's float operations and is the forward parity
+// target; the double version, with its analytic gradient, is the FP64
+// reference gradient.  Loss L = sum over pixels and RGBA of (v - target)^2.
+// ---------------------------------------------------------------------------
+namespace {
+
+template <typename T>
+struct DiffCtx {
+    const T *vol;
+    int n;
+    T k, b, step, density;
+    const T *tf;  // ntf * 4
+    int ntf;
+    int max_steps;
+};
+
+template <typename T>
+T dfloor(T x) { return std::floor(x); }
+
+// sample at brick-local l in [0,1]; fills raw indices and weights
+template <typename T>
+T diff_sample(const DiffCtx<T> &c, const T l[3], long long idx[8], T w[8]) {
+    const int P = c.n + 2;
+    const T fd = T(P);
+    T a[3];
+    int i0[3], i1[3];
+    for (int ax = 0; ax < 3; ++ax) {
+        T f = fd * (c.k * l[ax] + c.b);
+        f = f - fd * dfloor(f / fd);  // Wrap (identity for l in [0,1])
+        const T u = f - T(0.5);
+        const T flr = dfloor(u);
+        a[ax] = u - flr;
+        const int ix = iclamp(f2i(float(flr)), 0, P - 1);
+        const int jx = iclamp(f2i(float(std::ceil(u))), 0, P - 1);
+        i0[ax] = iclamp(ix - 1, 0, c.n - 1);
+        i1[ax] = iclamp(jx - 1, 0, c.n - 1);
+    }
+    auto at = [&](int X, int Y, int Z) {
+        return (long long)(Z * (long long)c.n + Y) * c.n + X;
+    };
+    const long long id[8] = {at(i0[0], i0[1], i0[2]), at(i1[0], i0[1], i0[2]),
+                             at(i0[0], i1[1], i0[2]), at(i1[0], i1[1], i0[2]),
+                             at(i0[0], i0[1], i1[2]), at(i1[0], i0[1], i1[2]),
+                             at(i0[0], i1[1], i1[2]), at(i1[0], i1[1], i1[2])};
+    const T bx = T(1) - a[0], by = T(1) - a[1], bz = T(1) - a[2];
+    const T x0_0 = c.vol[id[0]] * bx + c.vol[id[1]] * a[0];
+    const T x1_0 = c.vol[id[2]] * bx + c.vol[id[3]] * a[0];
+    const T x0_1 = c.vol[id[4]] * bx + c.vol[id[5]] * a[0];
+    const T x1_1 = c.vol[id[6]] * bx + c.vol[id[7]] * a[0];
+    const T y0 = x0_0 * by + x1_0 * a[1];
+    const T y1 = x0_1 * by + x1_1 * a[1];
+    if (idx) {
+        const T ww[8] = {bx * by * bz,   a[0] * by * bz,   bx * a[1] * bz,   a[0] * a[1] * bz,
+                         bx * by * a[2], a[0] * by * a[2], bx * a[1] * a[2], a[0] * a[1] * a[2]};
+        for (int t = 0; t < 8; ++t) {
+            idx[t] = id[t];
+            w[t] = ww[t];
+        }
+    }
+    return y0 * bz + y1 * a[2];
+}
+
+template <typename T>
+void diff_tf(const DiffCtx<T> &c, T s, T q[4], int &i, int &j, T &al, bool &inb) {
+    const T fn = T(c.ntf);
+    const T fx = fn * s;
+    inb = (T(0) <= fx && fx <= fn);
+    if (!inb) {
+        q[0] = q[1] = q[2] = q[3] = T(0);
+        i = j = 0;
+        al = T(0);
+        return;
+    }
+    const T u = fx - T(0.5);
+    const T flr = dfloor(u);
+    al = u - flr;
+    i = iclamp(f2i(float(flr)), 0, c.ntf - 1);
+    j = iclamp(f2i(float(std::ceil(u))), 0, c.ntf - 1);
+    for (int ch = 0; ch < 4; ++ch)
+        q[ch] = c.tf[4 * i + ch] * (T(1) - al) + c.tf[4 * j + ch] * al;
+}
+
+// ray for pixel (x, y) of a view; returns nsteps, sets o, d
+template <typename T>
+int diff_ray(const DiffCtx<T> &c, const float view[20], int x, int y, int W, int H, T o[3],
+             T d[3]) {
+    const T ccx = T(W) / T(2), ccy = T(H) / T(2);
+    const T ux = (T(x) - ccx) * T(2) / T(H);
+    const T uy = (T(y) - ccy) * T(2) / T(H);
+    const T v4[4] = {ux, -uy, -T(view[16]), T(1)};
+    T p[3];
+    for (int r = 0; r < 3; ++r)
+        p[r] = T(view[r]) * v4[0] + T(view[4 + r]) * v4[1] + T(view[8 + r]) * v4[2] +
+               T(view[12 + r]) * v4[3];
+    for (int r = 0; r < 3; ++r) {
+        o[r] = T(view[17 + r]);
+        d[r] = p[r] - o[r];
+    }
+    const T inv = T(1) / std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    for (int r = 0; r < 3; ++r) d[r] = d[r] * inv;
+    // slab test against [0,1]^3
+    T tn = -INFINITY, tf = INFINITY;
+    T tmin[3], tmax[3];
+    for (int r = 0; r < 3; ++r) {
+        const T ir = T(1) / d[r];
+        const T tb = ir * (T(0) - o[r]), tt = ir * (T(1) - o[r]);
+        tmin[r] = (tb < tt) ? tb : tt;
+        tmax[r] = (tt < tb) ? tb : tt;
+    }
+    tn = tmin[0];
+    tn = (tn < tmin[1]) ? tmin[1] : tn;
+    tn = (tn < tmin[2]) ? tmin[2] : tn;
+    tf = tmax[0];
+    tf = (tmax[1] < tf) ? tmax[1] : tf;
+    tf = (tmax[2] < tf) ? tmax[2] : tf;
+    if (!(tf > tn)) return 0;
+    if (tn < 0) tn = 0;
+    if (tf < 0) tf = 0;
+    for (int r = 0; r < 3; ++r) o[r] = o[r] + d[r] * tn;
+    return imin(c.max_steps, f2i(float((tf - tn) / c.step)));
+}
+
+template <typename T>
+void diff_pixel(const DiffCtx<T> &c, const float view[20], int x, int y, int W, int H, T v[4]) {
+    T o[3], d[3];
+    const int ns = diff_ray(c, view, x, y, W, H, o, d);
+    v[0] = v[1] = v[2] = v[3] = T(0);
+    const T s3[3] = {d[0] * c.step, d[1] * c.step, d[2] * c.step};
+    for (int s = 0; s < ns; ++s) {
+        const T l[3] = {o[0] - dfloor(o[0]), o[1] - dfloor(o[1]), o[2] - dfloor(o[2])};
+        const T val = diff_sample<T>(c, l, nullptr, nullptr);
+        T q[4];
+        int i, j;
+        T al;
+        bool inb;
+        diff_tf(c, val, q, i, j, al, inb);
+        q[3] = q[3] * c.density;
+        const T w = q[3];
+        const T ub[4] = {q[0] * w, q[1] * w, q[2] * w, q[3]};
+        const T t = T(1) - v[3];
+        for (int ch = 0; ch < 4; ++ch) v[ch] = v[ch] + ub[ch] * t;
+        for (int r = 0; r < 3; ++r) o[r] = o[r] + s3[r];
+    }
+}
+
+// FP64 adjoint of one pixel: g = dL/dv; accumulates into dvol / dtf.
+void diff_pixel_grad(const DiffCtx<double> &c, const float view[20], int x, int y, int W, int H,
+                     const double g[4], double *dvol, double *dtf) {
+    double o[3], d[3];
+    const int ns = diff_ray(c, view, x, y, W, H, o, d);
+    const double s3[3] = {d[0] * c.step, d[1] * c.step, d[2] * c.step};
+    std::vector<double> pw(ns), P(3 * size_t(ns));
+    double vw = 0;
+    for (int s = 0; s < ns; ++s) {
+        for (int r = 0; r < 3; ++r) P[3 * s + r] = o[r];
+        pw[s] = vw;
+        const double l[3] = {o[0] - std::floor(o[0]), o[1] - std::floor(o[1]), o[2] - std::floor(o[2])};
+        double q[4];
+        int i, j;
+        double al;
+        bool inb;
+        diff_tf(c, diff_sample<double>(c, l, nullptr, nullptr), q, i, j, al, inb);
+        const double a = q[3] * c.density;
+        vw = vw + a * (1.0 - vw);
+        for (int r = 0; r < 3; ++r) o[r] = o[r] + s3[r];
+    }
+    double R[4] = {0, 0, 0, 0};
+    for (int s = ns - 1; s >= 0; --s) {
+        const double l[3] = {P[3 * s] - std::floor(P[3 * s]), P[3 * s + 1] - std::floor(P[3 * s + 1]),
+                             P[3 * s + 2] - std::floor(P[3 * s + 2])};
+        long long idx[8];
+        double w[8];
+        const double val = diff_sample(c, l, idx, w);
+        double q[4];
+        int i, j;
+        double al;
+        bool inb;
+        diff_tf(c, val, q, i, j, al, inb);
+        const double a = q[3] * c.density;
+        const double T = 1.0 - pw[s];
+        const double gc[4] = {T * g[0], T * g[1], T * g[2], T * g[3]};
+        const double gdot = g[0] * R[0] + g[1] * R[1] + g[2] * R[2] + g[3] * R[3];
+        const double da = gc[0] * q[0] + gc[1] * q[1] + gc[2] * q[2] + gc[3] - T * gdot;
+        const double om = 1.0 - a;
+        R[0] = q[0] * a + om * R[0];
+        R[1] = q[1] * a + om * R[1];
+        R[2] = q[2] * a + om * R[2];
+        R[3] = a + om * R[3];
+        if (!inb) continue;
+        const double gq[4] = {gc[0] * a, gc[1] * a, gc[2] * a, da * c.density};
+        double ds = 0;
+        for (int ch = 0; ch < 4; ++ch) {
+            dtf[4 * i + ch] += gq[ch] * (1.0 - al);
+            dtf[4 * j + ch] += gq[ch] * al;
+            ds += gq[ch] * (c.tf[4 * j + ch] - c.tf[4 * i + ch]);
+        }
+        ds *= double(c.ntf);
+        for (int t = 0; t < 8; ++t) dvol[idx[t]] += ds * w[t];
+    }
+}
+
+template <typename T>
+DiffCtx<T> diff_ctx(const T *vol, int n, const T *tf, int ntf, float sample_rate, int max_steps,
+                    float density) {
+    DiffCtx<T> c;
+    c.vol = vol;
+    c.n = n;
+    c.k = T(n) / T(n + 2);
+    c.b = T(1) / T(n) * c.k;
+    const T du = T(1) / T(n);
+    c.step = du / T(4) / T(sample_rate);
+    c.density = T(density);
+    c.tf = tf;
+    c.ntf = ntf;
+    c.max_steps = max_steps;
+    return c;
+}
+
+}  // namespace
+
+extern "C" void orc_diff_forward(const float *vol, int32_t n, const float *tf, int32_t ntf,
+                                 float sample_rate, int32_t max_steps, float density,
+                                 const float *views, int32_t nviews, int32_t W, int32_t H,
+                                 int32_t nthreads, float *image) {
+    DiffCtx<float> c = diff_ctx<float>(vol, n, tf, ntf, sample_rate, max_steps, density);
+    if (nthreads <= 0) nthreads = 1;
+    std::vector<std::thread> th;
+    for (int t = 0; t < nthreads; ++t)
+        th.emplace_back([&, t] {
+            for (int row = t; row < nviews * H; row += nthreads) {
+                const int v = row / H, y = row % H;
+                for (int x = 0; x < W; ++x)
+                    diff_pixel(c, views + 20 * v, x, y, W, H,
+                               image + ((size_t(v) * H + y) * W + x) * 4);
+            }
+        });
+    for (auto &x : th) x.join();
+}
+
+extern "C" double orc_diff_loss_grad64(const double *vol, int32_t n, const double *tf, int32_t ntf,
+                                       float sample_rate, int32_t max_steps, float density,
+                                       const float *views, int32_t nviews, int32_t W, int32_t H,
+                                       const double *target, double *image, double *dvol,
+                                       double *dtf) {
+    DiffCtx<double> c = diff_ctx<double>(vol, n, tf, ntf, sample_rate, max_steps, density);
+    double loss = 0;
+    for (int v = 0; v < nviews; ++v)
+        for (int y = 0; y < H; ++y)
+            for (int x = 0; x < W; ++x) {
+                const size_t px = (size_t(v) * H + y) * W + x;
+                double pv[4];
+                diff_pixel(c, views + 20 * v, x, y, W, H, pv);
+                double g[4];
+                for (int ch = 0; ch < 4; ++ch) {
+                    const double r = pv[ch] - (target ? target[px * 4 + ch] : 0.0);
+                    loss += r * r;
+                    g[ch] = 2.0 * r;
+                    if (image) image[px * 4 + ch] = pv[ch];
+                }
+                if (dvol && dtf) diff_pixel_grad(c, views + 20 * v, x, y, W, H, g, dvol, dtf);
+            }
+    return loss;
+}

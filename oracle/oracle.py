@@ -208,3 +208,44 @@ def present_mask(vol: OracleVolume, ids) -> np.ndarray:
     m = np.zeros(vol.grid[0] * vol.grid[1] * vol.grid[2], np.uint8)
     m[np.asarray(ids, np.int64)] = 1
     return m
+
+
+def _diff_protos():
+    l = lib()
+    if not hasattr(l, "_diff_ready"):
+        l.orc_diff_forward.restype = None
+        l.orc_diff_forward.argtypes = [P, C.c_int32, P, C.c_int32, C.c_float, C.c_int32, C.c_float,
+                                       P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, P]
+        l.orc_diff_loss_grad64.restype = C.c_double
+        l.orc_diff_loss_grad64.argtypes = [P, C.c_int32, P, C.c_int32, C.c_float, C.c_int32,
+                                           C.c_float, P, C.c_int32, C.c_int32, C.c_int32, P, P, P, P]
+        l._diff_ready = True
+    return l
+
+
+def diff_forward(vol: np.ndarray, tf, views: np.ndarray, W: int, H: int, sample_rate=1.0,
+                 max_steps=4000000, density=1.0, nthreads=0) -> np.ndarray:
+    """FP32 differentiable-mode forward (reference float operations)."""
+    v = np.ascontiguousarray(vol, np.float32)
+    t = np.ascontiguousarray(np.asarray(tf, np.float32).reshape(-1, 4))
+    vw = np.ascontiguousarray(views, np.float32).reshape(-1, 20)
+    out = np.zeros((vw.shape[0], H, W, 4), np.float32)
+    _diff_protos().orc_diff_forward(_p(v), v.shape[0], _p(t), t.shape[0], sample_rate, max_steps,
+                                    density, _p(vw), vw.shape[0], W, H, nthreads or 8, _p(out))
+    return out
+
+
+def diff_loss_grad64(vol: np.ndarray, tf, views: np.ndarray, W: int, H: int, target=None,
+                     sample_rate=1.0, max_steps=4000000, density=1.0, grad=True):
+    """FP64 forward, L2 loss against `target` and its analytic gradient."""
+    v = np.ascontiguousarray(vol, np.float64)
+    t = np.ascontiguousarray(np.asarray(tf, np.float64).reshape(-1, 4))
+    vw = np.ascontiguousarray(views, np.float32).reshape(-1, 20)
+    tg = None if target is None else np.ascontiguousarray(target, np.float64)
+    img = np.zeros((vw.shape[0], H, W, 4), np.float64)
+    dv = np.zeros_like(v) if grad else None
+    dt = np.zeros_like(t) if grad else None
+    loss = _diff_protos().orc_diff_loss_grad64(_p(v), v.shape[0], _p(t), t.shape[0], sample_rate,
+                                               max_steps, density, _p(vw), vw.shape[0], W, H,
+                                               _p(tg), _p(img), _p(dv), _p(dt))
+    return loss, img, dv, dt

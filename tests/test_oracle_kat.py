@@ -223,3 +223,44 @@ def test_rows_subset_equals_full_render():
     full = orc.render(ov, TF9, params(), view, 16, 16)
     part = orc.render(ov, TF9, params(), view, 16, 16, rows=(5, 9))
     np.testing.assert_array_equal(full["v"][5:9], part["v"][5:9])
+
+
+def test_fp64_gradient_matches_central_differences():
+    """The oracle's FP64 analytic gradient of the differentiable march (TF
+    knots and voxels) against central finite differences, eps 1e-3."""
+    n, W, H = 16, 12, 12
+    rng = np.random.default_rng(11)
+    z, y, x = np.meshgrid(*(np.arange(n) + 0.5,) * 3, indexing="ij")
+    vol = np.zeros((n, n, n))
+    for _ in range(3):
+        c = rng.uniform(0.3, 0.7, 3) * n
+        s = rng.uniform(0.15, 0.3) * n
+        vol += rng.uniform(0.3, 0.7) * np.exp(-((x - c[0]) ** 2 + (y - c[1]) ** 2 + (z - c[2]) ** 2) / (2 * s * s))
+    vol = np.clip(vol, 0, 1)
+    ov = orc.OracleVolume(vol.astype(np.float32), n, 1)
+    views = np.stack([orc.camera_view(ov, orc.camera_orbit(a)) for a in [(20, 30, 2.2), (-70, -10, 2.4)]])
+    ntf = 8
+    tf_true = rng.uniform(0, 1, (ntf, 4))
+    tf_true[0] = 0
+    tf = np.full((ntf, 4), 0.5)
+    _, target, _, _ = orc.diff_loss_grad64(vol * 0.9, tf_true, views, W, H, grad=False)
+    _, _, dv, dt = orc.diff_loss_grad64(vol, tf, views, W, H, target)
+    eps = 1e-3
+
+    def loss(v, t):
+        return orc.diff_loss_grad64(v, t, views, W, H, target, grad=False)[0]
+
+    for i in range(ntf):
+        for c in range(4):
+            tp, tm = tf.copy(), tf.copy()
+            tp[i, c] += eps
+            tm[i, c] -= eps
+            fd = (loss(vol, tp) - loss(vol, tm)) / (2 * eps)
+            assert abs(fd - dt[i, c]) <= 1e-3 * max(abs(fd), 1e-2 * np.abs(dt).max()), (i, c, fd, dt[i, c])
+    for f in np.argsort(np.abs(dv).ravel())[-8:]:
+        vp, vm = vol.copy().ravel(), vol.copy().ravel()
+        vp[f] += eps
+        vm[f] -= eps
+        fd = (loss(vp.reshape(vol.shape), tf) - loss(vm.reshape(vol.shape), tf)) / (2 * eps)
+        g = dv.ravel()[f]
+        assert abs(fd - g) <= 1e-3 * max(abs(fd), 1e-2 * np.abs(dv).max()), (f, fd, g)
