@@ -50,7 +50,7 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["multiview", "volume", "tubes", "paging"],
+    ap.add_argument("--workload", choices=["multiview", "volume", "tubes", "paging", "diff"],
                     default="multiview")
     ap.add_argument("--frames", type=int, default=120, help="paging workload: orbit frames")
     ap.add_argument("--paging-scale", type=int, default=1,
@@ -528,12 +528,57 @@ def main_paging(args):
     return 0
 
 
+def main_diff(args):
+    """Differentiable fit: 256^3 f32 blob density (seed 4 truth, seed 5 init),
+    32-knot RGBA TF (seeded truth, uniform grey init), 16 views of 512^2 on a
+    seeded orbit, L2 image loss, checkpoints every 32 steps, Adam for
+    --steps iterations (default 200 here)."""
+    import numpy as np
+    import torch
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    build_all()
+    import hydrant_gb300 as hy
+    from hydrant_gb300 import fit
+
+    n, res, nviews, ntf = 256, 512, 16, 32
+    steps = args.frames if args.frames != 120 else 200
+    ctx = hy.Context(local)
+    vt = hy.synth_blobs_f32(4, (n, n, n), 24)
+    vi = hy.synth_blobs_f32(5, (n, n, n), 24)
+    holder = hy.Volume(ctx, vt, n, 1)
+    views = fit.orbit_views(holder, 4, nviews)
+    holder.close()
+    tft = fit.seeded_tf(4, ntf)
+    tfi = np.full((ntf, 4), 0.5, np.float32)
+    t0 = time.perf_counter()
+    res_fit = fit.fit(ctx, vt, vi, views, res, res, tft, tfi, steps=steps, ckpt_k=32)
+    wall = time.perf_counter() - t0
+    out = {
+        "metric": "fwd+adjoint ms/view", "value": res_fit.fwd_adj_ms_per_view, "unit": "ms/view",
+        "n_gpus": 1, "steps": steps, "warmup": 0, "higher_is_better": False, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": f"diff_fit_{n}cube_{nviews}x{res}px_{ntf}knots", "ckpt_k": 32},
+        "forward_ms_per_view": res_fit.fwd_ms_per_view,
+        "adjoint_over_forward": res_fit.fwd_adj_ms_per_view / res_fit.fwd_ms_per_view,
+        "loss_first": res_fit.losses[0], "loss_last": res_fit.losses[-1],
+        "loss_curve": res_fit.losses[:: max(1, steps // 20)],
+        "wall_s": wall,
+    }
+    print(json.dumps(out), flush=True)
+    ctx.close()
+    return 0
+
+
 def main():
     args = parse_args()
     if args.impl == "reference":
         return main_reference(args)
     if args.workload == "paging":
         return main_paging(args)
+    if args.workload == "diff":
+        return main_diff(args)
     return main_ours(args)
 
 

@@ -57,9 +57,13 @@ def test_adjoint_matches_fp64_gradient(setup):
     r = setup["r"]
     va = _va(setup["views"])
     _, target, _, _ = orc.diff_loss_grad64(setup["vt"], setup["tft"], va, W, H, grad=False)
-    loss64, img64, dv64, dt64 = orc.diff_loss_grad64(setup["vi"], setup["tfi"], va, W, H, target)
+    # a non-uniform TF: with the uniform initial one the image does not depend
+    # on the voxels at all (dTF/ds = 0) and the voxel gradient is exactly 0
+    tf_eval = np.clip(setup["tft"] * 0.8 + 0.1, 0, 1).astype(np.float32)
+    loss64, img64, dv64, dt64 = orc.diff_loss_grad64(setup["vi"], tf_eval, va, W, H, target)
+    assert np.linalg.norm(dv64) > 0 and np.linalg.norm(dt64) > 0
     vol = torch.from_numpy(setup["vi"]).cuda()
-    tf = torch.from_numpy(setup["tfi"]).cuda()
+    tf = torch.from_numpy(tf_eval).cuda()
     img = r.forward(vol, tf)
     g = 2.0 * (img - torch.from_numpy(target.astype(np.float32)).cuda())
     dv, dt = r.backward(vol, tf, g.contiguous())
