@@ -232,6 +232,33 @@ __global__ void __launch_bounds__(128) diff_backward_kernel(const __grid_constan
         float4 R = make_float4(0.f, 0.f, 0.f, 0.f);
         float px[kMaxK], py[kMaxK], pz[kMaxK], pw[kMaxK];
         const int nseg = (nsteps + a.K - 1) / a.K;
+        // Consecutive samples of a ray mostly share a knot interval and a
+        // voxel cell: gradients are summed in registers and flushed (one
+        // atomic per knot channel / cell corner) only when those change.
+        int ki_cur = -1, kj_cur = -1;
+        float4 acc_i = make_float4(0.f, 0.f, 0.f, 0.f), acc_j = acc_i;
+        int cell0 = -1, cell7 = -1;
+        int cidx[8];
+        float cacc[8];
+        auto flush_knots = [&]() {
+            if (ki_cur < 0) return;
+            atomicAdd(&gtf[ki_cur].x, acc_i.x);
+            atomicAdd(&gtf[ki_cur].y, acc_i.y);
+            atomicAdd(&gtf[ki_cur].z, acc_i.z);
+            atomicAdd(&gtf[ki_cur].w, acc_i.w);
+            atomicAdd(&gtf[kj_cur].x, acc_j.x);
+            atomicAdd(&gtf[kj_cur].y, acc_j.y);
+            atomicAdd(&gtf[kj_cur].z, acc_j.z);
+            atomicAdd(&gtf[kj_cur].w, acc_j.w);
+            acc_i = make_float4(0.f, 0.f, 0.f, 0.f);
+            acc_j = acc_i;
+        };
+        auto flush_cell = [&]() {
+            if (cell0 < 0) return;
+#pragma unroll
+            for (int t = 0; t < 8; ++t)
+                if (cacc[t] != 0.f) atomicAdd(a.dvol + cidx[t], cacc[t]);
+        };
         for (int seg = nseg - 1; seg >= 0; --seg) {
             const float4 c = a.ckpt[ray * a.max_ckpt + seg];
             float ox = c.x, oy = c.y, oz = c.z, vw = c.w;
@@ -276,25 +303,42 @@ __global__ void __launch_bounds__(128) diff_backward_kernel(const __grid_constan
                 // gradient of the TF output (r, g, b, A)
                 const float4 gq = make_float4(gcx * aa, gcy * aa, gcz * aa, da * a.density);
                 const float bb = 1.f - al;
-                atomicAdd(&gtf[i].x, gq.x * bb);
-                atomicAdd(&gtf[i].y, gq.y * bb);
-                atomicAdd(&gtf[i].z, gq.z * bb);
-                atomicAdd(&gtf[i].w, gq.w * bb);
-                atomicAdd(&gtf[j].x, gq.x * al);
-                atomicAdd(&gtf[j].y, gq.y * al);
-                atomicAdd(&gtf[j].z, gq.z * al);
-                atomicAdd(&gtf[j].w, gq.w * al);
+                if (i != ki_cur || j != kj_cur) {
+                    flush_knots();
+                    ki_cur = i;
+                    kj_cur = j;
+                }
+                acc_i.x += gq.x * bb;
+                acc_i.y += gq.y * bb;
+                acc_i.z += gq.z * bb;
+                acc_i.w += gq.w * bb;
+                acc_j.x += gq.x * al;
+                acc_j.y += gq.y * al;
+                acc_j.z += gq.z * al;
+                acc_j.w += gq.w * al;
                 // d TF / d s = (knot_j - knot_i) * n
                 const float4 kj = tf[j], ki = tf[i];
                 const float fn = float(a.ntf);
                 const float ds = (gq.x * (kj.x - ki.x) + gq.y * (kj.y - ki.y) +
                                   gq.z * (kj.z - ki.z) + gq.w * (kj.w - ki.w)) * fn;
-                if (ds != 0.f)
+                if (ds != 0.f) {
+                    if (tap.idx[0] != cell0 || tap.idx[7] != cell7) {
+                        flush_cell();
+                        cell0 = tap.idx[0];
+                        cell7 = tap.idx[7];
 #pragma unroll
-                    for (int t = 0; t < 8; ++t)
-                        if (tap.w[t] != 0.f) atomicAdd(a.dvol + tap.idx[t], ds * tap.w[t]);
+                        for (int t = 0; t < 8; ++t) {
+                            cidx[t] = tap.idx[t];
+                            cacc[t] = 0.f;
+                        }
+                    }
+#pragma unroll
+                    for (int t = 0; t < 8; ++t) cacc[t] += ds * tap.w[t];
+                }
             }
         }
+        flush_knots();
+        flush_cell();
     }
     __syncthreads();
     for (int i = threadIdx.x; i < a.ntf; i += blockDim.x) {

@@ -241,9 +241,9 @@ struct BrickCursor {
         pg = -1;
         br = BrickRef{};
     }
-    __device__ __forceinline__ void update(const DevVolume &V, float fgx, float fgy, float fgz,
-                                           float ox, float oy, float oz) {
+    __device__ __forceinline__ void update(const DevVolume &V, float ox, float oy, float oz) {
         if (ox >= ipx && ox < hx && oy >= ipy && oy < hy && oz >= ipz && oz < hz) return;
+        const float fgx = float(V.gx), fgy = float(V.gy), fgz = float(V.gz);
         ipx = floorf(ox);
         ipy = floorf(oy);
         ipz = floorf(oz);
@@ -261,26 +261,38 @@ struct BrickCursor {
     }
 };
 
-// VolumeShaderKernel::main (volume_shader.cu:32-81).
+// VolumeShaderKernel::main (volume_shader.cu:32-81), split into the per-ray
+// state and one loop iteration so that a caller can interleave rays (the
+// batched kernel refills finished lanes).  volume_main is the plain loop.
 // PADDED: the volume has an apron of >= 1 voxel, so the interior sampler applies.
-template <int PC, int DT, bool PADDED>
-__device__ __forceinline__ long long volume_main(Px &p, const ShadeArgs &A, const Shared &S) {
-    const DevVolume &V = A.vol;
-    long long samples = 0;
-    const float cdu = 1.f / gmax(gmax(fabsf(p.dx), fabsf(p.dy)), fabsf(p.dz));
-    const float rx = 1.f / p.dx, ry = 1.f / p.dy, rz = 1.f / p.dz;
-    const float fgx = float(V.gx), fgy = float(V.gy), fgz = float(V.gz);
+struct VolumeMarch {
     BrickCursor c;
-    c.reset();
-    int cur_ss = 0;
-    float sx = 0.f, sy = 0.f, sz = 0.f;
-    while (p.nsteps > 0) {
-        c.update(V, fgx, fgy, fgz, p.ox, p.oy, p.oz);
+    float cdu, rx, ry, rz;
+    float sx, sy, sz;
+    int cur_ss;
+
+    __device__ __forceinline__ void init(const Px &p) {
+        cdu = 1.f / gmax(gmax(fabsf(p.dx), fabsf(p.dy)), fabsf(p.dz));
+        rx = 1.f / p.dx;
+        ry = 1.f / p.dy;
+        rz = 1.f / p.dz;
+        c.reset();
+        cur_ss = 0;
+        sx = sy = sz = 0.f;
+    }
+
+    // One iteration of `while (nsteps > 0)`; false when the ray breaks out
+    // on an absent brick (volume_shader.cu:50).
+    template <int PC, int DT, bool PADDED>
+    __device__ __forceinline__ bool step(Px &p, const ShadeArgs &A, const Shared &S,
+                                         unsigned int &samples) {
+        const DevVolume &V = A.vol;
+        c.update(V, p.ox, p.oy, p.oz);
         if (c.cd) {
             p.nsteps -= skip_nblock_steps(p, rx, ry, rz, c.ipx, c.ipy, c.ipz, c.cd, cdu,
                                           A.step * float(p.step_size));
         } else {
-            if (c.pg == -1) break;
+            if (c.pg == -1) return false;
             float s = sample_brick<PC, DT, PADDED>(c.br, V.P, p.ox - c.ipx, p.oy - c.ipy,
                                                    p.oz - c.ipz, S.lut);
             ++samples;
@@ -326,7 +338,17 @@ __device__ __forceinline__ long long volume_main(Px &p, const ShadeArgs &A, cons
         p.oy = p.oy + sy;
         p.oz = p.oz + sz;
         p.nsteps -= p.step_size;
+        return true;
     }
+};
+
+template <int PC, int DT, bool PADDED>
+__device__ __forceinline__ long long volume_main(Px &p, const ShadeArgs &A, const Shared &S) {
+    unsigned int samples = 0;
+    VolumeMarch m;
+    m.init(p);
+    while (p.nsteps > 0)
+        if (!m.step<PC, DT, PADDED>(p, A, S, samples)) break;
     return samples;
 }
 
@@ -420,7 +442,7 @@ __device__ __forceinline__ long long iso_main(Px &p, const ShadeArgs &A, const V
     BrickCursor c;
     c.reset();
     while (p.nsteps > 0) {
-        c.update(V, fgx, fgy, fgz, p.ox, p.oy, p.oz);
+        c.update(V, p.ox, p.oy, p.oz);
         const float ipx = c.ipx, ipy = c.ipy, ipz = c.ipz;
         const BrickRef &br = c.br;
         if (c.cd) {
@@ -522,15 +544,14 @@ __device__ __forceinline__ void gen_ray(const ViewArgs &Vw, int x, int y, float 
     normalize3(dx, dy, dz);
 }
 
-// ray_emit_shader_impl (shader.hpp:113-137) against box [b0, b1]; init() of
-// the Volume (volume_shader.cu:16-21) and Isosurface (isosurface_shader.cu:34-39)
-// shaders.
-template <int SHADER, int PC, int DT, bool PADDED>
-__device__ __forceinline__ long long emit(Px &p, const ShadeArgs &A, const ViewArgs &Vw,
-                                          const Shared &S, float ox,
-                                          float oy, float oz, float dx, float dy, float dz,
-                                          float x0, float y0, float z0, float x1, float y1,
-                                          float z1) {
+// ray_emit_shader_impl (shader.hpp:113-137) against box [b0, b1] up to the
+// call of main: init() of the Volume (volume_shader.cu:16-21) and Isosurface
+// (isosurface_shader.cu:34-39) shaders, slab test, advance to tnear, step
+// count.  Returns false for a miss (nsteps = 0).
+template <int SHADER>
+__device__ __forceinline__ bool emit_setup(Px &p, const ShadeArgs &A, float ox, float oy,
+                                           float oz, float dx, float dy, float dz, float x0,
+                                           float y0, float z0, float x1, float y1, float z1) {
     p.ox = ox;
     p.oy = oy;
     p.oz = oz;
@@ -549,6 +570,7 @@ __device__ __forceinline__ long long emit(Px &p, const ShadeArgs &A, const ViewA
     } else {
         p.e0 = p.e1 = p.e2 = p.e3 = 0.f;
     }
+    p.step_size = 1;
     float tnear, tfar;
     if (intersect(ox, oy, oz, 1.f / dx, 1.f / dy, 1.f / dz, x0, y0, z0, x1, y1, z1, tnear, tfar)) {
         if (tnear < 0) tnear = 0;
@@ -557,11 +579,21 @@ __device__ __forceinline__ long long emit(Px &p, const ShadeArgs &A, const ViewA
         p.oy = p.oy + p.dy * tnear;
         p.oz = p.oz + p.dz * tnear;
         p.nsteps = min(A.max_steps, int((tfar - tnear) / A.step));
-        p.step_size = 1;
-        return run_main<SHADER, PC, DT, PADDED>(p, A, Vw, S);
+        return true;
     }
     p.nsteps = 0;
-    p.step_size = 1;
+    return false;
+}
+
+// ray_emit_shader_impl: emit_setup, then main on a hit (shader.hpp:113-137).
+template <int SHADER, int PC, int DT, bool PADDED>
+__device__ __forceinline__ long long emit(Px &p, const ShadeArgs &A, const ViewArgs &Vw,
+                                          const Shared &S, float ox,
+                                          float oy, float oz, float dx, float dy, float dz,
+                                          float x0, float y0, float z0, float x1, float y1,
+                                          float z1) {
+    if (emit_setup<SHADER>(p, A, ox, oy, oz, dx, dy, dz, x0, y0, z0, x1, y1, z1))
+        return run_main<SHADER, PC, DT, PADDED>(p, A, Vw, S);
     return 0;
 }
 
