@@ -409,7 +409,9 @@ int launch(hy_batch *b, uint8_t *out) {
         args.tile_w = b->cfg.tile_w;
         args.tile_h = 32 / b->cfg.tile_w;
         args.grab = b->cfg.grab;
-        args.block_queue = b->cfg.block_queue;
+        // mode 2 (lane refill) exists for the single-pass Volume shader only;
+        // other shaders run the per-warp queue
+        args.block_queue = b->cfg.block_queue == 1 ? 1 : 0;
         unit_shape(b->cfg, args.bx, args.by);
         args.queue = b->queue_dev;
         args.out = out;
