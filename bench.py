@@ -59,8 +59,6 @@ def parse_args():
     ap.add_argument("--res", type=int, default=0,
                     help="keep only the views of this resolution (profiling a small case)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--pool-f32", action="store_true",
-                    help="keep u8 bricks as normalised floats (4x pool, no table lookups)")
     ap.add_argument("--no-autotune", action="store_true",
                     help="use the default batch launch shape (profiling)")
     ap.add_argument("--cpu-sample-rows", type=int, default=0,
@@ -284,7 +282,7 @@ def main_ours(args):
     t_gen = time.perf_counter() - t0
     ctx = hy.Context(local)
     t0 = time.perf_counter()
-    vol = hy.Volume(ctx, vox, w.block_size, w.padding, pool_f32=args.pool_f32)
+    vol = hy.Volume(ctx, vox, w.block_size, w.padding)
     t_up = time.perf_counter() - t0
     ctx.set_transfer_fn(w.tf)
     info = vol.info

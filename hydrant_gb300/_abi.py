@@ -138,7 +138,6 @@ _PROTOS = {
     "hy_volume_create": (C.c_int, [P, C.POINTER(HyVolumeDesc), C.POINTER(P)]),
     "hy_volume_destroy": (C.c_int, [P]),
     "hy_volume_upload": (C.c_int, [P, P]),
-    "hy_volume_set_pool_f32": (C.c_int, [P, C.c_int32]),
     "hy_volume_get_info": (C.c_int, [P, C.POINTER(HyVolumeInfo)]),
     "hy_volume_thumbnails": (C.c_int, [P, P, P]),
     "hy_camera_orbit": (C.c_int, [P, P, C.c_float, C.POINTER(HyCamera)]),

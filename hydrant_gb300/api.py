@@ -77,8 +77,7 @@ class Context:
 class Volume:
     """A bricked volume resident on the device (hy_volume)."""
 
-    def __init__(self, ctx: Context, voxels: np.ndarray, block_size: int, padding: int = 1,
-                 pool_f32: bool = False):
+    def __init__(self, ctx: Context, voxels: np.ndarray, block_size: int, padding: int = 1):
         if voxels.ndim != 3:
             raise ValueError("voxels must be a (z, y, x) array")
         if voxels.dtype == np.uint8:
@@ -94,8 +93,6 @@ class Volume:
         ctx.check(lib().hy_volume_create(ctx.handle, C.byref(desc), C.byref(h)))
         self.handle = h
         self.desc = desc
-        if pool_f32:
-            ctx.check(lib().hy_volume_set_pool_f32(self.handle, 1))
         vox = np.ascontiguousarray(voxels)
         ctx.check(lib().hy_volume_upload(self.handle, _ptr(vox)))
 

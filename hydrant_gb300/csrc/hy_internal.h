@@ -118,8 +118,6 @@ struct hy_volume {
     float du = 0.f;
     bool uploaded = false;
     bool paged = false;       // pool is a brick cache owned by a hy_pager
-    bool pool_f32 = false;    // u8 volume stored as normalised floats
-    int pool_dtype() const { return (desc.dtype == HY_DTYPE_F32 || pool_f32) ? HY_DTYPE_F32 : HY_DTYPE_U8; }
 };
 
 int hy_volume_init(hy_ctx *ctx, const hy_volume_desc *desc, hy_volume *v);

@@ -225,8 +225,8 @@ extern "C" int hy_store_from_volume(const hy_volume *vol, hy_store **out) {
     if (!vol || !out) return HY_ERR_INVALID;
     *out = nullptr;
     hy_ctx *ctx = vol->ctx;
-    if (!vol->uploaded || vol->paged || vol->pool_f32)
-        return hy_fail(ctx, HY_ERR_STATE, "store: needs a resident, uploaded volume with its own dtype");
+    if (!vol->uploaded || vol->paged)
+        return hy_fail(ctx, HY_ERR_STATE, "store: needs a resident, uploaded volume");
     hy_store *s = new hy_store();
     s->ctx = ctx;
     store_geometry(s, vol->desc);

@@ -239,9 +239,7 @@ int dispatch_fused(const ShadeArgs &a, cudaStream_t s) {
     } else {
         const bool padded = a.vol.pad > 0;
         if (a.vol.dtype == HY_DTYPE_F32) {
-            if (padded && a.vol.P == 66)
-                launch_fused<SHADER, 66, HY_DTYPE_F32, true>(a, s);
-            else if (padded)
+            if (padded)
                 launch_fused<SHADER, 0, HY_DTYPE_F32, true>(a, s);
             else
                 launch_fused<SHADER, 0, HY_DTYPE_F32, false>(a, s);
@@ -308,7 +306,7 @@ int hy_fill_args(hy_ctx *ctx, const hy_volume *vol, const hy_shader_params *p, c
         return hy_fail(ctx, HY_ERR_STATE, "render: Volume shader needs a transfer function");
     std::memset(a, 0, sizeof(*a));
     a->vol = DevVolume{vol->pool, vol->info_dev, vol->reg_dev, vol->mean_dev, vol->grid[0],
-                       vol->grid[1], vol->grid[2], vol->P, vol->pool_dtype(), vol->desc.padding};
+                       vol->grid[1], vol->grid[2], vol->P, vol->desc.dtype, vol->desc.padding};
     for (int i = 0; i < 3; ++i) a->bbox_max[i] = vol->bbox_max[i];
     a->du = vol->du;
     a->step = vol->du / 4.f / p->sample_rate;  // basic_renderer.hpp:129

@@ -72,13 +72,7 @@ __global__ void brick_stats_kernel(const T *__restrict__ raw, int dx, int dy, in
     }
 }
 
-// u8 voxels written as u8, or as floats u / 255.f (the normalised value the
-// samplers read, texture_3d.hpp:78-86) when the pool holds floats.
-__device__ __forceinline__ void store_voxel(unsigned char *d, unsigned char v) { *d = v; }
-__device__ __forceinline__ void store_voxel(float *d, unsigned char v) { *d = float(v) / 255.f; }
-__device__ __forceinline__ void store_voxel(float *d, float v) { *d = v; }
-
-template <typename T, typename O>
+template <typename T>
 __global__ void brick_fill_kernel(const T *__restrict__ raw, int dx, int dy, int dz, int bs,
                                   int pad, int gx, int gy, const int *__restrict__ slot_brick,
                                   unsigned char *__restrict__ pool, long long slot_stride,
@@ -88,14 +82,14 @@ __global__ void brick_fill_kernel(const T *__restrict__ raw, int dx, int dy, int
     const int bx = bid % gx, by = (bid / gx) % gy, bz = bid / (gx * gy);
     const int P = bs + 2 * pad;
     const long long P3 = (long long)P * P * P;
-    O *dst = reinterpret_cast<O *>(pool + (long long)slot * slot_stride);
+    T *dst = reinterpret_cast<T *>(pool + (long long)slot * slot_stride);
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < P3;
          i += (long long)gridDim.x * blockDim.x) {
         int x = int(i % P), y = int((i / P) % P), z = int(i / ((long long)P * P));
         int X = min(max(bx * bs + x - pad, 0), dx - 1);
         int Y = min(max(by * bs + y - pad, 0), dy - 1);
         int Z = min(max(bz * bs + z - pad, 0), dz - 1);
-        store_voxel(dst + i, raw[((long long)Z * dy + Y) * dx + X]);
+        dst[i] = raw[((long long)Z * dy + Y) * dx + X];
     }
 }
 
@@ -171,10 +165,6 @@ int upload_impl(hy_volume *vol, const void *host) {
         }                                                      \
     } while (0)
     free_volume_device(vol);
-    {
-        const size_t pool_elem = (sizeof(T) == 1 && !vol->pool_f32) ? 1 : 4;
-        vol->slot_stride = (size_t(vol->P) * vol->P * vol->P * pool_elem + 255) / 256 * 256;
-    }
     HY_UP(cudaMalloc(&raw, nvox * sizeof(T)));
     HY_UP(cudaMemcpyAsync(raw, host, nvox * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
     const int nb = vol->nbricks;
@@ -218,9 +208,7 @@ int upload_impl(hy_volume *vol, const void *host) {
         for (int s0 = 0; s0 < vol->resident; s0 += 65535) {
             const int n = std::min(65535, vol->resident - s0);
             dim3 grid(unsigned((P3 + 255) / 256 < 512 ? (P3 + 255) / 256 : 512), unsigned(n));
-            auto fill = (sizeof(T) == 1 && !vol->pool_f32) ? brick_fill_kernel<T, T>
-                                                            : brick_fill_kernel<T, float>;
-            fill<<<grid, 256, 0, ctx->stream>>>(
+            brick_fill_kernel<T><<<grid, 256, 0, ctx->stream>>>(
                 raw, d.dim[0], d.dim[1], d.dim[2], d.block_size, d.padding, vol->grid[0],
                 vol->grid[1], slot_brick_dev, vol->pool, (long long)vol->slot_stride, s0);
             HY_UP(cudaGetLastError());
@@ -329,13 +317,5 @@ extern "C" int hy_volume_thumbnails(const hy_volume *vol, int32_t *chebyshev, fl
         if (chebyshev) chebyshev[i] = vol->cheb[i];
         if (mean) mean[i] = vol->mean[i];
     }
-    return HY_OK;
-}
-
-extern "C" int hy_volume_set_pool_f32(hy_volume *vol, int32_t enable) {
-    if (!vol) return HY_ERR_INVALID;
-    if (vol->paged) return hy_fail(vol->ctx, HY_ERR_STATE, "volume: paged volumes keep u8 bricks");
-    if (vol->uploaded) return hy_fail(vol->ctx, HY_ERR_STATE, "volume: set before upload");
-    vol->pool_f32 = enable != 0;
     return HY_OK;
 }

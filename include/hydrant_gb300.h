@@ -191,10 +191,6 @@ int hy_volume_destroy(hy_volume *vol);
  * decode + Texture3D::source upload of LosslessBlockPagingServer (
  * src/slave/paging/lossless_block_paging.cc:137-174) for resident volumes. */
 int hy_volume_upload(hy_volume *vol, const void *host_voxels);
-/* Before hy_volume_upload: keep a u8 volume's bricks as normalised floats
- * (u/255.f, the values the samplers read) -- 4x the pool, no per-voxel table
- * lookup; images are identical. */
-int hy_volume_set_pool_f32(hy_volume *vol, int32_t enable);
 int hy_volume_get_info(const hy_volume *vol, hy_volume_info *out);
 /* Copy the per-brick thumbnails to the host (grid x fastest). */
 int hy_volume_thumbnails(const hy_volume *vol, int32_t *chebyshev, float *mean);

@@ -214,24 +214,3 @@ def test_tubes_c1_isosurface_full(ctx):
             assert_parity(g, r, what=f"config 1 blocks {mode}")
     finally:
         c.close()
-
-
-@pytest.mark.parametrize("shader", ["Volume", "Isosurface"])
-def test_f32_pool_of_u8_volume_is_identical(ctx, shader):
-    vox = hy.synth_tubes_u8(1, (130, 130, 130), 12)  # 64^3 bricks, 3^3 grid, ragged edge
-    a = hy.Volume(ctx, vox, 64, 1)
-    b = hy.Volume(ctx, vox, 64, 1, pool_f32=True)
-    try:
-        assert b.info.slot_bytes >= 4 * 66 ** 3
-        ctx.set_transfer_fn(wl.TF9)
-        cam = camera(a=(35, 25, 2.3))
-        p = hy.shader_params(shader=shader, density=0.5, sample_rate=0.5, count_samples=True)
-        if shader == "Isosurface":
-            hy.iso_lighting(a, cam, p)
-        ra = hy.render(ctx, a, p, hy.camera_view(a, cam), 96, 80, want_v=True)
-        rb = hy.render(ctx, b, p, hy.camera_view(b, cam), 96, 80, want_v=True)
-        assert np.array_equal(ra.rgba, rb.rgba) and np.array_equal(ra.v, rb.v)
-        assert ra.samples == rb.samples
-    finally:
-        a.close()
-        b.close()
