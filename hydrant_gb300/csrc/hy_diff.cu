@@ -12,14 +12,15 @@
 // Every K steps the forward stores the ray state (position, v.w) in a
 // checkpoint buffer.  The adjoint walks a ray's segments back to front: it
 // restores a checkpoint, recomputes the K samples of that segment (positions,
-// values, transmittance) into a local array, and back-propagates through
-// front-to-back compositing, the transfer-function lookup and the trilinear
-// weights.  With c_n = (r a, g a, b a, a), T_n = 1 - v.w before sample n and
+// sample values, transmittance) into per-thread arrays, and back-propagates
+// through front-to-back compositing, the transfer-function lookup and the
+// trilinear weights without fetching the voxels a second time.  With c_n = (r a, g a, b a, a), T_n = 1 - v.w before sample n and
 // R_n = c_n + (1 - a_n) R_{n+1} the colour composited behind sample n:
 //   dL/dc_n = T_n g,   dL/da_n += -T_n (g . R_{n+1}),
-// with g = dL/dv of the pixel.  Knot gradients are summed per block in shared
-// memory before one global atomic per knot channel; voxel gradients are eight
-// atomics per sample.
+// with g = dL/dv of the pixel.  A ray sums its knot and voxel gradients in
+// registers while consecutive samples stay in one knot interval / voxel cell;
+// knot sums then go through shared memory (one global atomic per knot channel
+// and block), voxel sums straight to global atomics (eight per cell).
 
 #include <algorithm>
 #include <cstring>
@@ -62,60 +63,58 @@ struct DiffArgs {
     float *dtf;        // ntf * 4
 };
 
-// Trilinear sample of the padded brick at brick-local x in [0,1] (the
-// interior case of sample_brick: apron >= 1, no wrap, no clamps), returning
-// the eight raw-volume indices and weights for the adjoint.
-struct Tap {
-    int idx[8];
-    float w[8];
+// Trilinear footprint of the padded brick at brick-local x in [0,1] (the
+// interior case of sample_brick: apron >= 1, no wrap, no clamps): the raw
+// volume rows and columns of the 2x2x2 taps and the lerp fractions.  Voxel
+// indices fit in int (n^3 < 2^31 is checked on the host).
+struct Cell {
+    int r00, r10, r01, r11;  // row bases (z, y) -> (z * n + y) * n
+    int x0, x1;
+    float ax, ay, az;
 };
 
-__device__ __forceinline__ float diff_sample(const DiffArgs &a, float lx, float ly, float lz,
-                                             Tap *tap) {
+__device__ __forceinline__ void diff_cell(const DiffArgs &a, float lx, float ly, float lz,
+                                          Cell &c) {
     const int P = a.n + 2;
     const float fd = float(P);
     const float fx = fd * (a.k * lx + a.b), fy = fd * (a.k * ly + a.b), fz = fd * (a.k * lz + a.b);
     const float ux = fx - .5f, uy = fy - .5f, uz = fz - .5f;
     const float flx = floorf(ux), fly = floorf(uy), flz = floorf(uz);
-    const float ax = ux - flx, ay = uy - fly, az = uz - flz;
+    c.ax = ux - flx;
+    c.ay = uy - fly;
+    c.az = uz - flz;
     const int ix = int(flx), iy = int(fly), iz = int(flz);
     // padded index i -> raw clamp(i - 1, 0, n - 1)
-    const int x0 = iclamp(ix - 1, 0, a.n - 1), x1 = iclamp(ix, 0, a.n - 1);
-    const int y0 = iclamp(iy - 1, 0, a.n - 1), y1 = iclamp(iy, 0, a.n - 1);
-    const int z0 = iclamp(iz - 1, 0, a.n - 1), z1 = iclamp(iz, 0, a.n - 1);
-    const long long n = a.n;
-    const long long r00 = (z0 * n + y0) * n, r10 = (z0 * n + y1) * n, r01 = (z1 * n + y0) * n,
-                    r11 = (z1 * n + y1) * n;
-    const float v000 = __ldg(a.vol + r00 + x0), v100 = __ldg(a.vol + r00 + x1);
-    const float v010 = __ldg(a.vol + r10 + x0), v110 = __ldg(a.vol + r10 + x1);
-    const float v001 = __ldg(a.vol + r01 + x0), v101 = __ldg(a.vol + r01 + x1);
-    const float v011 = __ldg(a.vol + r11 + x0), v111 = __ldg(a.vol + r11 + x1);
-    const float bx = 1.f - ax, by = 1.f - ay, bz = 1.f - az;
-    const float x0_0 = v000 * bx + v100 * ax;
-    const float x1_0 = v010 * bx + v110 * ax;
-    const float x0_1 = v001 * bx + v101 * ax;
-    const float x1_1 = v011 * bx + v111 * ax;
-    const float yy0 = x0_0 * by + x1_0 * ay;
-    const float yy1 = x0_1 * by + x1_1 * ay;
-    if (tap) {
-        tap->idx[0] = int(r00 + x0);
-        tap->idx[1] = int(r00 + x1);
-        tap->idx[2] = int(r10 + x0);
-        tap->idx[3] = int(r10 + x1);
-        tap->idx[4] = int(r01 + x0);
-        tap->idx[5] = int(r01 + x1);
-        tap->idx[6] = int(r11 + x0);
-        tap->idx[7] = int(r11 + x1);
-        tap->w[0] = bx * by * bz;
-        tap->w[1] = ax * by * bz;
-        tap->w[2] = bx * ay * bz;
-        tap->w[3] = ax * ay * bz;
-        tap->w[4] = bx * by * az;
-        tap->w[5] = ax * by * az;
-        tap->w[6] = bx * ay * az;
-        tap->w[7] = ax * ay * az;
-    }
-    return yy0 * bz + yy1 * az;
+    const int n = a.n;
+    c.x0 = iclamp(ix - 1, 0, n - 1);
+    c.x1 = iclamp(ix, 0, n - 1);
+    const int y0 = iclamp(iy - 1, 0, n - 1), y1 = iclamp(iy, 0, n - 1);
+    const int z0 = iclamp(iz - 1, 0, n - 1), z1 = iclamp(iz, 0, n - 1);
+    c.r00 = (z0 * n + y0) * n;
+    c.r10 = (z0 * n + y1) * n;
+    c.r01 = (z1 * n + y0) * n;
+    c.r11 = (z1 * n + y1) * n;
+}
+
+__device__ __forceinline__ float diff_fetch(const DiffArgs &a, const Cell &c) {
+    const float v000 = __ldg(a.vol + c.r00 + c.x0), v100 = __ldg(a.vol + c.r00 + c.x1);
+    const float v010 = __ldg(a.vol + c.r10 + c.x0), v110 = __ldg(a.vol + c.r10 + c.x1);
+    const float v001 = __ldg(a.vol + c.r01 + c.x0), v101 = __ldg(a.vol + c.r01 + c.x1);
+    const float v011 = __ldg(a.vol + c.r11 + c.x0), v111 = __ldg(a.vol + c.r11 + c.x1);
+    const float bx = 1.f - c.ax, by = 1.f - c.ay, bz = 1.f - c.az;
+    const float x0_0 = v000 * bx + v100 * c.ax;
+    const float x1_0 = v010 * bx + v110 * c.ax;
+    const float x0_1 = v001 * bx + v101 * c.ax;
+    const float x1_1 = v011 * bx + v111 * c.ax;
+    const float yy0 = x0_0 * by + x1_0 * c.ay;
+    const float yy1 = x0_1 * by + x1_1 * c.ay;
+    return yy0 * bz + yy1 * c.az;
+}
+
+__device__ __forceinline__ float diff_sample(const DiffArgs &a, float lx, float ly, float lz) {
+    Cell c;
+    diff_cell(a, lx, ly, lz, c);
+    return diff_fetch(a, c);
 }
 
 // emit against the unit box; returns nsteps, sets o and d
@@ -186,10 +185,16 @@ __global__ void __launch_bounds__(128) diff_forward_kernel(const __grid_constant
     const int nsteps = diff_emit(a, view, x, y, ox, oy, oz, dx, dy, dz);
     float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
     const float sx = dx * a.step, sy = dy * a.step, sz = dz * a.step;  // step_size 1
+    float4 *cp = a.ckpt ? a.ckpt + ray * a.max_ckpt : nullptr;
+    int until_ckpt = 0;  // a checkpoint before steps 0, K, 2K, ...
     for (int s = 0; s < nsteps; ++s) {
-        if (a.ckpt && s % a.K == 0) a.ckpt[ray * a.max_ckpt + s / a.K] = make_float4(ox, oy, oz, v.w);
+        if (until_ckpt == 0) {
+            if (cp) *cp++ = make_float4(ox, oy, oz, v.w);
+            until_ckpt = a.K;
+        }
+        --until_ckpt;
         const float ipx = floorf(ox), ipy = floorf(oy), ipz = floorf(oz);
-        const float val = diff_sample(a, ox - ipx, oy - ipy, oz - ipz, nullptr);
+        const float val = diff_sample(a, ox - ipx, oy - ipy, oz - ipz);
         int i, j;
         float al;
         bool inb;
@@ -212,6 +217,114 @@ __global__ void __launch_bounds__(128) diff_forward_kernel(const __grid_constant
     if (a.nsteps_out) a.nsteps_out[ray] = nsteps;
 }
 
+// Gradient accumulators of one ray.  Consecutive samples mostly share a knot
+// interval and a voxel cell, so gradients are summed in registers and flushed
+// (one atomic per knot channel / cell corner) only when those change.
+struct GradAcc {
+    int ki = -1, kj = -1;
+    float4 acc_i = make_float4(0.f, 0.f, 0.f, 0.f), acc_j = make_float4(0.f, 0.f, 0.f, 0.f);
+    Cell cell;
+    bool has_cell = false;
+    float cacc[8];
+
+    __device__ __forceinline__ void flush_knots(float4 *gtf) {
+        if (ki < 0) return;
+        atomicAdd(&gtf[ki].x, acc_i.x);
+        atomicAdd(&gtf[ki].y, acc_i.y);
+        atomicAdd(&gtf[ki].z, acc_i.z);
+        atomicAdd(&gtf[ki].w, acc_i.w);
+        atomicAdd(&gtf[kj].x, acc_j.x);
+        atomicAdd(&gtf[kj].y, acc_j.y);
+        atomicAdd(&gtf[kj].z, acc_j.z);
+        atomicAdd(&gtf[kj].w, acc_j.w);
+        acc_i = make_float4(0.f, 0.f, 0.f, 0.f);
+        acc_j = acc_i;
+    }
+    __device__ __forceinline__ void flush_cell(float *dvol) {
+        if (!has_cell) return;
+        const int idx[8] = {cell.r00 + cell.x0, cell.r00 + cell.x1, cell.r10 + cell.x0,
+                            cell.r10 + cell.x1, cell.r01 + cell.x0, cell.r01 + cell.x1,
+                            cell.r11 + cell.x0, cell.r11 + cell.x1};
+#pragma unroll
+        for (int t = 0; t < 8; ++t)
+            if (cacc[t] != 0.f) atomicAdd(dvol + idx[t], cacc[t]);
+    }
+};
+
+// Back-propagates one sample: its position's cell, its value `val`, the
+// transmittance T before it and R (the colour composited behind it, updated
+// to include this sample).
+__device__ __forceinline__ void diff_adjoint_sample(const DiffArgs &a, const float4 *tf,
+                                                    float4 *gtf, GradAcc &G, const float4 &g,
+                                                    float4 &R, float px, float py, float pz,
+                                                    float val, float T) {
+    int i, j;
+    float al;
+    bool inb;
+    const float4 q = tf_eval(tf, a.ntf, val, i, j, al, inb);
+    const float aa = q.w * a.density;
+    // The gradient arithmetic has no float-exact counterpart to follow, so it
+    // uses fused multiply-adds (the file is compiled with contraction off).
+    // dL/dc = T g ; transmittance term through later samples
+    const float gcx = T * g.x, gcy = T * g.y, gcz = T * g.z, gcw = T * g.w;
+    const float gdot = __fmaf_rn(g.w, R.w, __fmaf_rn(g.z, R.z, __fmaf_rn(g.y, R.y, g.x * R.x)));
+    const float da =
+        __fmaf_rn(-T, gdot, __fmaf_rn(gcz, q.z, __fmaf_rn(gcy, q.y, __fmaf_rn(gcx, q.x, gcw))));
+    // R_n = c_n + (1 - a_n) R_{n+1}
+    const float om = 1.f - aa;
+    R = make_float4(__fmaf_rn(om, R.x, q.x * aa), __fmaf_rn(om, R.y, q.y * aa),
+                    __fmaf_rn(om, R.z, q.z * aa), __fmaf_rn(om, R.w, aa));
+    if (!inb) return;
+    // gradient of the TF output (r, g, b, A)
+    const float4 gq = make_float4(gcx * aa, gcy * aa, gcz * aa, da * a.density);
+    const float bb = 1.f - al;
+    if (i != G.ki || j != G.kj) {
+        G.flush_knots(gtf);
+        G.ki = i;
+        G.kj = j;
+    }
+    G.acc_i.x = __fmaf_rn(gq.x, bb, G.acc_i.x);
+    G.acc_i.y = __fmaf_rn(gq.y, bb, G.acc_i.y);
+    G.acc_i.z = __fmaf_rn(gq.z, bb, G.acc_i.z);
+    G.acc_i.w = __fmaf_rn(gq.w, bb, G.acc_i.w);
+    G.acc_j.x = __fmaf_rn(gq.x, al, G.acc_j.x);
+    G.acc_j.y = __fmaf_rn(gq.y, al, G.acc_j.y);
+    G.acc_j.z = __fmaf_rn(gq.z, al, G.acc_j.z);
+    G.acc_j.w = __fmaf_rn(gq.w, al, G.acc_j.w);
+    // d TF / d s = (knot_j - knot_i) * n
+    const float4 kj = tf[j], ki = tf[i];
+    const float fn = float(a.ntf);
+    const float ds = fn * __fmaf_rn(gq.w, kj.w - ki.w,
+                                    __fmaf_rn(gq.z, kj.z - ki.z,
+                                              __fmaf_rn(gq.y, kj.y - ki.y, gq.x * (kj.x - ki.x))));
+    if (ds == 0.f) return;
+    Cell c;
+    diff_cell(a, px - floorf(px), py - floorf(py), pz - floorf(pz), c);
+    if (!G.has_cell || c.r00 + c.x0 != G.cell.r00 + G.cell.x0 ||
+        c.r11 + c.x1 != G.cell.r11 + G.cell.x1) {
+        G.flush_cell(a.dvol);
+        G.cell = c;
+        G.has_cell = true;
+#pragma unroll
+        for (int t = 0; t < 8; ++t) G.cacc[t] = 0.f;
+    }
+    // trilinear weights w = (x-weight) * (y-weight) * (z-weight), times ds
+    const float ax = c.ax, ay = c.ay, az = c.az;
+    const float bx = 1.f - ax, by = 1.f - ay, bz = 1.f - az;
+    const float d00 = ds * (by * bz), d10 = ds * (ay * bz), d01 = ds * (by * az),
+                d11 = ds * (ay * az);
+    G.cacc[0] = __fmaf_rn(bx, d00, G.cacc[0]);
+    G.cacc[1] = __fmaf_rn(ax, d00, G.cacc[1]);
+    G.cacc[2] = __fmaf_rn(bx, d10, G.cacc[2]);
+    G.cacc[3] = __fmaf_rn(ax, d10, G.cacc[3]);
+    G.cacc[4] = __fmaf_rn(bx, d01, G.cacc[4]);
+    G.cacc[5] = __fmaf_rn(ax, d01, G.cacc[5]);
+    G.cacc[6] = __fmaf_rn(bx, d11, G.cacc[6]);
+    G.cacc[7] = __fmaf_rn(ax, d11, G.cacc[7]);
+}
+
+// The adjoint walks a ray's segments back to front; a segment's recomputed
+// positions, values and transmittances sit in per-thread arrays.
 __global__ void __launch_bounds__(128) diff_backward_kernel(const __grid_constant__ DiffArgs a) {
     __shared__ float4 tf[kMaxKnots];
     __shared__ float4 gtf[kMaxKnots];
@@ -230,115 +343,39 @@ __global__ void __launch_bounds__(128) diff_backward_kernel(const __grid_constan
         diff_emit(a, view, x, y, ox0, oy0, oz0, dx, dy, dz);
         const float sx = dx * a.step, sy = dy * a.step, sz = dz * a.step;
         float4 R = make_float4(0.f, 0.f, 0.f, 0.f);
-        float px[kMaxK], py[kMaxK], pz[kMaxK], pw[kMaxK];
-        const int nseg = (nsteps + a.K - 1) / a.K;
-        // Consecutive samples of a ray mostly share a knot interval and a
-        // voxel cell: gradients are summed in registers and flushed (one
-        // atomic per knot channel / cell corner) only when those change.
-        int ki_cur = -1, kj_cur = -1;
-        float4 acc_i = make_float4(0.f, 0.f, 0.f, 0.f), acc_j = acc_i;
-        int cell0 = -1, cell7 = -1;
-        int cidx[8];
-        float cacc[8];
-        auto flush_knots = [&]() {
-            if (ki_cur < 0) return;
-            atomicAdd(&gtf[ki_cur].x, acc_i.x);
-            atomicAdd(&gtf[ki_cur].y, acc_i.y);
-            atomicAdd(&gtf[ki_cur].z, acc_i.z);
-            atomicAdd(&gtf[ki_cur].w, acc_i.w);
-            atomicAdd(&gtf[kj_cur].x, acc_j.x);
-            atomicAdd(&gtf[kj_cur].y, acc_j.y);
-            atomicAdd(&gtf[kj_cur].z, acc_j.z);
-            atomicAdd(&gtf[kj_cur].w, acc_j.w);
-            acc_i = make_float4(0.f, 0.f, 0.f, 0.f);
-            acc_j = acc_i;
-        };
-        auto flush_cell = [&]() {
-            if (cell0 < 0) return;
-#pragma unroll
-            for (int t = 0; t < 8; ++t)
-                if (cacc[t] != 0.f) atomicAdd(a.dvol + cidx[t], cacc[t]);
-        };
+        const int K = a.K;
+        float px[kMaxK], py[kMaxK], pz[kMaxK], pw[kMaxK], pv[kMaxK];
+        const int nseg = (nsteps + K - 1) / K;
+        GradAcc G;
+        const float4 *cps = a.ckpt + ray * a.max_ckpt;
         for (int seg = nseg - 1; seg >= 0; --seg) {
-            const float4 c = a.ckpt[ray * a.max_ckpt + seg];
+            const float4 c = cps[seg];
             float ox = c.x, oy = c.y, oz = c.z, vw = c.w;
-            const int s0 = seg * a.K, cnt = min(a.K, nsteps - s0);
-            // recompute the segment's positions and v.w before each sample
+            const int cnt = min(K, nsteps - seg * K);
+            // recompute the segment: positions, values and v.w before each sample
             for (int s = 0; s < cnt; ++s) {
                 px[s] = ox;
                 py[s] = oy;
                 pz[s] = oz;
                 pw[s] = vw;
                 const float ipx = floorf(ox), ipy = floorf(oy), ipz = floorf(oz);
-                const float val = diff_sample(a, ox - ipx, oy - ipy, oz - ipz, nullptr);
+                const float val = diff_sample(a, ox - ipx, oy - ipy, oz - ipz);
+                pv[s] = val;
                 int i, j;
                 float al;
                 bool inb;
-                float4 ub = tf_eval(tf, a.ntf, val, i, j, al, inb);
+                const float4 ub = tf_eval(tf, a.ntf, val, i, j, al, inb);
                 const float aa = ub.w * a.density;
                 vw = vw + aa * (1.f - vw);
                 ox = ox + sx;
                 oy = oy + sy;
                 oz = oz + sz;
             }
-            for (int s = cnt - 1; s >= 0; --s) {
-                const float ipx = floorf(px[s]), ipy = floorf(py[s]), ipz = floorf(pz[s]);
-                Tap tap;
-                const float val = diff_sample(a, px[s] - ipx, py[s] - ipy, pz[s] - ipz, &tap);
-                int i, j;
-                float al;
-                bool inb;
-                const float4 q = tf_eval(tf, a.ntf, val, i, j, al, inb);
-                const float aa = q.w * a.density;
-                const float T = 1.f - pw[s];
-                // dL/dc = T g ; transmittance term through later samples
-                const float gcx = T * g.x, gcy = T * g.y, gcz = T * g.z, gcw = T * g.w;
-                const float gdot = g.x * R.x + g.y * R.y + g.z * R.z + g.w * R.w;
-                const float da = gcx * q.x + gcy * q.y + gcz * q.z + gcw - T * gdot;
-                // R_n = c_n + (1 - a_n) R_{n+1}
-                const float om = 1.f - aa;
-                R = make_float4(q.x * aa + om * R.x, q.y * aa + om * R.y, q.z * aa + om * R.z,
-                                aa + om * R.w);
-                if (!inb) continue;
-                // gradient of the TF output (r, g, b, A)
-                const float4 gq = make_float4(gcx * aa, gcy * aa, gcz * aa, da * a.density);
-                const float bb = 1.f - al;
-                if (i != ki_cur || j != kj_cur) {
-                    flush_knots();
-                    ki_cur = i;
-                    kj_cur = j;
-                }
-                acc_i.x += gq.x * bb;
-                acc_i.y += gq.y * bb;
-                acc_i.z += gq.z * bb;
-                acc_i.w += gq.w * bb;
-                acc_j.x += gq.x * al;
-                acc_j.y += gq.y * al;
-                acc_j.z += gq.z * al;
-                acc_j.w += gq.w * al;
-                // d TF / d s = (knot_j - knot_i) * n
-                const float4 kj = tf[j], ki = tf[i];
-                const float fn = float(a.ntf);
-                const float ds = (gq.x * (kj.x - ki.x) + gq.y * (kj.y - ki.y) +
-                                  gq.z * (kj.z - ki.z) + gq.w * (kj.w - ki.w)) * fn;
-                if (ds != 0.f) {
-                    if (tap.idx[0] != cell0 || tap.idx[7] != cell7) {
-                        flush_cell();
-                        cell0 = tap.idx[0];
-                        cell7 = tap.idx[7];
-#pragma unroll
-                        for (int t = 0; t < 8; ++t) {
-                            cidx[t] = tap.idx[t];
-                            cacc[t] = 0.f;
-                        }
-                    }
-#pragma unroll
-                    for (int t = 0; t < 8; ++t) cacc[t] += ds * tap.w[t];
-                }
-            }
+            for (int s = cnt - 1; s >= 0; --s)
+                diff_adjoint_sample(a, tf, gtf, G, g, R, px[s], py[s], pz[s], pv[s], 1.f - pw[s]);
         }
-        flush_knots();
-        flush_cell();
+        G.flush_knots(gtf);
+        G.flush_cell(a.dvol);
     }
     __syncthreads();
     for (int i = threadIdx.x; i < a.ntf; i += blockDim.x) {
@@ -354,6 +391,8 @@ int fill_diff(hy_ctx *ctx, const hy_diff_params *p, const float *vol, const floa
               const hy_view *views, int nviews, int W, int H, DiffArgs &a) {
     if (!p || !vol || !tf || !views) return hy_fail(ctx, HY_ERR_INVALID, "diff: null argument");
     if (p->n <= 1) return hy_fail(ctx, HY_ERR_INVALID, "diff: volume edge must be > 1");
+    if ((long long)p->n * p->n * p->n >= (1LL << 31))
+        return hy_fail(ctx, HY_ERR_INVALID, "diff: volume edge must be <= 1290 (n^3 < 2^31)");
     if (nviews <= 0 || nviews > kMaxDiffViews)
         return hy_fail(ctx, HY_ERR_INVALID, "diff: 1..64 views");
     if (W <= 0 || H <= 0) return hy_fail(ctx, HY_ERR_INVALID, "diff: bad resolution");

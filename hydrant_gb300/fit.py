@@ -34,7 +34,7 @@ class DiffRenderer:
     """One set of views at one resolution over an n^3 f32 volume."""
 
     def __init__(self, ctx: Context, n: int, views: List[_abi.HyView], width: int, height: int,
-                 ntf: int, sample_rate: float = 1.0, density: float = 1.0, ckpt_k: int = 32,
+                 ntf: int, sample_rate: float = 1.0, density: float = 1.0, ckpt_k: int = 16,
                  max_steps: int = 4000000):
         self.ctx = ctx
         self.p = _abi.HyDiffParams(n, sample_rate, max_steps, density, ntf, ckpt_k)
@@ -129,14 +129,18 @@ class FitResult:
     losses: List[float] = field(default_factory=list)
     fwd_ms_per_view: float = 0.0
     fwd_adj_ms_per_view: float = 0.0
+    iter_ms: List[float] = field(default_factory=list)
     steps: int = 0
 
 
 def fit(ctx: Context, target_vol: np.ndarray, init_vol: np.ndarray, views, W: int, H: int,
         true_tf: np.ndarray, init_tf: np.ndarray, steps: int = 200, lr_tf: float = 2e-2,
         lr_vol: float = 1e-2, sample_rate: float = 1.0, density: float = 1.0,
-        ckpt_k: int = 32) -> FitResult:
-    """Adam on (transfer function, volume) against images of the targets."""
+        ckpt_k: int = 16, warmup: int = 3) -> FitResult:
+    """Adam on (transfer function, volume) against images of the targets.
+
+    The first `warmup` iterations (one-off library and allocator set-up) are
+    left out of the forward + adjoint timing."""
     dev = torch.device("cuda", ctx.device)
     n = target_vol.shape[0]
     r = DiffRenderer(ctx, n, views, W, H, true_tf.shape[0], sample_rate, density, ckpt_k)
@@ -156,7 +160,7 @@ def fit(ctx: Context, target_vol: np.ndarray, init_vol: np.ndarray, views, W: in
     torch.cuda.synchronize()
     res.fwd_ms_per_view = (time.perf_counter() - t0) / 3 / nv * 1e3
     t_fb = 0.0
-    for it in range(steps):
+    for it in range(warmup + steps):
         opt.zero_grad(set_to_none=True)
         torch.cuda.synchronize()
         t1 = time.perf_counter()
@@ -164,7 +168,10 @@ def fit(ctx: Context, target_vol: np.ndarray, init_vol: np.ndarray, views, W: in
         loss = ((img - target) ** 2).mean()
         loss.backward()
         torch.cuda.synchronize()
-        t_fb += time.perf_counter() - t1
+        dt = time.perf_counter() - t1
+        if it >= warmup:
+            t_fb += dt
+            res.iter_ms.append(dt * 1e3)
         opt.step()
         with torch.no_grad():
             vol.clamp_(0.0, 1.0)

@@ -90,3 +90,24 @@ def test_autograd_and_adam(ctx, setup):
     torch.cuda.synchronize()
     assert torch.allclose(vol.grad, dv, rtol=1e-4, atol=1e-5 * float(dv.abs().max()))
     assert torch.allclose(tf.grad, dt, rtol=1e-4, atol=1e-5 * float(dt.abs().max()))
+
+
+@pytest.mark.parametrize("k", [4, 5, 1, 64])
+def test_checkpoint_interval_does_not_change_gradients(ctx, setup, k):
+    """K = 4 and 8 keep a segment in registers, other K in local memory; the
+    per-ray sums are the same, only the order of atomics between rays differs."""
+    torch = setup["torch"]
+    vol = torch.from_numpy(setup["vi"]).cuda()
+    tf = torch.from_numpy(np.clip(setup["tft"] * 0.8 + 0.1, 0, 1).astype(np.float32)).cuda()
+    out = []
+    for kk in (8, k):
+        r = fit.DiffRenderer(ctx, N, setup["views"], W, H, 16, sample_rate=1.0, density=1.0,
+                             ckpt_k=kk)
+        img = r.forward(vol, tf)
+        g = torch.linspace(-1, 1, img.numel(), device="cuda").reshape(img.shape)
+        dv, dt = r.backward(vol, tf, g)
+        torch.cuda.synchronize()
+        out.append((img.cpu().numpy(), dv.cpu().numpy(), dt.cpu().numpy()))
+    assert np.array_equal(out[0][0], out[1][0])
+    for a, b in ((out[0][1], out[1][1]), (out[0][2], out[1][2])):
+        assert np.linalg.norm(a - b) <= 1e-5 * np.linalg.norm(a), np.linalg.norm(a - b)
