@@ -59,6 +59,10 @@ def parse_args():
     ap.add_argument("--res", type=int, default=0,
                     help="keep only the views of this resolution (profiling a small case)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--coarse-level", type=int, default=3,
+                    help="paging: coarse fallback level (box filter 2**L; 0 = none)")
+    ap.add_argument("--max-uploads", type=int, default=0,
+                    help="paging: brick uploads per frame (0 = every missing brick)")
     ap.add_argument("--no-autotune", action="store_true",
                     help="use the default batch launch shape (profiling)")
     ap.add_argument("--cpu-sample-rows", type=int, default=0,
@@ -456,7 +460,9 @@ def main_paging(args):
     """Out-of-core configuration: 4096x4096x2048 u8 procedural value noise
     (3 octaves, 256-voxel cells, 15% occupancy) in 64^3 bricks held in a
     pinned host store; an 8 GiB device brick cache (realtime pager) renders a
-    120-frame orbit (azimuth +3 deg/frame) at 2048^2, density 5e-3."""
+    120-frame orbit (azimuth +3 deg/frame) at 2048^2, density 5e-3.  With
+    --coarse-level L the store's 2^L box-filtered level stays resident and
+    bricks not (yet) in the cache are drawn from it."""
     import numpy as np
     import torch
 
@@ -475,9 +481,13 @@ def main_paging(args):
     t0 = time.perf_counter()
     store = hy.Store.noise(ctx, dim, 64, 1, seed=2, cell_voxels=256.0 / sc, occupancy=0.15)
     t_store = time.perf_counter() - t0
+    t1 = time.perf_counter()
+    if args.coarse_level > 0:
+        store.build_coarse(args.coarse_level)
+    t_coarse = time.perf_counter() - t1
     si = store.info
     slots = int((8 * 2**30) // si.slot_bytes)
-    pg = hy.Pager(ctx, store, slots, _abi.PAGER_REALTIME)
+    pg = hy.Pager(ctx, store, slots, _abi.PAGER_REALTIME, args.max_uploads)
     p = hy.shader_params(shader="Volume", sample_rate=0.25, density=5e-3, count_samples=True)
     out = torch.empty(res * res * 4, dtype=torch.uint8, device=f"cuda:{local}")
     stream = torch.cuda.ExternalStream(ctx.stream)
@@ -490,12 +500,14 @@ def main_paging(args):
     clocks = Clocks(local)
     clocks.start()
     samples = 0
+    fallback = 0
     tw = time.perf_counter()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
     for f in range(frames):
         pg.render(p, hy.camera_orbit((3.0 * f, 30.0, 2.2)), res, res, out.data_ptr())
         samples += ctx.stats().samples
+        fallback += pg.stats()["fallback"]
     ev1.record(stream)
     ctx.synchronize()
     wall = time.perf_counter() - tw
@@ -511,7 +523,9 @@ def main_paging(args):
         "data": "synthetic",
         "config": {"workload": f"paging_{dim[0]}x{dim[1]}x{dim[2]}_{res}px", "block_size": 64,
                    "cache_gib": 8, "cache_slots": slots, "store_bricks": si.nonempty,
-                   "store_gb": si.pool_bytes / 1e9, "store_build_s": t_store},
+                   "store_gb": si.pool_bytes / 1e9, "store_build_s": t_store,
+                   "coarse_level": args.coarse_level, "coarse_build_s": t_coarse,
+                   "max_uploads_per_frame": args.max_uploads},
         "gsamples_per_s": samples / wall / 1e9,
         "samples_per_frame": samples / frames,
         "gpu_s": gpu_s, "wall_s": wall,
@@ -519,6 +533,7 @@ def main_paging(args):
         "uploads_per_frame": d["uploads"] / frames,
         "upload_gb_per_s": d["upload_bytes"] / wall / 1e9,
         "evictions": d["evictions"], "visible_last_frame": st["visible"],
+        "coarse_bricks_per_frame": fallback / frames,
         "clocks": ck,
     }
     print(json.dumps(outj), flush=True)

@@ -108,7 +108,7 @@ class HyPagerDesc(C.Structure):
 
 class HyPagerStats(C.Structure):
     _fields_ = [(n, C.c_int64) for n in ("frames", "passes", "uploads", "upload_bytes", "hits",
-                                         "misses", "evictions", "visible")]
+                                         "misses", "evictions", "visible", "fallback")]
 
 
 class HyDiffParams(C.Structure):
@@ -179,6 +179,9 @@ _PROTOS = {
     "hy_store_get_info": (C.c_int, [P, C.POINTER(HyVolumeInfo)]),
     "hy_store_thumbnails": (C.c_int, [P, P, P]),
     "hy_store_brick": (C.c_int, [P, C.c_int32, P]),
+    "hy_store_build_coarse": (C.c_int, [P, C.c_int32]),
+    "hy_store_coarse_grid": (C.c_int, [P, P]),
+    "hy_store_coarse_brick": (C.c_int, [P, C.c_int32, P]),
     "hy_cull": (C.c_int, [P, C.POINTER(HyView), P, C.c_int32, P, P, C.POINTER(C.c_int32)]),
     "hy_pager_create": (C.c_int, [P, P, C.POINTER(HyPagerDesc), C.POINTER(P)]),
     "hy_pager_destroy": (C.c_int, [P]),

@@ -387,6 +387,22 @@ class Store:
         self.ctx.check(lib().hy_store_brick(self.handle, b, _ptr(out)))
         return out.reshape(P, P, P)
 
+    def build_coarse(self, level: int) -> None:
+        """Coarse level (2**level box filter) for the realtime pager's fallback."""
+        self.ctx.check(lib().hy_store_build_coarse(self.handle, level))
+
+    @property
+    def coarse_grid(self):
+        g = (C.c_int32 * 3)()
+        self.ctx.check(lib().hy_store_coarse_grid(self.handle, g))
+        return (g[0], g[1], g[2])
+
+    def coarse_brick(self, b: int, dtype=np.uint8) -> np.ndarray:
+        P = self.info.padded
+        out = np.zeros(P ** 3, dtype)
+        self.ctx.check(lib().hy_store_coarse_brick(self.handle, b, _ptr(out)))
+        return out.reshape(P, P, P)
+
 
 class _PagedVolume:
     """Non-owning view of a pager's volume, usable wherever a Volume is."""

@@ -20,7 +20,9 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <atomic>
 #include <numeric>
+#include <thread>
 #include <vector>
 
 #include "hy_shade.cuh"
@@ -44,6 +46,11 @@ struct hy_store {
     unsigned char *host = nullptr;  // pinned
     size_t host_bytes = 0;
     int nonempty = 0;
+    // coarse level (0: none): every coarse brick, slot_stride apart
+    int coarse_level = 0;
+    int coarse_grid[3] = {0, 0, 0};
+    int ncoarse = 0;
+    std::vector<unsigned char> coarse;
 };
 
 namespace {
@@ -363,6 +370,121 @@ extern "C" int hy_store_create_noise(hy_ctx *ctx, const hy_volume_desc *desc, ui
     return HY_OK;
 }
 
+namespace {
+
+// fn(i) for i in [0, n) over the host's cores
+template <typename F>
+void parallel_for(int n, F fn) {
+    const int nt = std::max(1, std::min<int>(n, int(std::thread::hardware_concurrency())));
+    std::atomic<int> next{0};
+    std::vector<std::thread> ts;
+    for (int t = 0; t < nt; ++t)
+        ts.emplace_back([&]() {
+            for (int i = next++; i < n; i = next++) fn(i);
+        });
+    for (auto &t : ts) t.join();
+}
+
+// Coarse voxels of one fine brick: with bs a multiple of sc, the sc^3 cube of
+// every coarse voxel lies inside a single fine brick.
+template <typename T, typename Acc>
+void coarse_of_brick(const hy_store *s, int b, int sc, const int cdim[3], T *cvol) {
+    const int bs = s->desc.block_size, pad = s->desc.padding, P = s->P;
+    const int *dim = s->desc.dim;
+    const int bx = b % s->grid[0], by = (b / s->grid[0]) % s->grid[1],
+              bz = b / (s->grid[0] * s->grid[1]);
+    const T *src = reinterpret_cast<const T *>(s->host + s->offset[b]);
+    const int cpb = bs / sc;
+    for (int cz = 0; cz < cpb; ++cz)
+        for (int cy = 0; cy < cpb; ++cy)
+            for (int cx = 0; cx < cpb; ++cx) {
+                const int X = bx * cpb + cx, Y = by * cpb + cy, Z = bz * cpb + cz;
+                if (X >= cdim[0] || Y >= cdim[1] || Z >= cdim[2]) continue;
+                Acc sum = 0;
+                long long cnt = 0;
+                for (int z = Z * sc; z < std::min(Z * sc + sc, dim[2]); ++z)
+                    for (int y = Y * sc; y < std::min(Y * sc + sc, dim[1]); ++y)
+                        for (int x = X * sc; x < std::min(X * sc + sc, dim[0]); ++x) {
+                            const int lx = x - bx * bs + pad, ly = y - by * bs + pad,
+                                      lz = z - bz * bs + pad;
+                            sum += Acc(src[(size_t(lz) * P + ly) * P + lx]);
+                            ++cnt;
+                        }
+                T out;
+                if constexpr (sizeof(T) == 1)
+                    out = T((sum + Acc(cnt / 2)) / Acc(cnt));  // round half up
+                else
+                    out = T(double(sum) / double(cnt));
+                cvol[(size_t(Z) * cdim[1] + Y) * cdim[0] + X] = out;
+            }
+}
+
+template <typename T>
+void build_coarse(hy_store *s, int sc, const int cdim[3]) {
+    const size_t nc = size_t(cdim[0]) * cdim[1] * cdim[2];
+    std::vector<T> cvol(nc, T(0));  // empty fine bricks stay 0
+    parallel_for(s->nbricks, [&](int b) {
+        if (s->offset[b] < 0) return;
+        if constexpr (sizeof(T) == 1)
+            coarse_of_brick<T, unsigned long long>(s, b, sc, cdim, cvol.data());
+        else
+            coarse_of_brick<T, double>(s, b, sc, cdim, cvol.data());
+    });
+    // brick the coarse volume like the fine one: apron clamped at its border
+    const int bs = s->desc.block_size, pad = s->desc.padding, P = s->P;
+    const int *g = s->coarse_grid;
+    s->coarse.assign(size_t(s->ncoarse) * s->slot_stride, 0);
+    parallel_for(s->ncoarse, [&](int cb) {
+        const int bx = cb % g[0], by = (cb / g[0]) % g[1], bz = cb / (g[0] * g[1]);
+        T *dst = reinterpret_cast<T *>(s->coarse.data() + size_t(cb) * s->slot_stride);
+        for (int k = 0; k < P; ++k)
+            for (int j = 0; j < P; ++j)
+                for (int i = 0; i < P; ++i) {
+                    const int x = std::min(std::max(bx * bs + i - pad, 0), cdim[0] - 1);
+                    const int y = std::min(std::max(by * bs + j - pad, 0), cdim[1] - 1);
+                    const int z = std::min(std::max(bz * bs + k - pad, 0), cdim[2] - 1);
+                    dst[(size_t(k) * P + j) * P + i] = cvol[(size_t(z) * cdim[1] + y) * cdim[0] + x];
+                }
+    });
+}
+
+}  // namespace
+
+extern "C" int hy_store_build_coarse(hy_store *s, int32_t level) {
+    if (!s) return HY_ERR_INVALID;
+    hy_ctx *ctx = s->ctx;
+    const int bs = s->desc.block_size;
+    if (level < 1 || level > 12 || bs % (1 << level) != 0)
+        return hy_fail(ctx, HY_ERR_INVALID,
+                       "store: coarse level must be >= 1 with block_size a multiple of 2^level");
+    const int sc = 1 << level;
+    int cdim[3];
+    for (int i = 0; i < 3; ++i) {
+        cdim[i] = (s->desc.dim[i] + sc - 1) / sc;
+        s->coarse_grid[i] = (cdim[i] + bs - 1) / bs;
+    }
+    s->ncoarse = s->coarse_grid[0] * s->coarse_grid[1] * s->coarse_grid[2];
+    s->coarse_level = level;
+    if (s->desc.dtype == HY_DTYPE_U8)
+        build_coarse<unsigned char>(s, sc, cdim);
+    else
+        build_coarse<float>(s, sc, cdim);
+    return HY_OK;
+}
+
+extern "C" int hy_store_coarse_grid(const hy_store *s, int32_t grid[3]) {
+    if (!s || !grid) return HY_ERR_INVALID;
+    for (int i = 0; i < 3; ++i) grid[i] = s->coarse_grid[i];
+    return HY_OK;
+}
+
+extern "C" int hy_store_coarse_brick(const hy_store *s, int32_t brick, void *out) {
+    if (!s || !out || brick < 0 || brick >= s->ncoarse) return HY_ERR_INVALID;
+    const size_t bytes = size_t(s->P) * s->P * s->P * (s->desc.dtype == HY_DTYPE_U8 ? 1 : 4);
+    std::memcpy(out, s->coarse.data() + size_t(brick) * s->slot_stride, bytes);
+    return HY_OK;
+}
+
 extern "C" int hy_store_destroy(hy_store *s) {
     if (!s) return HY_OK;
     if (s->host) cudaFreeHost(s->host);
@@ -494,7 +616,8 @@ struct CullScratch {
 };
 
 int run_cull(hy_ctx *ctx, const hy_volume *vol, const hy_view &view, const float rect_in[4],
-             int limit, CullScratch &cs, std::vector<int> &ids, std::vector<float> &d2) {
+             int limit, CullScratch &cs, std::vector<int> &ids, std::vector<float> &d2,
+             std::vector<int> *all_visible = nullptr) {
     const float def_rect[4] = {-1.f, -1.f, 1.f, 1.f};
     const float *rect = rect_in ? rect_in : def_rect;
     if (cs.cap < vol->nbricks) {
@@ -531,6 +654,7 @@ int run_cull(hy_ctx *ctx, const hy_volume *vol, const hy_view &view, const float
                                      ctx->stream));
         HY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     }
+    if (all_visible) *all_visible = hid;
     std::vector<int> idx(n);
     std::iota(idx.begin(), idx.end(), 0);
     size_t keep = n;
@@ -590,6 +714,12 @@ struct hy_pager {
     cudaEvent_t staged[2] = {nullptr, nullptr};   // page-table copy out of each staging buffer
     std::vector<int> page;       // brick -> slot, -1 absent
     std::vector<int> owner;      // slot -> brick, -1 free
+    // realtime with the store's coarse level: the coarse bricks occupy the
+    // first `ncoarse` pool slots, registry ids [0, nbricks) sample them and
+    // cache slot i is registry id reg_base + i
+    bool coarse = false;
+    int ncoarse = 0;
+    int reg_base = 0;
     int next_free = 0;           // realtime: slots never used yet
     int2 *info_stage[2] = {nullptr, nullptr};  // pinned staging of the page table
     CullScratch cs;
@@ -618,7 +748,11 @@ int upload_page_table(hy_pager *pg, int buf = 0) {
     hy_volume *v = pg->vol;
     HY_CUDA(ctx, cudaEventSynchronize(pg->staged[buf]));
     int2 *st = pg->info_stage[buf];
-    for (int b = 0; b < v->nbricks; ++b) st[b] = make_int2(v->cheb[b], pg->page[b]);
+    for (int b = 0; b < v->nbricks; ++b) {
+        const int slot = pg->page[b];
+        const int id = slot >= 0 ? pg->reg_base + slot : (pg->coarse && v->cheb[b] == 0 ? b : -1);
+        st[b] = make_int2(v->cheb[b], id);
+    }
     HY_CUDA(ctx, cudaMemcpyAsync(v->info_dev, st, v->nbricks * sizeof(int2),
                                  cudaMemcpyHostToDevice, ctx->stream));
     HY_CUDA(ctx, cudaEventRecord(pg->staged[buf], ctx->stream));
@@ -631,7 +765,8 @@ int upload_bricks(hy_pager *pg, const int *bricks, const int *slots, int n) {
     for (int i = 0; i < n; ++i) {
         const long long off = pg->store->offset[bricks[i]];
         if (off < 0) return hy_fail(ctx, HY_ERR_INVALID, "pager: empty brick requested");
-        HY_CUDA(ctx, cudaMemcpyAsync(pg->vol->pool + size_t(slots[i]) * pg->vol->slot_stride,
+        HY_CUDA(ctx, cudaMemcpyAsync(pg->vol->pool +
+                                         size_t(pg->ncoarse + slots[i]) * pg->vol->slot_stride,
                                      pg->store->host + off, pg->store->slot_stride,
                                      cudaMemcpyHostToDevice, pg->copy));
     }
@@ -670,10 +805,14 @@ extern "C" int hy_pager_create(hy_ctx *ctx, hy_store *store, const hy_pager_desc
     v->nonempty = store->nonempty;
     v->resident = 0;
     v->reg_of_brick.assign(v->nbricks, -1);
-    v->pool_bytes = size_t(pg->nslots) * v->slot_stride;
+    pg->coarse = desc->mode == HY_PAGER_REALTIME && store->coarse_level > 0;
+    pg->ncoarse = pg->coarse ? store->ncoarse : 0;
+    pg->reg_base = pg->coarse ? v->nbricks : 0;
+    const int nreg = pg->reg_base + pg->nslots;
+    v->pool_bytes = size_t(pg->ncoarse + pg->nslots) * v->slot_stride;
     cudaError_t e = cudaMalloc(&v->pool, v->pool_bytes);
     if (e == cudaSuccess) e = cudaMalloc(&v->info_dev, v->nbricks * sizeof(int2));
-    if (e == cudaSuccess) e = cudaMalloc(&v->reg_dev, pg->nslots * sizeof(RegEntry));
+    if (e == cudaSuccess) e = cudaMalloc(&v->reg_dev, nreg * sizeof(RegEntry));
     if (e == cudaSuccess) e = cudaMalloc(&v->mean_dev, v->nbricks * sizeof(float));
     for (int i = 0; i < 2 && e == cudaSuccess; ++i) {
         e = cudaHostAlloc(reinterpret_cast<void **>(&pg->info_stage[i]), v->nbricks * sizeof(int2),
@@ -684,9 +823,31 @@ extern "C" int hy_pager_create(hy_ctx *ctx, hy_store *store, const hy_pager_desc
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&pg->copy, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&pg->copied, cudaEventDisableTiming);
     if (e != cudaSuccess) return fail(hy_cuda_fail(ctx, e, "pager: allocation"));
-    std::vector<RegEntry> reg(pg->nslots);
+    std::vector<RegEntry> reg(nreg);
+    if (pg->coarse) {
+        // LowestLevelBlock samplers (rt_block_paging.cc:141-188): fine brick
+        // b = base * s + d reads its sub-box of coarse brick `base`
+        const int sc = 1 << store->coarse_level;
+        const int P = v->P, bs = store->desc.block_size, pad = store->desc.padding;
+        const float kc = float(bs) / float(P) / float(sc);
+        const float b0 = float(pad) / float(P);
+        const int *cg = store->coarse_grid;
+        for (int b = 0; b < v->nbricks; ++b) {
+            const int x = b % v->grid[0], y = (b / v->grid[0]) % v->grid[1],
+                      z = b / (v->grid[0] * v->grid[1]);
+            const int cid = ((z / sc) * cg[1] + y / sc) * cg[0] + x / sc;
+            reg[b] = RegEntry{kc, b0 + float(x % sc) * kc, b0 + float(y % sc) * kc,
+                              b0 + float(z % sc) * kc, (long long)cid * (long long)v->slot_stride,
+                              {0, 0}};
+        }
+        e = cudaMemcpyAsync(v->pool, store->coarse.data(), store->coarse.size(),
+                            cudaMemcpyHostToDevice, ctx->stream);
+        if (e != cudaSuccess) return fail(hy_cuda_fail(ctx, e, "pager: coarse level upload"));
+    }
     for (int s = 0; s < pg->nslots; ++s)
-        reg[s] = RegEntry{v->k, v->b, v->b, v->b, (long long)s * (long long)v->slot_stride, {0, 0}};
+        reg[pg->reg_base + s] =
+            RegEntry{v->k, v->b, v->b, v->b,
+                     (long long)(pg->ncoarse + s) * (long long)v->slot_stride, {0, 0}};
     e = cudaMemcpyAsync(v->reg_dev, reg.data(), reg.size() * sizeof(RegEntry),
                         cudaMemcpyHostToDevice, ctx->stream);
     if (e == cudaSuccess)
@@ -854,9 +1015,9 @@ int render_realtime(hy_pager *pg, const hy_shader_params *p, const hy_view &view
                     uint8_t *rgba_dev) {
     hy_ctx *ctx = pg->ctx;
     hy_volume *v = pg->vol;
-    std::vector<int> req;
+    std::vector<int> req, visible;
     std::vector<float> d2;
-    int rc = run_cull(ctx, v, view, nullptr, pg->nslots, pg->cs, req, d2);
+    int rc = run_cull(ctx, v, view, nullptr, pg->nslots, pg->cs, req, d2, &visible);
     if (rc) return rc;
     std::vector<char> required(v->nbricks, 0);
     for (int b : req) required[b] = 1;
@@ -902,6 +1063,10 @@ int render_realtime(hy_pager *pg, const hy_shader_params *p, const hy_view &view
     for (int s = 0; s < pg->nslots; ++s) resident += pg->owner[s] >= 0;
     v->resident = resident;
     pg->stats.visible = int64_t(req.size());
+    int64_t fallback = 0;
+    if (pg->coarse)
+        for (int b : visible) fallback += pg->page[b] < 0;
+    pg->stats.fallback = fallback;
     ++pg->stats.passes;
     return hy_render_device(ctx, v, p, &view, W, H, rgba_dev, nullptr, nullptr);
 }
@@ -918,9 +1083,11 @@ extern "C" int hy_pager_render(hy_pager *pg, const hy_shader_params *p, const hy
     int rc = hy_camera_view(pg->vol, cam, &view);
     if (rc) return rc;
     ++pg->stats.frames;
+    hy_shader_params q = *p;
+    q.lowest_blkcnt = pg->reg_base;
     if (pg->desc.mode == HY_PAGER_LOSSLESS)
-        return render_lossless(pg, p, cam, view, W, H, rgba_dev);
-    return render_realtime(pg, p, view, W, H, rgba_dev);
+        return render_lossless(pg, &q, cam, view, W, H, rgba_dev);
+    return render_realtime(pg, &q, view, W, H, rgba_dev);
 }
 
 extern "C" int hy_pager_present(const hy_pager *pg, uint8_t *mask) {

@@ -247,6 +247,7 @@ typedef struct hy_pager_desc {
 
 typedef struct hy_pager_stats {
     int64_t frames, passes, uploads, upload_bytes, hits, misses, evictions, visible;
+    int64_t fallback;  /* realtime + coarse level: visible bricks drawn coarse, last frame */
 } hy_pager_stats;
 
 /* Store of a resident volume's bricks (copies its pool to pinned host memory). */
@@ -262,6 +263,17 @@ int hy_store_get_info(const hy_store *store, hy_volume_info *out);
 int hy_store_thumbnails(const hy_store *store, int32_t *chebyshev, float *mean);
 /* Copy one padded brick (P^3 voxels; zeros for an empty brick). */
 int hy_store_brick(const hy_store *store, int32_t brick, void *out);
+/* Coarse level of the store: the lowest sample level RtBlockPagingServer
+ * keeps resident (rt_block_paging.cc:119-196).  The volume box-filtered by
+ * s = 2^level per axis (a coarse voxel is the mean of the fine voxels of its
+ * s^3 cube that lie inside the volume; u8 rounds half up), bricked with the
+ * same block size and apron as the fine level, so one coarse brick covers
+ * s^3 fine bricks.  block_size must be a multiple of s.  Replaces an earlier
+ * coarse level. */
+int hy_store_build_coarse(hy_store *store, int32_t level);
+/* Coarse brick grid ({0,0,0} without a coarse level) and one coarse brick. */
+int hy_store_coarse_grid(const hy_store *store, int32_t grid[3]);
+int hy_store_coarse_brick(const hy_store *store, int32_t brick, void *out);
 
 /* OctreeCuller::cull (octree_culler.hpp:121-161) on the device: non-empty
  * bricks whose box meets the frustum, the nearest `limit` (< 0: all) by
@@ -278,7 +290,8 @@ int hy_pager_volume(hy_pager *pager, hy_volume **out);
 int hy_pager_stats_get(const hy_pager *pager, hy_pager_stats *out);
 /* Bricks resident after the last frame, one byte per brick. */
 int hy_pager_present(const hy_pager *pager, uint8_t *mask);
-/* One frame into a device RGBA8 image.
+/* One frame into a device RGBA8 image.  The pager sets params->lowest_blkcnt
+ * itself (the Paging mode's coarse / fine split).
  *  LOSSLESS: LosslessBlockPagingServer::start/next (lossless_block_paging.cc:
  *    116-174) + Volume/Isosurface/Blocks passes: visible bricks ordered by the
  *    distance of their centres to inverse(iet) * eye (as the reference
@@ -288,7 +301,13 @@ int hy_pager_present(const hy_pager *pager, uint8_t *mask);
  *  REALTIME: RtBlockPagingServer::update (rt_block_paging.cc:296-326): the
  *    nearest `slots` visible bricks are required; missing ones, nearest first,
  *    go to never-used slots and then to slots of bricks no longer required
- *    (highest index first); one emit pass renders with what is resident. */
+ *    (highest index first); one emit pass renders with what is resident.
+ *    With a coarse level in the store (created before the pager), the coarse
+ *    bricks stay resident and registry ids 0..nbricks-1 sample them, brick b
+ *    through its sub-box of the coarse brick (k = bs/P/s, b = pad/P + d*k,
+ *    rt_block_paging.cc:141-188); an absent brick's page entry is that id
+ *    instead of -1, so rays read the coarse level rather than stop, and cache
+ *    slot i is registry id nbricks + i (lowest_blkcnt = nbricks). */
 int hy_pager_render(hy_pager *pager, const hy_shader_params *params, const hy_camera *cam,
                     int32_t width, int32_t height, uint8_t *rgba_dev);
 

@@ -200,6 +200,16 @@ struct orc_volume {
     std::vector<float> bricks;  // nbricks * P^3, normalised like texture_3d.hpp:78-86
     std::vector<int> cheb;
     std::vector<int> vaddr;     // brick -> registry id or -1
+    // BlockSampler registry (block_paging.hpp:24-36): brick data + mapping
+    struct Entry {
+        const float *data;
+        float k, bx, by, bz;
+    };
+    std::vector<Entry> reg;
+    int lowest_blkcnt = 0;      // registry ids below this sample the coarse level
+    int coarse_level = 0;
+    int coarse_grid[3] = {0, 0, 0};
+    std::vector<float> coarse_bricks;
     std::vector<uint8_t> nonempty_mask;
     std::vector<float> mean;
     float k;                    // BlockSamplerMapping (lossless_block_paging.cc:21-22)
@@ -323,6 +333,9 @@ extern "C" orc_volume *orc_volume_create(const int32_t dim[3], int32_t block_siz
     // lossless_block_paging.cc:20-22: k = float(bs)/pad_bs; b = float(pad)/bs*k
     v->k = float(block_size) / float(v->P);
     v->b = float(padding) / float(block_size) * v->k;
+    const size_t P3 = size_t(v->P) * v->P * v->P;
+    v->reg.resize(v->nbricks);
+    for (int i = 0; i < v->nbricks; ++i) v->reg[i] = {&v->bricks[i * P3], v->k, v->b, v->b, v->b};
     // basic_renderer.hpp:104-118
     float blksz = float(block_size);
     v->bbox_max = f3(float(dim[0]) / blksz, float(dim[1]) / blksz, float(dim[2]) / blksz);
@@ -346,9 +359,99 @@ extern "C" void orc_volume_thumbnails(const orc_volume *v, int32_t *chebyshev, f
     }
 }
 
+// Absent bricks read the coarse level when there is one (the basic vaddr of
+// rt_block_paging.cc:212-218, restored on eviction at 262-264), else -1.
 extern "C" void orc_volume_set_present(orc_volume *v, const uint8_t *present) {
-    for (int i = 0; i < v->nbricks; ++i)
-        v->vaddr[i] = (v->nonempty_mask[i] && present[i]) ? i : -1;
+    for (int i = 0; i < v->nbricks; ++i) {
+        if (!v->nonempty_mask[i])
+            v->vaddr[i] = -1;
+        else if (present[i])
+            v->vaddr[i] = v->lowest_blkcnt + i;
+        else
+            v->vaddr[i] = v->coarse_level ? i : -1;
+    }
+}
+
+// The lowest sample level: the volume box-filtered by s = 2^level (mean of
+// the fine voxels of each s^3 cube inside the volume, u8 rounded half up),
+// bricked like the fine level; registry [0, nbricks) = one coarse sampler per
+// fine brick (k = bs/P/s, b = pad/P + d*k, rt_block_paging.cc:141-188),
+// [nbricks, 2*nbricks) = the fine bricks.
+extern "C" int orc_volume_build_coarse(orc_volume *v, int32_t level) {
+    if (level < 1 || level > 12 || v->bs % (1 << level) != 0) return -1;
+    const int sc = 1 << level, bs = v->bs, pad = v->pad, P = v->P;
+    const size_t P3 = size_t(P) * P * P;
+    int cdim[3];
+    for (int i = 0; i < 3; ++i) {
+        cdim[i] = (v->dim[i] + sc - 1) / sc;
+        v->coarse_grid[i] = (cdim[i] + bs - 1) / bs;
+    }
+    // fine voxel (x, y, z) is the core voxel of brick (x, y, z) / bs
+    auto fine = [&](int x, int y, int z) {
+        const int b = ((z / bs) * v->grid[1] + y / bs) * v->grid[0] + x / bs;
+        const int lx = x % bs + pad, ly = y % bs + pad, lz = z % bs + pad;
+        return v->bricks[b * P3 + (size_t(lz) * P + ly) * P + lx];
+    };
+    std::vector<float> cvol(size_t(cdim[0]) * cdim[1] * cdim[2]);
+    for (int Z = 0; Z < cdim[2]; ++Z)
+        for (int Y = 0; Y < cdim[1]; ++Y)
+            for (int X = 0; X < cdim[0]; ++X) {
+                long long isum = 0, cnt = 0;
+                double fsum = 0.0;
+                for (int z = Z * sc; z < std::min((Z + 1) * sc, v->dim[2]); ++z)
+                    for (int y = Y * sc; y < std::min((Y + 1) * sc, v->dim[1]); ++y)
+                        for (int x = X * sc; x < std::min((X + 1) * sc, v->dim[0]); ++x) {
+                            const float f = fine(x, y, z);
+                            if (v->dtype == 0)
+                                isum += (long long)(f * 255.f + 0.5f);  // u / 255.f -> u
+                            else
+                                fsum += double(f);
+                            ++cnt;
+                        }
+                float c;
+                if (v->dtype == 0)
+                    c = float(int((isum + cnt / 2) / cnt)) / 255.f;
+                else
+                    c = float(fsum / double(cnt));
+                cvol[(size_t(Z) * cdim[1] + Y) * cdim[0] + X] = c;
+            }
+    const int *g = v->coarse_grid;
+    const int ncoarse = g[0] * g[1] * g[2];
+    v->coarse_bricks.assign(size_t(ncoarse) * P3, 0.f);
+    for (int cb = 0; cb < ncoarse; ++cb) {
+        const int bx = cb % g[0], by = (cb / g[0]) % g[1], bz = cb / (g[0] * g[1]);
+        for (int k = 0; k < P; ++k)
+            for (int j = 0; j < P; ++j)
+                for (int i = 0; i < P; ++i) {
+                    const int x = iclamp(bx * bs + i - pad, 0, cdim[0] - 1);
+                    const int y = iclamp(by * bs + j - pad, 0, cdim[1] - 1);
+                    const int z = iclamp(bz * bs + k - pad, 0, cdim[2] - 1);
+                    v->coarse_bricks[cb * P3 + (size_t(k) * P + j) * P + i] =
+                        cvol[(size_t(z) * cdim[1] + y) * cdim[0] + x];
+                }
+    }
+    const float kc = float(bs) / float(P) / float(sc);
+    const float b0 = float(pad) / float(P);
+    v->reg.resize(2 * size_t(v->nbricks));
+    for (int b = 0; b < v->nbricks; ++b) {
+        const int x = b % v->grid[0], y = (b / v->grid[0]) % v->grid[1],
+                  z = b / (v->grid[0] * v->grid[1]);
+        const int cid = ((z / sc) * g[1] + y / sc) * g[0] + x / sc;
+        v->reg[b] = {&v->coarse_bricks[cid * P3], kc, b0 + float(x % sc) * kc,
+                     b0 + float(y % sc) * kc, b0 + float(z % sc) * kc};
+        v->reg[v->nbricks + b] = {&v->bricks[b * P3], v->k, v->b, v->b, v->b};
+    }
+    v->coarse_level = level;
+    v->lowest_blkcnt = v->nbricks;
+    for (int i = 0; i < v->nbricks; ++i) v->vaddr[i] = v->nonempty_mask[i] ? v->nbricks + i : -1;
+    return 0;
+}
+
+extern "C" int32_t orc_volume_lowest_blkcnt(const orc_volume *v) { return v->lowest_blkcnt; }
+
+extern "C" void orc_volume_coarse_brick(const orc_volume *v, int32_t brick, float *out) {
+    const size_t P3 = size_t(v->P) * v->P * v->P;
+    std::memcpy(out, &v->coarse_bricks[size_t(brick) * P3], P3 * sizeof(float));
 }
 
 extern "C" void orc_volume_brick(const orc_volume *v, int32_t brick, float *out) {
@@ -501,8 +604,9 @@ inline float lerp(float x, float y, float a) { return x * (1.f - a) + y * a; }  
 // (cpu_sampler.hpp:142-166, filter_linear 88-104).
 float sample_brick(const orc_volume *v, int pgid, F3 x) {
     const int P = v->P;
-    const float *data = &v->bricks[size_t(pgid) * size_t(P) * P * P];
-    F3 m = f3(v->k * x.x + v->b, v->k * x.y + v->b, v->k * x.z + v->b);
+    const orc_volume::Entry &e = v->reg[pgid];
+    const float *data = e.data;
+    F3 m = f3(e.k * x.x + e.bx, e.k * x.y + e.by, e.k * x.z + e.bz);
     float fd = float(P);
     F3 fx = f3(fd * m.x, fd * m.y, fd * m.z);
     // glm mod(x, y) = x - y * floor(x / y)

@@ -59,6 +59,12 @@ void orc_volume_thumbnails(const orc_volume *v, int32_t *chebyshev, float *mean)
 void orc_volume_set_present(orc_volume *v, const uint8_t *present_mask);
 /* Normalised float contents of one padded brick (P^3 floats). */
 void orc_volume_brick(const orc_volume *v, int32_t brick, float *out);
+/* Coarse (lowest) sample level for the realtime paging fallback; afterwards
+ * absent bricks sample it and fine bricks are registry ids >= lowest_blkcnt.
+ * Returns 0, or -1 when block_size is not a multiple of 2^level. */
+int orc_volume_build_coarse(orc_volume *v, int32_t level);
+int32_t orc_volume_lowest_blkcnt(const orc_volume *v);
+void orc_volume_coarse_brick(const orc_volume *v, int32_t brick, float *out);
 
 /* camera: out[0..2] position, [3..5] target, [6..8] up, [9] ctg_fovy_2 */
 void orc_camera_orbit(const float arm[3], const float center[3], float fovy_deg, float out[10]);

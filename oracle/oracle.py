@@ -58,6 +58,9 @@ def lib() -> C.CDLL:
             "orc_volume_thumbnails": (None, [P, P, P]),
             "orc_volume_set_present": (None, [P, P]),
             "orc_volume_brick": (None, [P, C.c_int32, P]),
+            "orc_volume_build_coarse": (C.c_int, [P, C.c_int32]),
+            "orc_volume_lowest_blkcnt": (C.c_int32, [P]),
+            "orc_volume_coarse_brick": (None, [P, C.c_int32, P]),
             "orc_camera_orbit": (None, [P, P, C.c_float, P]),
             "orc_camera_ptu": (None, [P, P, P, C.c_float, P]),
             "orc_camera_view": (None, [P, P, P]),
@@ -129,6 +132,22 @@ class OracleVolume:
     def set_present(self, mask: np.ndarray) -> None:
         m = np.ascontiguousarray(mask.astype(np.uint8).ravel())
         lib().orc_volume_set_present(self.h, _p(m))
+
+    def build_coarse(self, level: int) -> None:
+        """Coarse sample level: absent bricks then sample it (realtime paging)."""
+        if lib().orc_volume_build_coarse(self.h, level) != 0:
+            raise ValueError("block_size must be a multiple of 2**level")
+        self.coarse_level = level
+
+    @property
+    def lowest_blkcnt(self) -> int:
+        return int(lib().orc_volume_lowest_blkcnt(self.h))
+
+    def coarse_brick(self, i: int) -> np.ndarray:
+        P_ = self.block_size + 2 * self.padding
+        out = np.zeros(P_ ** 3, np.float32)
+        lib().orc_volume_coarse_brick(self.h, i, _p(out))
+        return out.reshape(P_, P_, P_)
 
 
 def camera_orbit(arm, center=(0.0, 0.0, 0.0), fovy=60.0) -> np.ndarray:

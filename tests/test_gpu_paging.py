@@ -186,3 +186,65 @@ def test_noise_store(ctx):
         assert 0.08 < float(np.mean(occ)) < 0.25
     finally:
         store.close()
+
+
+@pytest.fixture(scope="module")
+def tubes_coarse(ctx):
+    # 130^3 with 16^3 bricks: a ragged last brick; level 2 -> 33^3 coarse voxels,
+    # 3^3 coarse bricks, each covering 4^3 fine bricks
+    vox = hy.synth_tubes_u8(3, (130, 130, 130), 14)
+    vol = hy.Volume(ctx, vox, 16, 1)
+    ov = orc.OracleVolume(vox, 16, 1)
+    ov.build_coarse(2)
+    store = hy.Store.from_volume(vol)
+    store.build_coarse(2)
+    yield vol, ov, store
+    store.close()
+    vol.close()
+
+
+def test_coarse_level_matches_oracle(tubes_coarse):
+    _, ov, store = tubes_coarse
+    g = store.coarse_grid
+    assert g == (3, 3, 3)
+    for cb in range(g[0] * g[1] * g[2]):
+        got = store.coarse_brick(cb).astype(np.float32) / np.float32(255)
+        np.testing.assert_array_equal(got, ov.coarse_brick(cb), err_msg=f"coarse brick {cb}")
+    assert ov.lowest_blkcnt == 9 ** 3
+
+
+@pytest.mark.parametrize("mode", ["Default", "Paging"])
+def test_realtime_coarse_fallback_matches_oracle(ctx, tubes_coarse, mode):
+    """Absent bricks sample the coarse level instead of stopping the ray; the
+    Paging mode colours coarse samples red and fine ones green."""
+    torch = pytest.importorskip("torch")
+    vol, ov, store = tubes_coarse
+    ctx.set_transfer_fn(wl.TF9)
+    pg = hy.Pager(ctx, store, 30, _abi.PAGER_REALTIME, 8)
+    try:
+        W, H = 64, 48
+        nb = ov.grid[0] * ov.grid[1] * ov.grid[2]
+        saw_fallback = False
+        for f in range(5):
+            c = wl.make_camera(wl.Camera("orbit", (20 + 30 * f, 35, 2.2)))
+            p = hy.shader_params(shader="Volume", mode=mode, density=0.4, sample_rate=0.5,
+                                 count_samples=True)
+            out = torch.zeros(W * H * 4, dtype=torch.uint8, device="cuda")
+            pg.render(p, c, W, H, out.data_ptr())
+            ctx.synchronize()
+            st = pg.stats()
+            saw_fallback |= st["fallback"] > 0
+            ov.set_present(pg.present())
+            op = orc.params_from(p)
+            op.lowest_blkcnt = ov.lowest_blkcnt
+            view = view_array(hy.camera_view(vol, c))
+            ref = orc.render(ov, wl.TF9, op, view, W, H)
+            got = out.cpu().numpy().reshape(H, W, 4)
+            d = np.abs(got.astype(int) - ref["rgba"].astype(int))
+            assert d.max() <= 1, f"frame {f}: {d.max()} LSB"
+            if mode == "Paging" and st["fallback"] > 0:
+                assert (got[..., 0] > 0).any() and (got[..., 1] > 0).any()
+        assert saw_fallback
+    finally:
+        ov.set_present(np.ones(nb, np.uint8))
+        pg.close()

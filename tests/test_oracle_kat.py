@@ -264,3 +264,51 @@ def test_fp64_gradient_matches_central_differences():
         fd = (loss(vp.reshape(vol.shape), tf) - loss(vm.reshape(vol.shape), tf)) / (2 * eps)
         g = dv.ravel()[f]
         assert abs(fd - g) <= 1e-3 * max(abs(fd), 1e-2 * np.abs(dv).max()), (f, fd, g)
+
+
+@pytest.mark.parametrize("dims,bs,level", [((16, 16, 16), 8, 1), ((21, 18, 13), 8, 2),
+                                          ((33, 17, 9), 4, 2)])
+def test_coarse_level_is_rounded_box_mean(dims, bs, level):
+    rng = np.random.default_rng(7)
+    vox = rng.integers(0, 256, dims[::-1]).astype(np.uint8)
+    ov = orc.OracleVolume(vox, bs, 1)
+    ov.build_coarse(level)
+    s = 1 << level
+    cd = [-(-d // s) for d in dims]  # x, y, z
+    ref = np.zeros(cd[::-1], np.int64)
+    for Z in range(cd[2]):
+        for Y in range(cd[1]):
+            for X in range(cd[0]):
+                blk = vox[Z * s:(Z + 1) * s, Y * s:(Y + 1) * s, X * s:(X + 1) * s].astype(np.int64)
+                ref[Z, Y, X] = (blk.sum() + blk.size // 2) // blk.size
+    cg = [-(-c // bs) for c in cd]
+    P = bs + 2
+    for cb in range(cg[0] * cg[1] * cg[2]):
+        bx, by, bz = cb % cg[0], (cb // cg[0]) % cg[1], cb // (cg[0] * cg[1])
+        idx = [np.clip(np.arange(P) + b * bs - 1, 0, c - 1) for b, c in zip((bx, by, bz), cd)]
+        want = ref[np.ix_(idx[2], idx[1], idx[0])].astype(np.float32) / F(255)
+        np.testing.assert_array_equal(ov.coarse_brick(cb), want)
+    assert ov.lowest_blkcnt == ov.grid[0] * ov.grid[1] * ov.grid[2]
+
+
+def test_coarse_fallback_of_constant_volume_equals_fine_render():
+    # trilinear filtering of a constant is that constant at either level (up
+    # to the rounding of x*(1-a) + x*a), so a frame with every brick absent
+    # renders what the fine level does, with the same samples
+    vox = np.full((32, 32, 32), 200, np.uint8)
+    ov = orc.OracleVolume(vox, 8, 1)
+    view = orc.camera_view(ov, orc.camera_orbit((30, 40, 2.2)))
+    p = params(sample_rate=0.5, density=0.3)
+    fine = orc.render(ov, TF9, p, view, 24, 24)
+    ov.build_coarse(2)
+    nb = ov.grid[0] * ov.grid[1] * ov.grid[2]
+    ov.set_present(np.zeros(nb, np.uint8))
+    p.lowest_blkcnt = ov.lowest_blkcnt
+    coarse = orc.render(ov, TF9, p, view, 24, 24)
+    assert coarse["samples"] == fine["samples"] > 0
+    np.testing.assert_allclose(coarse["v"], fine["v"], rtol=0, atol=1e-6)
+    # Paging mode: all samples from the coarse level are red
+    p.mode = 2
+    red = orc.render(ov, TF9, p, view, 24, 24)["v"]
+    hit = red[..., 3] > 0
+    assert hit.any() and not red[..., 1][hit].any() and (red[..., 0][hit] > 0).all()
