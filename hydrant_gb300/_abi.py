@@ -182,12 +182,17 @@ _PROTOS = {
     "hy_store_build_coarse": (C.c_int, [P, C.c_int32]),
     "hy_store_coarse_grid": (C.c_int, [P, P]),
     "hy_store_coarse_brick": (C.c_int, [P, C.c_int32, P]),
+    "hy_store_save": (C.c_int, [P, C.c_char_p]),
+    "hy_store_open": (C.c_int, [P, C.c_char_p, C.POINTER(P)]),
+    "hy_store_ingest_raw": (C.c_int, [P, C.c_char_p, C.POINTER(HyVolumeDesc), C.POINTER(P)]),
     "hy_cull": (C.c_int, [P, C.POINTER(HyView), P, C.c_int32, P, P, C.POINTER(C.c_int32)]),
     "hy_pager_create": (C.c_int, [P, P, C.POINTER(HyPagerDesc), C.POINTER(P)]),
     "hy_pager_destroy": (C.c_int, [P]),
     "hy_pager_volume": (C.c_int, [P, C.POINTER(P)]),
     "hy_pager_stats_get": (C.c_int, [P, C.POINTER(HyPagerStats)]),
     "hy_pager_present": (C.c_int, [P, P]),
+    "hy_pager_render_host": (
+        C.c_int, [P, C.POINTER(HyShaderParams), C.POINTER(HyCamera), C.c_int32, C.c_int32, P]),
     "hy_pager_render": (
         C.c_int, [P, C.POINTER(HyShaderParams), C.POINTER(HyCamera), C.c_int32, C.c_int32, P]),
     "hy_diff_ckpt_bytes": (

@@ -363,6 +363,26 @@ class Store:
                                               occupancy, C.byref(h)))
         return cls(ctx, h)
 
+    @classmethod
+    def open(cls, ctx: Context, path) -> "Store":
+        """Read a dataset directory written by save() (package_meta.json + bricks)."""
+        h = C.c_void_p()
+        ctx.check(lib().hy_store_open(ctx.handle, str(path).encode(), C.byref(h)))
+        return cls(ctx, h)
+
+    @classmethod
+    def ingest_raw(cls, ctx: Context, path, dim, block_size: int, padding: int = 1,
+                   dtype: int = _abi.DTYPE_U8) -> "Store":
+        """Brick a raw volume file (x fastest) on the host."""
+        desc = HyVolumeDesc(tuple(dim), block_size, padding, dtype)
+        h = C.c_void_p()
+        ctx.check(lib().hy_store_ingest_raw(ctx.handle, str(path).encode(), C.byref(desc),
+                                            C.byref(h)))
+        return cls(ctx, h)
+
+    def save(self, path) -> None:
+        self.ctx.check(lib().hy_store_save(self.handle, str(path).encode()))
+
     def close(self) -> None:
         if self.handle:
             lib().hy_store_destroy(self.handle)

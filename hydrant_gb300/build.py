@@ -20,7 +20,8 @@ CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libhydrant_gb300.so"
 
-SOURCES = ["hy_api.cc", "hy_volume.cu", "hy_render.cu", "hy_batch.cu", "hy_page.cu", "hy_diff.cu", "hy_synth.cc"]
+SOURCES = ["hy_api.cc", "hy_volume.cu", "hy_render.cu", "hy_batch.cu", "hy_page.cu", "hy_diff.cu",
+           "hy_synth.cc", "hy_store_io.cc"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_COMMON = [
@@ -61,7 +62,7 @@ def _stale(sources: list[Path], target: Path) -> bool:
         return True
     t = target.stat().st_mtime
     deps = list(sources) + list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh"))
-    deps += [PKG.parent / "include" / "hydrant_gb300.h", Path(__file__)]
+    deps += list((PKG.parent / "include").glob("*.h*")) + [Path(__file__)]
     return any(p.exists() and p.stat().st_mtime > t for p in deps)
 
 

@@ -120,7 +120,36 @@ struct hy_volume {
     bool paged = false;       // pool is a brick cache owned by a hy_pager
 };
 
+// Brick store: every non-empty padded brick in pinned host memory, laid out
+// like device slots (slot_stride apart), plus the thumbnails.
+struct hy_store {
+    hy_ctx *ctx = nullptr;
+    hy_volume_desc desc{};
+    int grid[3] = {0, 0, 0};
+    int nbricks = 0;
+    int P = 0;
+    size_t slot_stride = 0;
+    std::vector<int> cheb;
+    std::vector<float> mean;
+    std::vector<long long> offset;  // brick -> byte offset in `host`, -1 if empty
+    unsigned char *host = nullptr;  // pinned
+    size_t host_bytes = 0;
+    int nonempty = 0;
+    // coarse level (0: none): every coarse brick, slot_stride apart
+    int coarse_level = 0;
+    int coarse_grid[3] = {0, 0, 0};
+    int ncoarse = 0;
+    std::vector<unsigned char> coarse;
+};
+
 int hy_volume_init(hy_ctx *ctx, const hy_volume_desc *desc, hy_volume *v);
+// store helpers (hy_page.cu): grid / padded edge / slot stride from a
+// descriptor, and the pinned allocation for `nonempty` bricks
+void hy_store_geometry(hy_store *s, const hy_volume_desc &d);
+int hy_store_alloc(hy_store *s, int nonempty);
+// Chebyshev distance over the brick grid (hy_page.cu)
+void hy_chebyshev_transform(const std::vector<unsigned char> &nonempty, const int grid[3],
+                            std::vector<int> &out);
 
 // error helpers (hy_api.cc)
 int hy_fail(hy_ctx *ctx, int code, const std::string &msg);

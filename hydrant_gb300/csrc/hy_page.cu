@@ -33,35 +33,48 @@ using namespace hy::dev;
 // ---------------------------------------------------------------------------
 // Brick store
 // ---------------------------------------------------------------------------
-struct hy_store {
-    hy_ctx *ctx = nullptr;
-    hy_volume_desc desc{};
-    int grid[3] = {0, 0, 0};
-    int nbricks = 0;
-    int P = 0;
-    size_t slot_stride = 0;
-    std::vector<int> cheb;
-    std::vector<float> mean;
-    std::vector<long long> offset;  // brick -> byte offset in `host`, -1 if empty
-    unsigned char *host = nullptr;  // pinned
-    size_t host_bytes = 0;
-    int nonempty = 0;
-    // coarse level (0: none): every coarse brick, slot_stride apart
-    int coarse_level = 0;
-    int coarse_grid[3] = {0, 0, 0};
-    int ncoarse = 0;
-    std::vector<unsigned char> coarse;
-};
 
-namespace {
+// Chebyshev distance transform over the brick grid (26-neighbour dilation).
+void hy_chebyshev_transform(const std::vector<unsigned char> &ne, const int g[3],
+                            std::vector<int> &out) {
+    const int n = g[0] * g[1] * g[2];
+    const int cap = std::max(g[0], std::max(g[1], g[2]));
+    out.assign(n, -1);
+    std::vector<int> frontier;
+    for (int i = 0; i < n; ++i)
+        if (ne[i]) {
+            out[i] = 0;
+            frontier.push_back(i);
+        }
+    for (int r = 1; r <= cap && !frontier.empty(); ++r) {
+        std::vector<int> next;
+        for (int id : frontier) {
+            const int x = id % g[0], y = (id / g[0]) % g[1], z = id / (g[0] * g[1]);
+            for (int k = 0; k < 27; ++k) {
+                const int X = x + k % 3 - 1, Y = y + (k / 3) % 3 - 1, Z = z + k / 9 - 1;
+                if (X < 0 || Y < 0 || Z < 0 || X >= g[0] || Y >= g[1] || Z >= g[2]) continue;
+                const int j = (Z * g[1] + Y) * g[0] + X;
+                if (out[j] < 0) {
+                    out[j] = r;
+                    next.push_back(j);
+                }
+            }
+        }
+        frontier.swap(next);
+    }
+    for (int i = 0; i < n; ++i)
+        if (out[i] < 0) out[i] = cap;
+}
 
-int store_alloc(hy_store *s, int nonempty) {
+int hy_store_alloc(hy_store *s, int nonempty) {
     s->nonempty = nonempty;
     s->host_bytes = std::max<size_t>(1, size_t(nonempty)) * s->slot_stride;
     HY_CUDA(s->ctx, cudaHostAlloc(reinterpret_cast<void **>(&s->host), s->host_bytes,
                                   cudaHostAllocDefault));
     return HY_OK;
 }
+
+namespace {
 
 // ---- procedural value noise (the 32 GiB paging workload) --------------------
 
@@ -186,38 +199,11 @@ __global__ void noise_brick_kernel(const __grid_constant__ NoiseChunk a) {
     }
 }
 
-// Chebyshev distance transform over the brick grid (26-neighbour dilation).
-void cheb_transform(const std::vector<unsigned char> &ne, const int g[3], std::vector<int> &out) {
-    const int n = g[0] * g[1] * g[2];
-    const int cap = std::max(g[0], std::max(g[1], g[2]));
-    out.assign(n, -1);
-    std::vector<int> frontier;
-    for (int i = 0; i < n; ++i)
-        if (ne[i]) {
-            out[i] = 0;
-            frontier.push_back(i);
-        }
-    for (int r = 1; r <= cap && !frontier.empty(); ++r) {
-        std::vector<int> next;
-        for (int id : frontier) {
-            const int x = id % g[0], y = (id / g[0]) % g[1], z = id / (g[0] * g[1]);
-            for (int k = 0; k < 27; ++k) {
-                const int X = x + k % 3 - 1, Y = y + (k / 3) % 3 - 1, Z = z + k / 9 - 1;
-                if (X < 0 || Y < 0 || Z < 0 || X >= g[0] || Y >= g[1] || Z >= g[2]) continue;
-                const int j = (Z * g[1] + Y) * g[0] + X;
-                if (out[j] < 0) {
-                    out[j] = r;
-                    next.push_back(j);
-                }
-            }
-        }
-        frontier.swap(next);
-    }
-    for (int i = 0; i < n; ++i)
-        if (out[i] < 0) out[i] = cap;
-}
 
-void store_geometry(hy_store *s, const hy_volume_desc &d) {
+
+}  // namespace
+
+void hy_store_geometry(hy_store *s, const hy_volume_desc &d) {
     s->desc = d;
     for (int i = 0; i < 3; ++i) s->grid[i] = (d.dim[i] + d.block_size - 1) / d.block_size;
     s->nbricks = s->grid[0] * s->grid[1] * s->grid[2];
@@ -225,8 +211,6 @@ void store_geometry(hy_store *s, const hy_volume_desc &d) {
     const size_t elem = d.dtype == HY_DTYPE_U8 ? 1 : 4;
     s->slot_stride = (size_t(s->P) * s->P * s->P * elem + 255) / 256 * 256;
 }
-
-}  // namespace
 
 extern "C" int hy_store_from_volume(const hy_volume *vol, hy_store **out) {
     if (!vol || !out) return HY_ERR_INVALID;
@@ -236,11 +220,11 @@ extern "C" int hy_store_from_volume(const hy_volume *vol, hy_store **out) {
         return hy_fail(ctx, HY_ERR_STATE, "store: needs a resident, uploaded volume");
     hy_store *s = new hy_store();
     s->ctx = ctx;
-    store_geometry(s, vol->desc);
+    hy_store_geometry(s, vol->desc);
     s->cheb = vol->cheb;
     s->mean = vol->mean;
     s->offset.assign(s->nbricks, -1);
-    int rc = store_alloc(s, vol->resident);
+    int rc = hy_store_alloc(s, vol->resident);
     if (rc) {
         delete s;
         return rc;
@@ -271,7 +255,7 @@ extern "C" int hy_store_create_noise(hy_ctx *ctx, const hy_volume_desc *desc, ui
     HY_CUDA(ctx, cudaSetDevice(ctx->device));
     hy_store *s = new hy_store();
     s->ctx = ctx;
-    store_geometry(s, *desc);
+    hy_store_geometry(s, *desc);
     const unsigned int sd = unsigned(seed ^ (seed >> 32));
     const float inv_cell = 1.f / cell_voxels;
     // occupancy threshold: the (1 - occupancy) quantile of 2^22 sampled voxels
@@ -326,7 +310,7 @@ extern "C" int hy_store_create_noise(hy_ctx *ctx, const hy_volume_desc *desc, ui
         if (e != cudaSuccess) return fail(e, "noise store: emptiness pass");
         for (int i = 0; i < n; ++i) ne[b0 + i] = nb[i] ? 1 : 0;
     }
-    cheb_transform(ne, s->grid, s->cheb);
+    hy_chebyshev_transform(ne, s->grid, s->cheb);
     const double ncore = double(desc->block_size) * desc->block_size * desc->block_size;
     s->mean.resize(s->nbricks);
     s->offset.assign(s->nbricks, -1);
@@ -335,7 +319,7 @@ extern "C" int hy_store_create_noise(hy_ctx *ctx, const hy_volume_desc *desc, ui
         s->mean[b] = float(double(sums[b]) / 255.0 / ncore);
         if (ne[b]) s->offset[b] = (long long)(nonempty++) * s->slot_stride;
     }
-    rc = store_alloc(s, nonempty);
+    rc = hy_store_alloc(s, nonempty);
     if (rc) {
         cudaFree(samp);
         cudaFree(chunk);
@@ -1088,6 +1072,22 @@ extern "C" int hy_pager_render(hy_pager *pg, const hy_shader_params *p, const hy
     if (pg->desc.mode == HY_PAGER_LOSSLESS)
         return render_lossless(pg, &q, cam, view, W, H, rgba_dev);
     return render_realtime(pg, &q, view, W, H, rgba_dev);
+}
+
+extern "C" int hy_pager_render_host(hy_pager *pg, const hy_shader_params *p, const hy_camera *cam,
+                                    int32_t W, int32_t H, uint8_t *rgba_host) {
+    if (!pg || !p || !cam || !rgba_host || W <= 0 || H <= 0) return HY_ERR_INVALID;
+    hy_ctx *ctx = pg->ctx;
+    HY_CUDA(ctx, cudaSetDevice(ctx->device));
+    void *dev = nullptr;
+    const size_t bytes = size_t(W) * H * 4;
+    int rc = hy_stage(ctx, bytes, &dev);
+    if (rc) return rc;
+    rc = hy_pager_render(pg, p, cam, W, H, static_cast<uint8_t *>(dev));
+    if (rc) return rc;
+    HY_CUDA(ctx, cudaMemcpyAsync(rgba_host, dev, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    HY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return HY_OK;
 }
 
 extern "C" int hy_pager_present(const hy_pager *pg, uint8_t *mask) {

@@ -275,6 +275,22 @@ int hy_store_build_coarse(hy_store *store, int32_t level);
 int hy_store_coarse_grid(const hy_store *store, int32_t grid[3]);
 int hy_store_coarse_brick(const hy_store *store, int32_t brick, void *out);
 
+/* On-disk dataset (replaces the varch archive set of build_dataset.sh:77-126
+ * that RendererFactory reads, renderer.hpp:53-59): a directory holding
+ * package_meta.json ("sample_levels" with the level-0 bricks, chebyshev and
+ * mean thumbnails, and the coarse level if built) and uncompressed bricks.
+ * hy_store_save writes one (creating the directory), hy_store_open reads it
+ * into a pinned store. */
+int hy_store_save(const hy_store *store, const char *dir);
+int hy_store_open(hy_ctx *ctx, const char *dir, hy_store **out);
+/* Ingest a raw volume file (x fastest, desc->dtype, exactly dim product
+ * voxels) on the host: bricks with a border-clamped apron, emptiness,
+ * chebyshev and mean thumbnails as for hy_volume_upload, in slabs of
+ * block_size (+ apron) z-slices, so the volume never has to fit on the
+ * device. */
+int hy_store_ingest_raw(hy_ctx *ctx, const char *raw_path, const hy_volume_desc *desc,
+                        hy_store **out);
+
 /* OctreeCuller::cull (octree_culler.hpp:121-161) on the device: non-empty
  * bricks whose box meets the frustum, the nearest `limit` (< 0: all) by
  * squared distance of the brick centre to the eye (ties by index), returned in
@@ -310,6 +326,9 @@ int hy_pager_present(const hy_pager *pager, uint8_t *mask);
  *    slot i is registry id nbricks + i (lowest_blkcnt = nbricks). */
 int hy_pager_render(hy_pager *pager, const hy_shader_params *params, const hy_camera *cam,
                     int32_t width, int32_t height, uint8_t *rgba_dev);
+/* Same into a host image; returns when it is there. */
+int hy_pager_render_host(hy_pager *pager, const hy_shader_params *params, const hy_camera *cam,
+                         int32_t width, int32_t height, uint8_t *rgba_host);
 
 /* ---- differentiable rendering (transfer function and voxel gradients) -------
  * No counterpart in the reference (its shaders have no derivatives).  The

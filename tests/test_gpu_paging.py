@@ -248,3 +248,83 @@ def test_realtime_coarse_fallback_matches_oracle(ctx, tubes_coarse, mode):
     finally:
         ov.set_present(np.ones(nb, np.uint8))
         pg.close()
+
+
+def test_store_save_open_round_trip(ctx, tubes_coarse, tmp_path):
+    torch = pytest.importorskip("torch")
+    vol, ov, store = tubes_coarse
+    store.save(tmp_path / "ds")
+    meta = (tmp_path / "ds" / "package_meta.json").read_text()
+    assert '"sample_levels"' in meta and '"chebyshev"' in meta
+    again = hy.Store.open(ctx, tmp_path / "ds")
+    try:
+        a, b = store.info, again.info
+        assert tuple(a.grid) == tuple(b.grid) and a.nonempty == b.nonempty
+        ca, ma = store.thumbnails()
+        cb, mb = again.thumbnails()
+        assert np.array_equal(ca, cb) and np.array_equal(ma, mb)
+        for i in range(a.nbricks):
+            assert np.array_equal(store.brick(i), again.brick(i))
+        assert again.coarse_grid == store.coarse_grid
+        for i in range(int(np.prod(store.coarse_grid))):
+            assert np.array_equal(store.coarse_brick(i), again.coarse_brick(i))
+        # the same frames from either store
+        ctx.set_transfer_fn(wl.TF9)
+        imgs = []
+        for st in (store, again):
+            pg = hy.Pager(ctx, st, 30, _abi.PAGER_REALTIME, 8)
+            out = torch.zeros(48 * 40 * 4, dtype=torch.uint8, device="cuda")
+            p = hy.shader_params(shader="Volume", density=0.4, sample_rate=0.5)
+            pg.render(p, wl.make_camera(wl.Camera("orbit", (30, 30, 2.2))), 48, 40, out.data_ptr())
+            ctx.synchronize()
+            imgs.append(out.cpu().numpy())
+            pg.close()
+        assert np.array_equal(imgs[0], imgs[1])
+    finally:
+        again.close()
+
+
+def test_store_open_rejects_damaged_dataset(ctx, tubes, tmp_path):
+    _, _, store = tubes
+    store.save(tmp_path / "ds")
+    bricks = tmp_path / "ds" / "level0.bricks"
+    data = bricks.read_bytes()
+    bricks.write_bytes(data[:-1])
+    with pytest.raises(hy.HydrantError):
+        hy.Store.open(ctx, tmp_path / "ds")
+    (tmp_path / "ds" / "package_meta.json").write_text('{"format": "something-else"}')
+    with pytest.raises(hy.HydrantError):
+        hy.Store.open(ctx, tmp_path / "ds")
+
+
+@pytest.mark.parametrize("dtype", ["u8", "f32"])
+def test_ingest_raw_equals_device_bricking(ctx, tmp_path, dtype):
+    if dtype == "u8":
+        vox = hy.synth_tubes_u8(5, (70, 45, 38), 9)
+    else:
+        vox = hy.synth_blobs_f32(6, (70, 45, 38), 8)
+        vox[vox < 0.2] = 0.0  # some empty bricks
+    raw = tmp_path / "vol.raw"
+    vox.tofile(raw)
+    vol = hy.Volume(ctx, vox, 16, 1)
+    ref = hy.Store.from_volume(vol)
+    got = hy.Store.ingest_raw(ctx, raw, (70, 45, 38), 16, 1,
+                              _abi.DTYPE_U8 if dtype == "u8" else _abi.DTYPE_F32)
+    try:
+        assert got.info.nonempty == ref.info.nonempty > 0
+        c0, m0 = ref.thumbnails()
+        c1, m1 = got.thumbnails()
+        assert np.array_equal(c0, c1)
+        if dtype == "u8":
+            assert np.array_equal(m0, m1)
+        else:
+            np.testing.assert_allclose(m1, m0, rtol=1e-6, atol=1e-7)
+        npd = np.uint8 if dtype == "u8" else np.float32
+        for b in range(got.info.nbricks):
+            assert np.array_equal(ref.brick(b, npd), got.brick(b, npd)), f"brick {b}"
+    finally:
+        got.close()
+        ref.close()
+        vol.close()
+    with pytest.raises(hy.HydrantError):
+        hy.Store.ingest_raw(ctx, raw, (70, 45, 39), 16, 1)
