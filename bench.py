@@ -91,6 +91,26 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(values, device="cpu"):
+    """Element-wise maximum of a list of floats over all ranks (the job's
+    time is its slowest rank's); the values themselves at one rank."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return [float(v) for v in values]
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t.tolist()]
+
+
+def aggregate_gsamples(samples_per_rank_step, world_size, steps, seconds):
+    """Whole-job throughput: every rank renders its own replica of the batch
+    (replicas only: no data exchange), so the job processes world_size times
+    one rank's samples in the slowest rank's time."""
+    return samples_per_rank_step * world_size * steps / seconds / 1e9
+
+
 def measured_peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -363,9 +383,7 @@ def main_ours(args):
     step_ms = [a.elapsed_time(b) for a, b in evs]
     t = sum(step_ms) / 1e3
     if ws > 1:
-        tt = torch.tensor([t, t_plain], device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t, t_plain = float(tt[0].item()), float(tt[1].item())
+        t, t_plain = max_over_ranks([t, t_plain], dev)
         torch.distributed.barrier()
 
     # ---- e2e: the host-buffer entry point (device -> host images per step) --
@@ -380,13 +398,11 @@ def main_ours(args):
     ctx.synchronize()
     t_e2e = time.perf_counter() - te
     if ws > 1:
-        tt = torch.tensor([t_e2e], device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_e2e = float(tt.item())
+        (t_e2e,) = max_over_ranks([t_e2e], dev)
 
-    value = samples * ws * args.steps / t / 1e9
-    plain_value = samples * ws * args.steps / t_plain / 1e9
-    e2e = samples * ws * args.steps / t_e2e / 1e9
+    value = aggregate_gsamples(samples, ws, args.steps, t)
+    plain_value = aggregate_gsamples(samples, ws, args.steps, t_plain)
+    e2e = aggregate_gsamples(samples, ws, args.steps, t_e2e)
     hbm, peak_kind = measured_peaks()
     mean_launch_s = t / args.steps  # one batch kernel per step
     achieved = samples * BYTES_PER_SAMPLE / mean_launch_s / 1e9
