@@ -153,101 +153,6 @@ __global__ void __launch_bounds__(kMaxBlockThreads)
     }
 }
 
-// Lane refill (Volume shader, single pass): each warp keeps a pool of rays
-// (the 32 rays of each of `grab` queue tiles); a lane whose ray ends writes
-// its pixel and takes the next ray of the pool, so lanes do not idle while
-// the longest ray of a tile finishes.  Every ray runs the same iterations as
-// in the other kernels, so images are identical.
-template <int PC, int DT, bool PADDED>
-__global__ void __launch_bounds__(kMaxBlockThreads)
-    batch_refill_kernel(const __grid_constant__ BatchArgs B) {
-    extern __shared__ float4 smem[];
-    const ShadeArgs &A = B.A;
-    float4 *tf = smem;
-    float *lut = reinterpret_cast<float *>(smem + A.ntf);
-    int *starts = reinterpret_cast<int *>(lut + 256);
-    for (int i = threadIdx.x; i < A.ntf; i += blockDim.x) tf[i] = A.tf[i];
-    for (int i = threadIdx.x; i < 256; i += blockDim.x) lut[i] = float(i) / 255.f;
-    for (int i = threadIdx.x; i < B.nviews; i += blockDim.x) starts[i] = B.starts[i];
-    __syncthreads();
-    const Shared S{tf, A.ntf, float(A.ntf), lut};
-    const unsigned int full = 0xffffffffu;
-    const int lane = threadIdx.x & 31;
-    const unsigned int lt_mask = (1u << lane) - 1u;
-    unsigned int samples = 0;
-    unsigned int pool_next = 0, pool_end = 0;  // ray indices: tile * 32 + lane-in-tile
-    bool exhausted = false, active = false;
-    Px p;
-    VolumeMarch m;
-    unsigned char *dst = nullptr;
-    for (;;) {
-        // give a ray to every lane without one
-        for (;;) {
-            const unsigned int need = __ballot_sync(full, !active);
-            if (!need || exhausted) break;
-            if (pool_next >= pool_end) {
-                unsigned int t0 = 0;
-                if (lane == 0) t0 = atomicAdd(B.queue, unsigned(B.grab));
-                t0 = __shfl_sync(full, t0, 0);
-                if (t0 >= unsigned(B.total_tiles)) {
-                    exhausted = true;
-                    break;
-                }
-                pool_next = t0 * 32u;
-                pool_end = min(t0 + unsigned(B.grab), unsigned(B.total_tiles)) * 32u;
-            }
-            const unsigned int avail = pool_end - pool_next;
-            const unsigned int rank = __popc(need & lt_mask);
-            if (!active && rank < avail) {
-                const unsigned int r = pool_next + rank;
-                const int t = int(r >> 5), li = int(r & 31u);
-                const int vi = find_view(starts, B.nviews, t);
-                const BatchView &bv = B.views[vi];
-                const int local = t - starts[vi];
-                const int ty = local / bv.tiles_x, tx = local - ty * bv.tiles_x;
-                const int x = tx * B.tile_w + li % B.tile_w, y = ty * B.tile_h + li / B.tile_w;
-                if (x < bv.view.W && y < bv.view.H) {
-                    float ox, oy, oz, dx, dy, dz;
-                    gen_ray(bv.view, x, y, ox, oy, oz, dx, dy, dz);
-                    dst = B.out + bv.out_off + (size_t(y) * bv.view.W + x) * 4;
-                    emit_setup<HY_SHADER_VOLUME>(p, A, ox, oy, oz, dx, dy, dz, 0.f, 0.f, 0.f,
-                                                 A.bbox_max[0], A.bbox_max[1], A.bbox_max[2]);
-                    if (p.nsteps > 0) {
-                        m.init(p);
-                        active = true;
-                    } else {
-                        *reinterpret_cast<uchar4 *>(dst) =
-                            make_uchar4(A.clear_u8[0], A.clear_u8[1], A.clear_u8[2], 0);
-                    }
-                }
-            }
-            pool_next += min(unsigned(__popc(need)), avail);
-        }
-        if (!__any_sync(full, active)) {
-            if (exhausted) break;
-            continue;
-        }
-        if (active) {
-            const bool go = m.step<PC, DT, PADDED>(p, A, S, samples);
-            if (!go || p.nsteps <= 0) {
-                uchar4 q;
-                if (p.vw != 0.f)
-                    q = make_uchar4(saturate_u8(p.vx), saturate_u8(p.vy), saturate_u8(p.vz),
-                                    saturate_u8(p.vw));
-                else
-                    q = make_uchar4(A.clear_u8[0], A.clear_u8[1], A.clear_u8[2], 0);
-                *reinterpret_cast<uchar4 *>(dst) = q;
-                active = false;
-            }
-        }
-    }
-    if (A.count) {
-        unsigned long long s = samples;
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(full, s, o);
-        if (lane == 0 && s) atomicAdd(A.counter, s);
-    }
-}
-
 template <int SHADER, int PC, int DT, bool PADDED>
 const void *pick_c(int composite) {
     if (composite) return reinterpret_cast<const void *>(&batch_kernel<SHADER, PC, DT, PADDED, 1>);
@@ -260,9 +165,10 @@ const void *pick_shader(const ShadeArgs &a) {
         return pick_c<SHADER, 0, HY_DTYPE_U8, false>(a.composite);
     } else {
         const bool padded = a.vol.pad > 0;
-        if (a.vol.dtype == HY_DTYPE_F32)
+        if (a.vol.dtype == HY_DTYPE_F32) {
             return padded ? pick_c<SHADER, 0, HY_DTYPE_F32, true>(a.composite)
                           : pick_c<SHADER, 0, HY_DTYPE_F32, false>(a.composite);
+        }
         if (padded && a.vol.P == 66) return pick_c<SHADER, 66, HY_DTYPE_U8, true>(a.composite);
         if (padded && a.vol.P == 130) return pick_c<SHADER, 130, HY_DTYPE_U8, true>(a.composite);
         return padded ? pick_c<SHADER, 0, HY_DTYPE_U8, true>(a.composite)
@@ -270,20 +176,7 @@ const void *pick_shader(const ShadeArgs &a) {
     }
 }
 
-template <int PC, int DT, bool PADDED>
-const void *pick_refill() {
-    return reinterpret_cast<const void *>(&batch_refill_kernel<PC, DT, PADDED>);
-}
-
-const void *pick_kernel(const ShadeArgs &a, int queue_mode = 1) {
-    if (queue_mode == 2 && a.shader == HY_SHADER_VOLUME && !a.composite) {
-        const bool padded = a.vol.pad > 0;
-        if (a.vol.dtype == HY_DTYPE_F32)
-            return padded ? pick_refill<0, HY_DTYPE_F32, true>() : pick_refill<0, HY_DTYPE_F32, false>();
-        if (padded && a.vol.P == 66) return pick_refill<66, HY_DTYPE_U8, true>();
-        if (padded && a.vol.P == 130) return pick_refill<130, HY_DTYPE_U8, true>();
-        return padded ? pick_refill<0, HY_DTYPE_U8, true>() : pick_refill<0, HY_DTYPE_U8, false>();
-    }
+const void *pick_kernel(const ShadeArgs &a) {
     switch (a.shader) {
         case HY_SHADER_VOLUME:
             return pick_shader<HY_SHADER_VOLUME>(a);
@@ -324,7 +217,7 @@ bool valid_config(const hy_batch_config &c) {
     const bool tw = c.tile_w == 4 || c.tile_w == 8 || c.tile_w == 16 || c.tile_w == 32;
     return tw && c.grab >= 1 && c.grab <= 16 && c.block_warps >= 1 &&
            c.block_warps * 32 <= kMaxBlockThreads && c.blocks_per_sm >= 0 &&
-           c.blocks_per_sm <= 32 && c.block_queue >= 0 && c.block_queue <= 2;
+           c.blocks_per_sm <= 32 && (c.block_queue == 0 || c.block_queue == 1);
 }
 
 void drop_graph(hy_batch *b) {
@@ -335,7 +228,7 @@ void drop_graph(hy_batch *b) {
 }
 
 void unit_shape(const hy_batch_config &c, int &bx, int &by) {
-    if (c.block_queue != 1) {
+    if (!c.block_queue) {
         bx = by = 1;
         return;
     }
@@ -346,7 +239,7 @@ void unit_shape(const hy_batch_config &c, int &bx, int &by) {
 // (Re)build the tile layout for the current config and the persistent grid.
 int layout(hy_batch *b) {
     hy_ctx *ctx = b->ctx;
-    b->kernel = pick_kernel(b->base, b->cfg.block_queue);
+    b->kernel = pick_kernel(b->base);
     int bx, by;
     unit_shape(b->cfg, bx, by);
     const int tw = b->cfg.tile_w * bx, th = (32 / b->cfg.tile_w) * by;
@@ -409,9 +302,7 @@ int launch(hy_batch *b, uint8_t *out) {
         args.tile_w = b->cfg.tile_w;
         args.tile_h = 32 / b->cfg.tile_w;
         args.grab = b->cfg.grab;
-        // mode 2 (lane refill) exists for the single-pass Volume shader only;
-        // other shaders run the per-warp queue
-        args.block_queue = b->cfg.block_queue == 1 ? 1 : 0;
+        args.block_queue = b->cfg.block_queue;
         unit_shape(b->cfg, args.bx, args.by);
         args.queue = b->queue_dev;
         args.out = out;
@@ -564,7 +455,7 @@ extern "C" int hy_batch_autotune(hy_batch *b, uint8_t *rgba_dev, int32_t reps,
     HY_CUDA(ctx, cudaEventCreate(&e0));
     HY_CUDA(ctx, cudaEventCreate(&e1));
     int rc = HY_OK;
-    for (int bq = 0; bq < 3; ++bq)
+    for (int bq = 0; bq < 2; ++bq)
     for (int tw : tws)
         for (int g : grabs)
             for (int w : warps) {
