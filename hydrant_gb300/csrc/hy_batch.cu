@@ -45,9 +45,14 @@ struct BatchArgs {
 
 constexpr int kMaxViews = 2048;
 constexpr int kMaxBlockThreads = 256;
+// Resident 256-thread blocks per SM the compiler is asked to fit (a register
+// budget of 65536 / (256 * n) per thread).
+#ifndef HY_BATCH_MIN_BLOCKS
+#define HY_BATCH_MIN_BLOCKS 4
+#endif
 
 // Shades one pixel of a batch view and stores its RGBA8 value.
-template <int SHADER, int PC, int DT, bool PADDED, int COMPOSITE>
+template <int SHADER, int PC, int DT, bool PADDED, int COMPOSITE, bool LEAN>
 __device__ __forceinline__ long long shade_batch_pixel(const BatchArgs &B, const Shared &S,
                                                        const BatchView &bv, int x, int y) {
     const ShadeArgs &A = B.A;
@@ -62,8 +67,9 @@ __device__ __forceinline__ long long shade_batch_pixel(const BatchArgs &B, const
                                                         aux);
     } else {
         Px p;
-        samples = emit<SHADER, PC, DT, PADDED>(p, A, bv.view, S, ox, oy, oz, dx, dy, dz, 0.f, 0.f,
-                                               0.f, A.bbox_max[0], A.bbox_max[1], A.bbox_max[2]);
+        samples = emit<SHADER, PC, DT, PADDED, LEAN>(p, A, bv.view, S, ox, oy, oz, dx, dy, dz,
+                                                     0.f, 0.f, 0.f, A.bbox_max[0], A.bbox_max[1],
+                                                     A.bbox_max[2]);
         v = make_float4(p.vx, p.vy, p.vz, p.vw);
     }
     uchar4 q;
@@ -91,8 +97,10 @@ __device__ __forceinline__ int find_view(const int *starts, int n, int t) {
 // own units), or one block tile of bx x by warp tiles per unit (block_queue
 // == 1, the block takes a unit and warp w shades its w-th warp tile, so the
 // warps of an SM work on neighbouring rays and share L1 lines).
-template <int SHADER, int PC, int DT, bool PADDED, int COMPOSITE>
-__global__ void __launch_bounds__(kMaxBlockThreads)
+// LEAN: Volume shader in Default mode without compositing (theta / phi are
+// not needed for an RGBA image; see VolumeMarch::step).
+template <int SHADER, int PC, int DT, bool PADDED, int COMPOSITE, bool LEAN>
+__global__ void __launch_bounds__(kMaxBlockThreads, HY_BATCH_MIN_BLOCKS)
     batch_kernel(const __grid_constant__ BatchArgs B) {
     extern __shared__ float4 smem[];
     __shared__ unsigned int s_t0;
@@ -125,7 +133,7 @@ __global__ void __launch_bounds__(kMaxBlockThreads)
                 const int uy = local / bv.tiles_x, ux = local - uy * bv.tiles_x;
                 const int x = (ux * B.bx + wx) * B.tile_w + lx;
                 const int y = (uy * B.by + wy) * B.tile_h + ly;
-                samples += shade_batch_pixel<SHADER, PC, DT, PADDED, COMPOSITE>(B, S, bv, x, y);
+                samples += shade_batch_pixel<SHADER, PC, DT, PADDED, COMPOSITE, LEAN>(B, S, bv, x, y);
             }
         }
     } else {
@@ -141,7 +149,7 @@ __global__ void __launch_bounds__(kMaxBlockThreads)
                 const BatchView &bv = B.views[vi];
                 const int local = t - starts[vi];
                 const int ty = local / bv.tiles_x, tx = local - ty * bv.tiles_x;
-                samples += shade_batch_pixel<SHADER, PC, DT, PADDED, COMPOSITE>(
+                samples += shade_batch_pixel<SHADER, PC, DT, PADDED, COMPOSITE, LEAN>(
                     B, S, bv, tx * B.tile_w + lx, ty * B.tile_h + ly);
             }
         }
@@ -154,25 +162,30 @@ __global__ void __launch_bounds__(kMaxBlockThreads)
 }
 
 template <int SHADER, int PC, int DT, bool PADDED>
-const void *pick_c(int composite) {
-    if (composite) return reinterpret_cast<const void *>(&batch_kernel<SHADER, PC, DT, PADDED, 1>);
-    return reinterpret_cast<const void *>(&batch_kernel<SHADER, PC, DT, PADDED, 0>);
+const void *pick_c(const ShadeArgs &a) {
+    if (a.composite)
+        return reinterpret_cast<const void *>(&batch_kernel<SHADER, PC, DT, PADDED, 1, false>);
+    if constexpr (SHADER == HY_SHADER_VOLUME) {
+        if (a.mode == HY_VOLUME_DEFAULT)
+            return reinterpret_cast<const void *>(&batch_kernel<SHADER, PC, DT, PADDED, 0, true>);
+    }
+    return reinterpret_cast<const void *>(&batch_kernel<SHADER, PC, DT, PADDED, 0, false>);
 }
 
 template <int SHADER>
 const void *pick_shader(const ShadeArgs &a) {
     if constexpr (SHADER == HY_SHADER_BLOCKS) {
-        return pick_c<SHADER, 0, HY_DTYPE_U8, false>(a.composite);
+        return pick_c<SHADER, 0, HY_DTYPE_U8, false>(a);
     } else {
         const bool padded = a.vol.pad > 0;
         if (a.vol.dtype == HY_DTYPE_F32) {
-            return padded ? pick_c<SHADER, 0, HY_DTYPE_F32, true>(a.composite)
-                          : pick_c<SHADER, 0, HY_DTYPE_F32, false>(a.composite);
+            return padded ? pick_c<SHADER, 0, HY_DTYPE_F32, true>(a)
+                          : pick_c<SHADER, 0, HY_DTYPE_F32, false>(a);
         }
-        if (padded && a.vol.P == 66) return pick_c<SHADER, 66, HY_DTYPE_U8, true>(a.composite);
-        if (padded && a.vol.P == 130) return pick_c<SHADER, 130, HY_DTYPE_U8, true>(a.composite);
-        return padded ? pick_c<SHADER, 0, HY_DTYPE_U8, true>(a.composite)
-                      : pick_c<SHADER, 0, HY_DTYPE_U8, false>(a.composite);
+        if (padded && a.vol.P == 66) return pick_c<SHADER, 66, HY_DTYPE_U8, true>(a);
+        if (padded && a.vol.P == 130) return pick_c<SHADER, 130, HY_DTYPE_U8, true>(a);
+        return padded ? pick_c<SHADER, 0, HY_DTYPE_U8, true>(a)
+                      : pick_c<SHADER, 0, HY_DTYPE_U8, false>(a);
     }
 }
 

@@ -48,7 +48,9 @@ __device__ __forceinline__ uchar4 quantise(const ShadeArgs &A, float4 v) {
     return make_uchar4(A.clear_u8[0], A.clear_u8[1], A.clear_u8[2], 0);
 }
 
-template <int SHADER, int PC, int DT, bool PADDED, int COMPOSITE>
+// LEAN: Volume shader, Default mode, no compositing and no aux output
+// (theta / phi are not computed; see VolumeMarch::step).
+template <int SHADER, int PC, int DT, bool PADDED, int COMPOSITE, bool LEAN>
 __global__ void __launch_bounds__(kThreads) render_kernel(const __grid_constant__ ShadeArgs A) {
     extern __shared__ float4 smem[];
     float4 *tf = smem;
@@ -66,8 +68,9 @@ __global__ void __launch_bounds__(kThreads) render_kernel(const __grid_constant_
             samples = composite_ray<SHADER, PC, DT, PADDED>(A, A.view, S, ox, oy, oz, dx, dy, dz, v, aux);
         } else {
             Px p;
-            samples = emit<SHADER, PC, DT, PADDED>(p, A, A.view, S, ox, oy, oz, dx, dy, dz, 0.f, 0.f, 0.f,
-                                                   A.bbox_max[0], A.bbox_max[1], A.bbox_max[2]);
+            samples = emit<SHADER, PC, DT, PADDED, LEAN>(p, A, A.view, S, ox, oy, oz, dx, dy, dz,
+                                                         0.f, 0.f, 0.f, A.bbox_max[0],
+                                                         A.bbox_max[1], A.bbox_max[2]);
             v = make_float4(p.vx, p.vy, p.vz, p.vw);
             if (SHADER == HY_SHADER_VOLUME)
                 aux = make_float4(p.e0, p.e1, p.e2, p.e3);
@@ -79,7 +82,7 @@ __global__ void __launch_bounds__(kThreads) render_kernel(const __grid_constant_
         const size_t idx = size_t(y) * A.view.W + x;
         A.rgba[idx] = quantise(A, v);
         if (A.vout) A.vout[idx] = v;
-        if (A.aux) A.aux[idx] = aux;
+        if (!LEAN && A.aux) A.aux[idx] = aux;
     }
     count_samples(A, samples);
 }
@@ -224,10 +227,17 @@ dim3 grid_of(const ShadeArgs &a) {
 
 template <int SHADER, int PC, int DT, bool PADDED>
 void launch_fused(const ShadeArgs &a, cudaStream_t s) {
-    if (a.composite)
-        render_kernel<SHADER, PC, DT, PADDED, 1><<<grid_of(a), kThreads, smem_bytes(a), s>>>(a);
-    else
-        render_kernel<SHADER, PC, DT, PADDED, 0><<<grid_of(a), kThreads, smem_bytes(a), s>>>(a);
+    if (a.composite) {
+        render_kernel<SHADER, PC, DT, PADDED, 1, false><<<grid_of(a), kThreads, smem_bytes(a), s>>>(a);
+        return;
+    }
+    if constexpr (SHADER == HY_SHADER_VOLUME) {
+        if (a.mode == HY_VOLUME_DEFAULT && !a.aux) {
+            render_kernel<SHADER, PC, DT, PADDED, 0, true><<<grid_of(a), kThreads, smem_bytes(a), s>>>(a);
+            return;
+        }
+    }
+    render_kernel<SHADER, PC, DT, PADDED, 0, false><<<grid_of(a), kThreads, smem_bytes(a), s>>>(a);
 }
 
 // Instantiations: Blocks reads no bricks; u8 volumes with a 1-voxel apron and

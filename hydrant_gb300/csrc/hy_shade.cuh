@@ -129,7 +129,9 @@ __device__ __forceinline__ float sample_brick(const BrickRef &b, int Prt, float 
     float v000, v100, v010, v110, v001, v101, v011, v111;
     if (INTERIOR ||
         (ix >= 0 && ix <= P - 2 && iy >= 0 && iy <= P - 2 && iz >= 0 && iz <= P - 2)) {
-        const long long base = ((long long)iz * P + iy) * P + ix;
+        // a compile-time brick edge (<= 130) keeps the offset in 32 bits
+        const long long base = PC ? (long long)((iz * PC + iy) * PC + ix)
+                                  : ((long long)iz * P + iy) * P + ix;
         if (DT == HY_DTYPE_U8) {
             const unsigned char *q = b.base + base;
             v000 = lut[__ldg(q)];
@@ -227,29 +229,32 @@ struct Shared {
 
 // Tracks the brick of the current sample position.  floor(o) only changes
 // when o leaves [ip, ip+1) on some axis, so the texel lookups are redone only
-// then (same texel, same values); o == NaN fails the test and redoes them
-// every step, exactly like the reference.
+// then (same texel, same values).  The test reads the brick-local
+// coordinate l = o - ip the sampler needs anyway: l in [+0, 1) as an unsigned
+// compare of its bits.  fl(o - ip) >= +0 and < 1 imply ip <= o < ip + 1
+// (rounding is monotone and a non-zero difference of floats never rounds to
+// 0); the converse can fail only where o - ip rounds up to 1, which merely
+// redoes the lookups of the same cell.  NaN and the initial ip = +inf fail
+// the test, so those steps redo them every time, like the reference.
+__device__ __forceinline__ bool unit_interval(float l) { return __float_as_uint(l) < 0x3f800000u; }
+
 struct BrickCursor {
-    float ipx, ipy, ipz, hx, hy, hz;
+    float ipx, ipy, ipz;
     int cur, cd, pg;
     BrickRef br;
     __device__ __forceinline__ void reset() {
         ipx = ipy = ipz = __int_as_float(0x7f800000);
-        hx = hy = hz = -__int_as_float(0x7f800000);
         cur = -1;
         cd = 0;
         pg = -1;
         br = BrickRef{};
     }
-    __device__ __forceinline__ void update(const DevVolume &V, float ox, float oy, float oz) {
-        if (ox >= ipx && ox < hx && oy >= ipy && oy < hy && oz >= ipz && oz < hz) return;
+    // o's cell changed (or may have): redo floor(o) and the thumbnail lookups
+    __device__ __forceinline__ void locate(const DevVolume &V, float ox, float oy, float oz) {
         const float fgx = float(V.gx), fgy = float(V.gy), fgz = float(V.gz);
         ipx = floorf(ox);
         ipy = floorf(oy);
         ipz = floorf(oz);
-        hx = ipx + 1.f;
-        hy = ipy + 1.f;
-        hz = ipz + 1.f;
         const int bid = thumb_index(V, fgx, fgy, fgz, ipx, ipy, ipz);
         if (bid != cur) {
             cur = bid;
@@ -258,6 +263,18 @@ struct BrickCursor {
             pg = in.y;
             if (cd == 0 && pg >= 0) br = load_brick(V, pg);
         }
+    }
+    // brick-local coordinates of o, relocating first when o left the cell
+    __device__ __forceinline__ void update(const DevVolume &V, float ox, float oy, float oz,
+                                           float &lx, float &ly, float &lz) {
+        lx = ox - ipx;
+        ly = oy - ipy;
+        lz = oz - ipz;
+        if (unit_interval(lx) & unit_interval(ly) & unit_interval(lz)) return;
+        locate(V, ox, oy, oz);
+        lx = ox - ipx;
+        ly = oy - ipy;
+        lz = oz - ipz;
     }
 };
 
@@ -282,22 +299,25 @@ struct VolumeMarch {
     }
 
     // One iteration of `while (nsteps > 0)`; false when the ray breaks out
-    // on an absent brick (volume_shader.cu:50).
-    template <int PC, int DT, bool PADDED>
+    // on an absent brick (volume_shader.cu:50).  LEAN: Default mode and
+    // nobody reads theta / phi (no film, aux output or per-brick
+    // compositing), so their updates are left out; v is unchanged.
+    template <int PC, int DT, bool PADDED, bool LEAN = false>
     __device__ __forceinline__ bool step(Px &p, const ShadeArgs &A, const Shared &S,
                                          unsigned int &samples) {
         const DevVolume &V = A.vol;
-        c.update(V, p.ox, p.oy, p.oz);
+        float lx, ly, lz;
+        c.update(V, p.ox, p.oy, p.oz, lx, ly, lz);
         if (c.cd) {
             p.nsteps -= skip_nblock_steps(p, rx, ry, rz, c.ipx, c.ipy, c.ipz, c.cd, cdu,
                                           A.step * float(p.step_size));
         } else {
             if (c.pg == -1) return false;
-            float s = sample_brick<PC, DT, PADDED>(c.br, V.P, p.ox - c.ipx, p.oy - c.ipy,
-                                                   p.oz - c.ipz, S.lut);
+            float s = sample_brick<PC, DT, PADDED>(c.br, V.P, lx, ly, lz, S.lut);
             ++samples;
             float4 ub = sample_tf(S.tf, S.ntf, S.fntf, s);
-            if (A.mode == HY_VOLUME_PARTITION) {
+            if (LEAN) {
+            } else if (A.mode == HY_VOLUME_PARTITION) {
                 float r = A.rank;
                 float mr = 1.f * (1.f - r) + 0.f * r, mg = 0.f * (1.f - r) + 0.f * r,
                       mb = 0.f * (1.f - r) + 1.f * r;
@@ -312,10 +332,12 @@ struct VolumeMarch {
             ub.x = ub.x * w;
             ub.y = ub.y * w;
             ub.z = ub.z * w;
-            p.e0 = p.e0 + ub.x * p.e3;
-            p.e1 = p.e1 + ub.y * p.e3;
-            p.e2 = p.e2 + ub.z * p.e3;
-            p.e3 = p.e3 * (1.f - ub.w);
+            if (!LEAN) {
+                p.e0 = p.e0 + ub.x * p.e3;
+                p.e1 = p.e1 + ub.y * p.e3;
+                p.e2 = p.e2 + ub.z * p.e3;
+                p.e3 = p.e3 * (1.f - ub.w);
+            }
             const float t = 1.f - p.vw;
             p.vx = p.vx + ub.x * t;
             p.vy = p.vy + ub.y * t;
@@ -342,13 +364,13 @@ struct VolumeMarch {
     }
 };
 
-template <int PC, int DT, bool PADDED>
+template <int PC, int DT, bool PADDED, bool LEAN = false>
 __device__ __forceinline__ long long volume_main(Px &p, const ShadeArgs &A, const Shared &S) {
     unsigned int samples = 0;
     VolumeMarch m;
     m.init(p);
     while (p.nsteps > 0)
-        if (!m.step<PC, DT, PADDED>(p, A, S, samples)) break;
+        if (!m.step<PC, DT, PADDED, LEAN>(p, A, S, samples)) break;
     return samples;
 }
 
@@ -442,15 +464,15 @@ __device__ __forceinline__ long long iso_main(Px &p, const ShadeArgs &A, const V
     BrickCursor c;
     c.reset();
     while (p.nsteps > 0) {
-        c.update(V, p.ox, p.oy, p.oz);
+        float l0x, l0y, l0z;
+        c.update(V, p.ox, p.oy, p.oz, l0x, l0y, l0z);
         const float ipx = c.ipx, ipy = c.ipy, ipz = c.ipz;
         const BrickRef &br = c.br;
         if (c.cd) {
             p.nsteps -= skip_nblock_steps(p, rx, ry, rz, ipx, ipy, ipz, c.cd, cdu, A.step);
         } else {
             if (c.pg == -1) break;  // page fault: resume in the next march pass
-            float value = sample_brick<PC, DT, PADDED>(br, V.P, p.ox - ipx, p.oy - ipy,
-                                                       p.oz - ipz, S.lut);
+            float value = sample_brick<PC, DT, PADDED>(br, V.P, l0x, l0y, l0z, S.lut);
             ++samples;
             if (fsign(value - iso) != prev_sign) {
                 const float dt = A.step;
@@ -518,10 +540,10 @@ __device__ __forceinline__ long long iso_main(Px &p, const ShadeArgs &A, const V
     return samples;
 }
 
-template <int SHADER, int PC, int DT, bool PADDED>
+template <int SHADER, int PC, int DT, bool PADDED, bool LEAN = false>
 __device__ __forceinline__ long long run_main(Px &p, const ShadeArgs &A, const ViewArgs &Vw,
                                              const Shared &S) {
-    if (SHADER == HY_SHADER_VOLUME) return volume_main<PC, DT, PADDED>(p, A, S);
+    if (SHADER == HY_SHADER_VOLUME) return volume_main<PC, DT, PADDED, LEAN>(p, A, S);
     if (SHADER == HY_SHADER_BLOCKS) return blocks_main(p, A);
     return iso_main<PC, DT, PADDED>(p, A, Vw, S);
 }
@@ -586,14 +608,14 @@ __device__ __forceinline__ bool emit_setup(Px &p, const ShadeArgs &A, float ox, 
 }
 
 // ray_emit_shader_impl: emit_setup, then main on a hit (shader.hpp:113-137).
-template <int SHADER, int PC, int DT, bool PADDED>
+template <int SHADER, int PC, int DT, bool PADDED, bool LEAN = false>
 __device__ __forceinline__ long long emit(Px &p, const ShadeArgs &A, const ViewArgs &Vw,
                                           const Shared &S, float ox,
                                           float oy, float oz, float dx, float dy, float dz,
                                           float x0, float y0, float z0, float x1, float y1,
                                           float z1) {
     if (emit_setup<SHADER>(p, A, ox, oy, oz, dx, dy, dz, x0, y0, z0, x1, y1, z1))
-        return run_main<SHADER, PC, DT, PADDED>(p, A, Vw, S);
+        return run_main<SHADER, PC, DT, PADDED, LEAN>(p, A, Vw, S);
     return 0;
 }
 
