@@ -63,6 +63,9 @@ def parse_args():
                     help="paging: coarse fallback level (box filter 2**L; 0 = none)")
     ap.add_argument("--max-uploads", type=int, default=0,
                     help="paging: brick uploads per frame (0 = every missing brick)")
+    ap.add_argument("--launch-shape", default="",
+                    help="fixed batch launch shape tile_w,grab,block_warps,blocks_per_sm,"
+                         "block_queue (implies --no-autotune)")
     ap.add_argument("--no-autotune", action="store_true",
                     help="use the default batch launch shape (profiling)")
     ap.add_argument("--cpu-sample-rows", type=int, default=0,
@@ -353,11 +356,13 @@ def main_ours(args):
     out = torch.empty(batch.nbytes, dtype=torch.uint8, device=dev)
     key = autotune.signature(torch.cuda.get_device_name(local), params[0], vol.desc,
                              [(W, H) for _, W, H in views])
-    if args.no_autotune:
+    if args.launch_shape:
+        batch.set_config(*[int(x) for x in args.launch_shape.split(",")])
+    if args.no_autotune or args.launch_shape:
         c = batch.config
         tuned = {"tile_w": c.tile_w, "grab": c.grab, "block_warps": c.block_warps,
                  "blocks_per_sm": c.blocks_per_sm, "block_queue": c.block_queue,
-                 "source": "default"}
+                 "source": "fixed" if args.launch_shape else "default"}
     else:
         tuned = autotune.tuned_config(batch, key, out.data_ptr(), reps=1)
     batch.set_counting(True)

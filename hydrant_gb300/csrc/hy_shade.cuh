@@ -110,6 +110,28 @@ __device__ __forceinline__ BrickRef load_brick(const DevVolume &V, int reg) {
 // f = P*(k*x + b) lies in [pad, bs+pad] (up to rounding far below 0.5), so
 // Wrap is the identity and floor(f - 0.5) is in [pad-1, bs+pad-1] within
 // [0, P-2]: both range checks are known to pass and are left out.
+// u / 255.f for a u8 voxel without the table: q = u * fl(1/255) and one
+// fused residual correction (Markstein), the correctly rounded quotient for
+// every u in 0..255 (checked exhaustively against u / 255.f).  Taps below
+// HY_U8_ARITH_TAPS use it, the others the shared-memory table (whose lookups
+// conflict on banks when neighbouring lanes read distant values).  All 8
+// arithmetic measured fastest on the per-view kernel (-3%) and even on the
+// batched one.
+#ifndef HY_U8_ARITH_TAPS
+#define HY_U8_ARITH_TAPS 8
+#endif
+__device__ __forceinline__ float u8_norm(unsigned int u) {
+    const float x = __uint2float_rn(u);
+    const float inv = 1.f / 255.f;
+    const float q = __fmul_rn(x, inv);
+    const float r = __fmaf_rn(-q, 255.f, x);
+    return __fmaf_rn(r, inv, q);
+}
+template <int TAP>
+__device__ __forceinline__ float u8_value(unsigned char u, const float *__restrict__ lut) {
+    return TAP < HY_U8_ARITH_TAPS ? u8_norm(u) : lut[u];
+}
+
 template <int PC, int DT, bool INTERIOR = false>
 __device__ __forceinline__ float sample_brick(const BrickRef &b, int Prt, float lx, float ly,
                                               float lz, const float *__restrict__ lut) {
@@ -134,14 +156,14 @@ __device__ __forceinline__ float sample_brick(const BrickRef &b, int Prt, float 
                                   : ((long long)iz * P + iy) * P + ix;
         if (DT == HY_DTYPE_U8) {
             const unsigned char *q = b.base + base;
-            v000 = lut[__ldg(q)];
-            v100 = lut[__ldg(q + 1)];
-            v010 = lut[__ldg(q + P)];
-            v110 = lut[__ldg(q + P + 1)];
-            v001 = lut[__ldg(q + P * P)];
-            v101 = lut[__ldg(q + P * P + 1)];
-            v011 = lut[__ldg(q + P * P + P)];
-            v111 = lut[__ldg(q + P * P + P + 1)];
+            v000 = u8_value<0>(__ldg(q), lut);
+            v100 = u8_value<1>(__ldg(q + 1), lut);
+            v010 = u8_value<2>(__ldg(q + P), lut);
+            v110 = u8_value<3>(__ldg(q + P + 1), lut);
+            v001 = u8_value<4>(__ldg(q + P * P), lut);
+            v101 = u8_value<5>(__ldg(q + P * P + 1), lut);
+            v011 = u8_value<6>(__ldg(q + P * P + P), lut);
+            v111 = u8_value<7>(__ldg(q + P * P + P + 1), lut);
         } else {
             const float *q = reinterpret_cast<const float *>(b.base) + base;
             v000 = __ldg(q);
