@@ -112,8 +112,8 @@ __global__ void __launch_bounds__(kMaxBlockThreads, HY_BATCH_MIN_BLOCKS)
     for (int i = threadIdx.x; i < 256; i += blockDim.x) lut[i] = float(i) / 255.f;
     for (int i = threadIdx.x; i < B.nviews; i += blockDim.x) starts[i] = B.starts[i];
     __syncthreads();
-    const Shared S{tf, A.ntf, float(A.ntf), lut};
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const Shared S{tf, A.ntf, float(A.ntf), lut};
     const int lx = lane % B.tile_w, ly = lane / B.tile_w;
     long long samples = 0;
     if (B.block_queue) {
@@ -226,6 +226,12 @@ struct hy_batch {
 
 namespace {
 
+// Dynamic shared memory above the default 48 KiB needs an opt-in per kernel.
+cudaError_t allow_smem(const void *kernel, size_t smem) {
+    if (smem <= 48 * 1024) return cudaSuccess;
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+}
+
 bool valid_config(const hy_batch_config &c) {
     const bool tw = c.tile_w == 4 || c.tile_w == 8 || c.tile_w == 16 || c.tile_w == 32;
     return tw && c.grab >= 1 && c.grab <= 16 && c.block_warps >= 1 &&
@@ -285,7 +291,9 @@ int layout(hy_batch *b) {
     HY_CUDA(ctx, cudaMemcpyAsync(b->starts_dev, b->starts.data(), b->starts.size() * sizeof(int),
                                  cudaMemcpyHostToDevice, ctx->stream));
     HY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    b->smem = size_t(b->base.ntf) * sizeof(float4) + 256 * sizeof(float) + b->in.size() * sizeof(int);
+    b->smem = size_t(b->base.ntf) * sizeof(float4) + 256 * sizeof(float) +
+              b->in.size() * sizeof(int);
+    HY_CUDA(ctx, allow_smem(b->kernel, b->smem));
     const int threads = b->cfg.block_warps * 32;
     int per_sm = b->cfg.blocks_per_sm;
     if (per_sm == 0) {
@@ -631,6 +639,7 @@ extern "C" int hy_render_views_noalloc(hy_ctx *ctx, const hy_volume *vol,
     const size_t smem = size_t(base.ntf) * sizeof(float4) + 256 * sizeof(float) +
                         size_t(nviews) * sizeof(int);
     int per_sm = 0, sms = 0;
+    HY_CUDA(ctx, allow_smem(kernel, smem));
     HY_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem));
     HY_CUDA(ctx, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
     void *kargs[] = {&args};

@@ -127,9 +127,12 @@ __device__ __forceinline__ float u8_norm(unsigned int u) {
     const float r = __fmaf_rn(-q, 255.f, x);
     return __fmaf_rn(r, inv, q);
 }
+__device__ __forceinline__ float lut_at(const float *__restrict__ lut, unsigned int u) {
+    return lut[u];
+}
 template <int TAP>
 __device__ __forceinline__ float u8_value(unsigned char u, const float *__restrict__ lut) {
-    return TAP < HY_U8_ARITH_TAPS ? u8_norm(u) : lut[u];
+    return TAP < HY_U8_ARITH_TAPS ? u8_norm(u) : lut_at(lut, u);
 }
 
 template <int PC, int DT, bool INTERIOR = false>
@@ -185,14 +188,14 @@ __device__ __forceinline__ float sample_brick(const BrickRef &b, int Prt, float 
                         r01 = ((long long)jz * P + iy) * P, r11 = ((long long)jz * P + jy) * P;
         if (DT == HY_DTYPE_U8) {
             const unsigned char *q = b.base;
-            v000 = lut[__ldg(q + r00 + ix)];
-            v100 = lut[__ldg(q + r00 + jx)];
-            v010 = lut[__ldg(q + r10 + ix)];
-            v110 = lut[__ldg(q + r10 + jx)];
-            v001 = lut[__ldg(q + r01 + ix)];
-            v101 = lut[__ldg(q + r01 + jx)];
-            v011 = lut[__ldg(q + r11 + ix)];
-            v111 = lut[__ldg(q + r11 + jx)];
+            v000 = lut_at(lut, __ldg(q + r00 + ix));
+            v100 = lut_at(lut, __ldg(q + r00 + jx));
+            v010 = lut_at(lut, __ldg(q + r10 + ix));
+            v110 = lut_at(lut, __ldg(q + r10 + jx));
+            v001 = lut_at(lut, __ldg(q + r01 + ix));
+            v101 = lut_at(lut, __ldg(q + r01 + jx));
+            v011 = lut_at(lut, __ldg(q + r11 + ix));
+            v111 = lut_at(lut, __ldg(q + r11 + jx));
         } else {
             const float *q = reinterpret_cast<const float *>(b.base);
             v000 = __ldg(q + r00 + ix);
