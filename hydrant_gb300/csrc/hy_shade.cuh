@@ -110,22 +110,25 @@ __device__ __forceinline__ BrickRef load_brick(const DevVolume &V, int reg) {
 // f = P*(k*x + b) lies in [pad, bs+pad] (up to rounding far below 0.5), so
 // Wrap is the identity and floor(f - 0.5) is in [pad-1, bs+pad-1] within
 // [0, P-2]: both range checks are known to pass and are left out.
-// u / 255.f for a u8 voxel without the table: q = u * fl(1/255) and one
-// fused residual correction (Markstein), the correctly rounded quotient for
-// every u in 0..255 (checked exhaustively against u / 255.f).  Taps below
-// HY_U8_ARITH_TAPS use it, the others the shared-memory table (whose lookups
-// conflict on banks when neighbouring lanes read distant values).  All 8
-// arithmetic measured fastest on the per-view kernel (-3%) and even on the
-// batched one.
+// u / 255.f for a u8 voxel without the table: 1/255 as an unevaluated sum
+// hi + lo of two floats (hi = fl(1/255), lo = fl(1/255 - hi)) and
+// q = fma(u, hi, u * lo) (multiplication by a constant carried in two words,
+// Brisebarre & Muller 2008).  The exact quotient u/255 repeats u's 8 bits,
+// so it lies at least 1/510 ulp from a rounding boundary while hi + lo and
+// the rounding of u * lo are off by ~2^-48: q is the correctly rounded
+// quotient for every u in 0..255 (also checked exhaustively,
+// tests/test_u8_normalisation.py).  Taps below HY_U8_ARITH_TAPS use it, the
+// others the shared-memory table (whose lookups conflict on banks when
+// neighbouring lanes read distant values); all eight arithmetic measured
+// fastest.
 #ifndef HY_U8_ARITH_TAPS
 #define HY_U8_ARITH_TAPS 8
 #endif
 __device__ __forceinline__ float u8_norm(unsigned int u) {
+    constexpr float hi = 1.f / 255.f;
+    constexpr float lo = float(1.0 / 255.0 - double(1.f / 255.f));
     const float x = __uint2float_rn(u);
-    const float inv = 1.f / 255.f;
-    const float q = __fmul_rn(x, inv);
-    const float r = __fmaf_rn(-q, 255.f, x);
-    return __fmaf_rn(r, inv, q);
+    return __fmaf_rn(x, hi, __fmul_rn(x, lo));
 }
 __device__ __forceinline__ float lut_at(const float *__restrict__ lut, unsigned int u) {
     return lut[u];
