@@ -509,7 +509,8 @@ def main_paging(args):
     si = store.info
     slots = int((8 * 2**30) // si.slot_bytes)
     pg = hy.Pager(ctx, store, slots, _abi.PAGER_REALTIME, args.max_uploads)
-    p = hy.shader_params(shader="Volume", sample_rate=0.25, density=5e-3, count_samples=True)
+    p = hy.shader_params(shader="Volume", sample_rate=0.25, density=5e-3)
+    pc = hy.shader_params(shader="Volume", sample_rate=0.25, density=5e-3, count_samples=True)
     out = torch.empty(res * res * 4, dtype=torch.uint8, device=f"cuda:{local}")
     stream = torch.cuda.ExternalStream(ctx.stream)
     frames = max(1, args.frames)
@@ -520,14 +521,12 @@ def main_paging(args):
     st0 = pg.stats()
     clocks = Clocks(local)
     clocks.start()
-    samples = 0
     fallback = 0
     tw = time.perf_counter()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
     for f in range(frames):
         pg.render(p, hy.camera_orbit((3.0 * f, 30.0, 2.2)), res, res, out.data_ptr())
-        samples += ctx.stats().samples
         fallback += pg.stats()["fallback"]
     ev1.record(stream)
     ctx.synchronize()
@@ -536,6 +535,14 @@ def main_paging(args):
     gpu_s = ev0.elapsed_time(ev1) / 1e3
     st = pg.stats()
     d = {k: st[k] - st0[k] for k in st}
+    # samples: a second, untimed pass over the same orbit with counting on
+    # (reading the counter synchronises every frame).  With the coarse level
+    # every visible brick is sampled, so the count does not depend on what
+    # the cache holds; without it the second pass starts from a warmer cache.
+    samples = 0
+    for f in range(frames):
+        pg.render(pc, hy.camera_orbit((3.0 * f, 30.0, 2.2)), res, res, out.data_ptr())
+        samples += ctx.stats().samples
     lookups = d["hits"] + d["misses"]
     outj = {
         "metric": "frames/s", "value": frames / wall, "unit": "frames/s", "n_gpus": 1,

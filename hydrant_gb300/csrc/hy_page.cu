@@ -525,7 +525,8 @@ struct CullArgs {
     float norm[4][3];
     float rdir[4][3];  // 1 / normalize(border[i])
     float orig[3];
-    const int2 *info;
+    const int *cheb;  // chebyshev value of brick b at cheb[b * cheb_stride]
+    int cheb_stride;
     int gx, gy, gz;
     int *ids;
     float *d2;
@@ -543,7 +544,7 @@ __device__ __forceinline__ bool frustum_contains(const CullArgs &a, float x, flo
 __global__ void cull_kernel(const __grid_constant__ CullArgs a) {
     const int id = blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= a.gx * a.gy * a.gz) return;
-    if (a.info[id].x != 0) return;
+    if (a.cheb[size_t(id) * a.cheb_stride] != 0) return;
     const int x = id % a.gx, y = (id / a.gx) % a.gy, z = id / (a.gx * a.gy);
     const float x0 = float(x), y0 = float(y), z0 = float(z);
     const float x1 = float(x + 1), y1 = float(y + 1), z1 = float(z + 1);
@@ -599,9 +600,13 @@ struct CullScratch {
     int cap = 0;
 };
 
+// Culls on `stream` (default: the context's); the chebyshev values come
+// from the volume's page table unless `cheb` (one int per brick) is given.
 int run_cull(hy_ctx *ctx, const hy_volume *vol, const hy_view &view, const float rect_in[4],
              int limit, CullScratch &cs, std::vector<int> &ids, std::vector<float> &d2,
-             std::vector<int> *all_visible = nullptr) {
+             std::vector<int> *all_visible = nullptr, cudaStream_t stream = nullptr,
+             const int *cheb = nullptr) {
+    if (!stream) stream = ctx->stream;
     const float def_rect[4] = {-1.f, -1.f, 1.f, 1.f};
     const float *rect = rect_in ? rect_in : def_rect;
     if (cs.cap < vol->nbricks) {
@@ -616,27 +621,28 @@ int run_cull(hy_ctx *ctx, const hy_volume *vol, const hy_view &view, const float
     }
     CullArgs a;
     host_frustum(view, rect, a);
-    a.info = vol->info_dev;
+    a.cheb = cheb ? cheb : reinterpret_cast<const int *>(vol->info_dev);
+    a.cheb_stride = cheb ? 1 : 2;
     a.gx = vol->grid[0];
     a.gy = vol->grid[1];
     a.gz = vol->grid[2];
     a.ids = cs.ids;
     a.d2 = cs.d2;
     a.count = cs.count;
-    HY_CUDA(ctx, cudaMemsetAsync(cs.count, 0, sizeof(unsigned int), ctx->stream));
-    cull_kernel<<<(vol->nbricks + 255) / 256, 256, 0, ctx->stream>>>(a);
+    HY_CUDA(ctx, cudaMemsetAsync(cs.count, 0, sizeof(unsigned int), stream));
+    cull_kernel<<<(vol->nbricks + 255) / 256, 256, 0, stream>>>(a);
     HY_CUDA(ctx, cudaGetLastError());
     unsigned int n = 0;
-    HY_CUDA(ctx, cudaMemcpyAsync(&n, cs.count, sizeof(n), cudaMemcpyDeviceToHost, ctx->stream));
-    HY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    HY_CUDA(ctx, cudaMemcpyAsync(&n, cs.count, sizeof(n), cudaMemcpyDeviceToHost, stream));
+    HY_CUDA(ctx, cudaStreamSynchronize(stream));
     std::vector<int> hid(n);
     std::vector<float> hd(n);
     if (n) {
         HY_CUDA(ctx, cudaMemcpyAsync(hid.data(), cs.ids, n * sizeof(int), cudaMemcpyDeviceToHost,
-                                     ctx->stream));
+                                     stream));
         HY_CUDA(ctx, cudaMemcpyAsync(hd.data(), cs.d2, n * sizeof(float), cudaMemcpyDeviceToHost,
-                                     ctx->stream));
-        HY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+                                     stream));
+        HY_CUDA(ctx, cudaStreamSynchronize(stream));
     }
     if (all_visible) *all_visible = hid;
     std::vector<int> idx(n);
@@ -706,6 +712,13 @@ struct hy_pager {
     int reg_base = 0;
     int next_free = 0;           // realtime: slots never used yet
     int2 *info_stage[2] = {nullptr, nullptr};  // pinned staging of the page table
+    // realtime frames overlap: a frame culls on its own stream, from a copy
+    // of the chebyshev values, while the previous frame still renders; its
+    // uploads into slots that frame may read wait for `rendered`
+    cudaStream_t cull_stream = nullptr;
+    cudaEvent_t rendered = nullptr;
+    int *cheb_dev = nullptr;
+    int frame_buf = 0;           // page-table staging buffer of the next frame
     CullScratch cs;
     void *film = nullptr;
     size_t film_bytes = 0;
@@ -806,6 +819,13 @@ extern "C" int hy_pager_create(hy_ctx *ctx, hy_store *store, const hy_pager_desc
     }
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&pg->copy, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&pg->copied, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&pg->cull_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&pg->rendered, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaMalloc(&pg->cheb_dev, v->nbricks * sizeof(int));
+    if (e == cudaSuccess)
+        e = cudaMemcpy(pg->cheb_dev, v->cheb.data(), v->nbricks * sizeof(int),
+                       cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaEventRecord(pg->rendered, ctx->stream);
     if (e != cudaSuccess) return fail(hy_cuda_fail(ctx, e, "pager: allocation"));
     std::vector<RegEntry> reg(nreg);
     if (pg->coarse) {
@@ -857,6 +877,12 @@ extern "C" int hy_pager_destroy(hy_pager *pg) {
         cudaStreamDestroy(pg->copy);
     }
     if (pg->copied) cudaEventDestroy(pg->copied);
+    if (pg->cull_stream) {
+        cudaStreamSynchronize(pg->cull_stream);
+        cudaStreamDestroy(pg->cull_stream);
+    }
+    if (pg->rendered) cudaEventDestroy(pg->rendered);
+    if (pg->cheb_dev) cudaFree(pg->cheb_dev);
     for (int i = 0; i < 2; ++i) {
         if (pg->marched[i]) cudaEventDestroy(pg->marched[i]);
         if (pg->staged[i]) cudaEventDestroy(pg->staged[i]);
@@ -1001,7 +1027,8 @@ int render_realtime(hy_pager *pg, const hy_shader_params *p, const hy_view &view
     hy_volume *v = pg->vol;
     std::vector<int> req, visible;
     std::vector<float> d2;
-    int rc = run_cull(ctx, v, view, nullptr, pg->nslots, pg->cs, req, d2, &visible);
+    int rc = run_cull(ctx, v, view, nullptr, pg->nslots, pg->cs, req, d2, &visible,
+                      pg->cull_stream, pg->cheb_dev);
     if (rc) return rc;
     std::vector<char> required(v->nbricks, 0);
     for (int b : req) required[b] = 1;
@@ -1017,10 +1044,13 @@ int render_realtime(hy_pager *pg, const hy_shader_params *p, const hy_view &view
     pg->stats.misses += int64_t(missing.size());
     const int budget = pg->desc.max_uploads_per_frame > 0 ? pg->desc.max_uploads_per_frame
                                                            : int(missing.size());
-    std::vector<int> bricks, slots;
-    for (int i = 0; i < int(missing.size()) && int(bricks.size()) < budget; ++i) {
+    // fresh slots: nothing reads them; reused slots: the previous frame may
+    std::vector<int> fresh_b, fresh_s, reused_b, reused_s;
+    for (int i = 0; i < int(missing.size()) && int(fresh_b.size() + reused_b.size()) < budget;
+         ++i) {
         const int b = missing[i].second;
         int slot;
+        bool reused = false;
         if (pg->next_free < pg->nslots) {
             slot = pg->next_free++;
         } else if (!redundant.empty()) {
@@ -1029,20 +1059,27 @@ int render_realtime(hy_pager *pg, const hy_shader_params *p, const hy_view &view
             slot = pg->page[old];
             pg->page[old] = -1;
             ++pg->stats.evictions;
+            reused = true;
         } else {
             break;  // no slot: the brick stays absent this frame
         }
         pg->owner[slot] = b;
         pg->page[b] = slot;
-        bricks.push_back(b);
-        slots.push_back(slot);
+        (reused ? reused_b : fresh_b).push_back(b);
+        (reused ? reused_s : fresh_s).push_back(slot);
     }
-    rc = upload_bricks(pg, bricks.data(), slots.data(), int(bricks.size()));
+    rc = upload_bricks(pg, fresh_b.data(), fresh_s.data(), int(fresh_b.size()));
     if (rc) return rc;
+    if (!reused_b.empty()) {
+        HY_CUDA(ctx, cudaStreamWaitEvent(pg->copy, pg->rendered, 0));
+        rc = upload_bricks(pg, reused_b.data(), reused_s.data(), int(reused_b.size()));
+        if (rc) return rc;
+    }
     HY_CUDA(ctx, cudaEventRecord(pg->copied, pg->copy));
     HY_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, pg->copied, 0));
-    rc = upload_page_table(pg);
+    rc = upload_page_table(pg, pg->frame_buf);
     if (rc) return rc;
+    pg->frame_buf ^= 1;
     int resident = 0;
     for (int s = 0; s < pg->nslots; ++s) resident += pg->owner[s] >= 0;
     v->resident = resident;
@@ -1052,7 +1089,10 @@ int render_realtime(hy_pager *pg, const hy_shader_params *p, const hy_view &view
         for (int b : visible) fallback += pg->page[b] < 0;
     pg->stats.fallback = fallback;
     ++pg->stats.passes;
-    return hy_render_device(ctx, v, p, &view, W, H, rgba_dev, nullptr, nullptr);
+    rc = hy_render_device(ctx, v, p, &view, W, H, rgba_dev, nullptr, nullptr);
+    if (rc) return rc;
+    HY_CUDA(ctx, cudaEventRecord(pg->rendered, ctx->stream));
+    return HY_OK;
 }
 
 }  // namespace

@@ -269,12 +269,14 @@ __device__ __forceinline__ bool unit_interval(float l) { return __float_as_uint(
 struct BrickCursor {
     float ipx, ipy, ipz;
     int cur, cd, pg;
+    bool sample;  // cd == 0 && pg != -1: the cell is sampled (one test per step)
     BrickRef br;
     __device__ __forceinline__ void reset() {
         ipx = ipy = ipz = __int_as_float(0x7f800000);
         cur = -1;
         cd = 0;
         pg = -1;
+        sample = false;
         br = BrickRef{};
     }
     // o's cell changed (or may have): redo floor(o) and the thumbnail lookups
@@ -289,6 +291,7 @@ struct BrickCursor {
             const int2 in = __ldg(&V.info[bid]);
             cd = in.x;
             pg = in.y;
+            sample = cd == 0 && pg != -1;
             if (cd == 0 && pg >= 0) br = load_brick(V, pg);
         }
     }
@@ -336,11 +339,11 @@ struct VolumeMarch {
         const DevVolume &V = A.vol;
         float lx, ly, lz;
         c.update(V, p.ox, p.oy, p.oz, lx, ly, lz);
-        if (c.cd) {
+        if (!c.sample) {
+            if (c.cd == 0) return false;  // absent brick (pg == -1)
             p.nsteps -= skip_nblock_steps(p, rx, ry, rz, c.ipx, c.ipy, c.ipz, c.cd, cdu,
                                           A.step * float(p.step_size));
         } else {
-            if (c.pg == -1) return false;
             float s = sample_brick<PC, DT, PADDED>(c.br, V.P, lx, ly, lz, S.lut);
             ++samples;
             float4 ub = sample_tf(S.tf, S.ntf, S.fntf, s);
