@@ -132,7 +132,8 @@ struct hy_store {
     std::vector<int> cheb;
     std::vector<float> mean;
     std::vector<long long> offset;  // brick -> byte offset in `host`, -1 if empty
-    unsigned char *host = nullptr;  // pinned
+    unsigned char *host = nullptr;  // pinned, mapped into the device address space
+    const unsigned char *host_dev = nullptr;  // the same memory as the device sees it
     size_t host_bytes = 0;
     int nonempty = 0;
     // coarse level (0: none): every coarse brick, slot_stride apart

@@ -70,7 +70,10 @@ int hy_store_alloc(hy_store *s, int nonempty) {
     s->nonempty = nonempty;
     s->host_bytes = std::max<size_t>(1, size_t(nonempty)) * s->slot_stride;
     HY_CUDA(s->ctx, cudaHostAlloc(reinterpret_cast<void **>(&s->host), s->host_bytes,
-                                  cudaHostAllocDefault));
+                                  cudaHostAllocMapped | cudaHostAllocPortable));
+    void *dev = nullptr;
+    HY_CUDA(s->ctx, cudaHostGetDevicePointer(&dev, s->host, 0));
+    s->host_dev = static_cast<const unsigned char *>(dev);
     return HY_OK;
 }
 
@@ -692,6 +695,31 @@ extern "C" int hy_cull(const hy_volume *vol, const hy_view *view, const float re
 // ---------------------------------------------------------------------------
 // Pager
 // ---------------------------------------------------------------------------
+namespace {
+
+// One brick move of a realtime frame: store bytes at `src` -> cache slot `dst`.
+struct GatherItem {
+    long long src;
+    int dst;
+    int pad_;
+};
+
+// One block per brick: the slot is filled straight from the mapped pinned
+// store (the GPU reads host memory over the C2C link), 16 bytes per thread
+// and iteration; slot_stride is a multiple of 256 bytes.
+__global__ void gather_bricks_kernel(const unsigned char *__restrict__ store,
+                                     const GatherItem *__restrict__ items,
+                                     unsigned char *__restrict__ pool, long long slot0,
+                                     long long stride) {
+    const GatherItem it = items[blockIdx.x];
+    const uint4 *src = reinterpret_cast<const uint4 *>(store + it.src);
+    uint4 *dst = reinterpret_cast<uint4 *>(pool + (slot0 + it.dst) * stride);
+    const int n = int(stride / 16);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src[i];
+}
+
+}  // namespace
+
 struct hy_pager {
     hy_ctx *ctx = nullptr;
     hy_store *store = nullptr;
@@ -719,6 +747,8 @@ struct hy_pager {
     cudaEvent_t rendered = nullptr;
     int *cheb_dev = nullptr;
     int frame_buf = 0;           // page-table staging buffer of the next frame
+    GatherItem *gather_stage[2] = {nullptr, nullptr};  // pinned: a frame's brick moves
+    GatherItem *gather_dev = nullptr;
     CullScratch cs;
     void *film = nullptr;
     size_t film_bytes = 0;
@@ -826,6 +856,10 @@ extern "C" int hy_pager_create(hy_ctx *ctx, hy_store *store, const hy_pager_desc
         e = cudaMemcpy(pg->cheb_dev, v->cheb.data(), v->nbricks * sizeof(int),
                        cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaEventRecord(pg->rendered, ctx->stream);
+    for (int i = 0; i < 2 && e == cudaSuccess; ++i)
+        e = cudaHostAlloc(reinterpret_cast<void **>(&pg->gather_stage[i]),
+                          pg->nslots * sizeof(GatherItem), cudaHostAllocDefault);
+    if (e == cudaSuccess) e = cudaMalloc(&pg->gather_dev, pg->nslots * sizeof(GatherItem));
     if (e != cudaSuccess) return fail(hy_cuda_fail(ctx, e, "pager: allocation"));
     std::vector<RegEntry> reg(nreg);
     if (pg->coarse) {
@@ -883,6 +917,9 @@ extern "C" int hy_pager_destroy(hy_pager *pg) {
     }
     if (pg->rendered) cudaEventDestroy(pg->rendered);
     if (pg->cheb_dev) cudaFree(pg->cheb_dev);
+    for (int i = 0; i < 2; ++i)
+        if (pg->gather_stage[i]) cudaFreeHost(pg->gather_stage[i]);
+    if (pg->gather_dev) cudaFree(pg->gather_dev);
     for (int i = 0; i < 2; ++i) {
         if (pg->marched[i]) cudaEventDestroy(pg->marched[i]);
         if (pg->staged[i]) cudaEventDestroy(pg->staged[i]);
@@ -1068,15 +1105,33 @@ int render_realtime(hy_pager *pg, const hy_shader_params *p, const hy_view &view
         (reused ? reused_b : fresh_b).push_back(b);
         (reused ? reused_s : fresh_s).push_back(slot);
     }
-    rc = upload_bricks(pg, fresh_b.data(), fresh_s.data(), int(fresh_b.size()));
-    if (rc) return rc;
-    if (!reused_b.empty()) {
-        HY_CUDA(ctx, cudaStreamWaitEvent(pg->copy, pg->rendered, 0));
-        rc = upload_bricks(pg, reused_b.data(), reused_s.data(), int(reused_b.size()));
-        if (rc) return rc;
+    // one gather kernel on the render stream moves every brick of the frame:
+    // it runs after the previous frame's render, so reused slots are free
+    const int nmove = int(fresh_b.size() + reused_b.size());
+    if (nmove) {
+        const int buf = pg->frame_buf;
+        HY_CUDA(ctx, cudaEventSynchronize(pg->staged[buf]));  // last use of this staging
+        GatherItem *items = pg->gather_stage[buf];
+        int k = 0;
+        for (int pass = 0; pass < 2; ++pass) {
+            const std::vector<int> &bs = pass ? reused_b : fresh_b;
+            const std::vector<int> &ss = pass ? reused_s : fresh_s;
+            for (size_t i = 0; i < bs.size(); ++i) {
+                const long long off = pg->store->offset[bs[i]];
+                if (off < 0 || off + (long long)v->slot_stride > (long long)pg->store->host_bytes ||
+                    ss[i] < 0 || ss[i] >= pg->nslots)
+                    return hy_fail(ctx, HY_ERR_STATE, "pager: brick move out of range");
+                items[k++] = GatherItem{off, ss[i], 0};
+            }
+        }
+        HY_CUDA(ctx, cudaMemcpyAsync(pg->gather_dev, items, nmove * sizeof(GatherItem),
+                                     cudaMemcpyHostToDevice, ctx->stream));
+        gather_bricks_kernel<<<nmove, 256, 0, ctx->stream>>>(
+            pg->store->host_dev, pg->gather_dev, v->pool, pg->ncoarse, (long long)v->slot_stride);
+        HY_CUDA(ctx, cudaGetLastError());
+        pg->stats.uploads += nmove;
+        pg->stats.upload_bytes += (int64_t)nmove * (int64_t)pg->store->slot_stride;
     }
-    HY_CUDA(ctx, cudaEventRecord(pg->copied, pg->copy));
-    HY_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, pg->copied, 0));
     rc = upload_page_table(pg, pg->frame_buf);
     if (rc) return rc;
     pg->frame_buf ^= 1;
