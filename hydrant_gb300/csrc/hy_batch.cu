@@ -227,7 +227,7 @@ struct hy_batch {
 namespace {
 
 // Dynamic shared memory above the default 48 KiB needs an opt-in per kernel.
-// (The driver's default L1 / shared-memory split is kept: asking for the
+// (The CUDA runtime's default L1 / shared-memory split is kept: asking for the
 // largest L1 left too little shared memory for the resident blocks.)
 cudaError_t allow_smem(const void *kernel, size_t smem) {
     if (smem <= 48 * 1024) return cudaSuccess;
