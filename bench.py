@@ -61,6 +61,10 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--coarse-level", type=int, default=3,
                     help="paging: coarse fallback level (box filter 2**L; 0 = none)")
+    ap.add_argument("--pager", choices=["realtime", "lossless"], default="realtime",
+                    help="paging: the realtime cache or lossless batches (offline frames)")
+    ap.add_argument("--lossless-batch", type=int, default=4096,
+                    help="paging, lossless: bricks per batch (the reference caps it at 4096)")
     ap.add_argument("--max-uploads", type=int, default=0,
                     help="paging: brick uploads per frame (0 = every missing brick)")
     ap.add_argument("--launch-shape", default="",
@@ -507,8 +511,12 @@ def main_paging(args):
         store.build_coarse(args.coarse_level)
     t_coarse = time.perf_counter() - t1
     si = store.info
-    slots = int((8 * 2**30) // si.slot_bytes)
-    pg = hy.Pager(ctx, store, slots, _abi.PAGER_REALTIME, args.max_uploads)
+    if args.pager == "lossless":
+        slots = args.lossless_batch
+        pg = hy.Pager(ctx, store, slots, _abi.PAGER_LOSSLESS)
+    else:
+        slots = int((8 * 2**30) // si.slot_bytes)
+        pg = hy.Pager(ctx, store, slots, _abi.PAGER_REALTIME, args.max_uploads)
     p = hy.shader_params(shader="Volume", sample_rate=0.25, density=5e-3)
     pc = hy.shader_params(shader="Volume", sample_rate=0.25, density=5e-3, count_samples=True)
     out = torch.empty(res * res * 4, dtype=torch.uint8, device=f"cuda:{local}")
@@ -550,7 +558,8 @@ def main_paging(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
         "config": {"workload": f"paging_{dim[0]}x{dim[1]}x{dim[2]}_{res}px", "block_size": 64,
-                   "cache_gib": 8, "cache_slots": slots, "store_bricks": si.nonempty,
+                   "pager": args.pager, "cache_gib": 8 if args.pager == "realtime" else None,
+                   "cache_slots": slots, "store_bricks": si.nonempty,
                    "store_gb": si.pool_bytes / 1e9, "store_build_s": t_store,
                    "coarse_level": args.coarse_level, "coarse_build_s": t_coarse,
                    "max_uploads_per_frame": args.max_uploads},
@@ -559,6 +568,7 @@ def main_paging(args):
         "gpu_s": gpu_s, "wall_s": wall,
         "cache_hit_rate": (d["hits"] / lookups) if lookups else None,
         "uploads_per_frame": d["uploads"] / frames,
+        "passes_per_frame": d["passes"] / frames,
         "upload_gb_per_s": d["upload_bytes"] / wall / 1e9,
         "evictions": d["evictions"], "visible_last_frame": st["visible"],
         "coarse_bricks_per_frame": fallback / frames,

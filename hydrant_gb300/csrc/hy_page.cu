@@ -741,14 +741,15 @@ struct hy_pager {
     int next_free = 0;           // realtime: slots never used yet
     int2 *info_stage[2] = {nullptr, nullptr};  // pinned staging of the page table
     // realtime frames overlap: a frame culls on its own stream, from a copy
-    // of the chebyshev values, while the previous frame still renders; its
-    // uploads into slots that frame may read wait for `rendered`
+    // of the chebyshev values, while the previous frame still renders
     cudaStream_t cull_stream = nullptr;
-    cudaEvent_t rendered = nullptr;
     int *cheb_dev = nullptr;
     int frame_buf = 0;           // page-table staging buffer of the next frame
-    GatherItem *gather_stage[2] = {nullptr, nullptr};  // pinned: a frame's brick moves
+    // brick moves: two pinned staging lists, their device copies (nslots
+    // items each) and the event after each list's upload
+    GatherItem *gather_stage[2] = {nullptr, nullptr};
     GatherItem *gather_dev = nullptr;
+    cudaEvent_t gathered[2] = {nullptr, nullptr};
     CullScratch cs;
     void *film = nullptr;
     size_t film_bytes = 0;
@@ -787,16 +788,32 @@ int upload_page_table(hy_pager *pg, int buf = 0) {
 }
 
 // Upload bricks into slots on the copy stream; returns after queuing.
-int upload_bricks(hy_pager *pg, const int *bricks, const int *slots, int n) {
+// Moves n bricks from the store into cache slots with one gather kernel on
+// `stream`: the list goes through staging list `buf` (reused only after its
+// previous upload ran), the kernel reads the mapped pinned store directly.
+int move_bricks(hy_pager *pg, const int *bricks, const int *slots, int n, cudaStream_t stream,
+                int buf) {
+    if (n == 0) return HY_OK;
     hy_ctx *ctx = pg->ctx;
+    hy_volume *v = pg->vol;
+    if (n > pg->nslots) return hy_fail(ctx, HY_ERR_STATE, "pager: more moves than slots");
+    HY_CUDA(ctx, cudaEventSynchronize(pg->gathered[buf]));
+    GatherItem *items = pg->gather_stage[buf];
     for (int i = 0; i < n; ++i) {
         const long long off = pg->store->offset[bricks[i]];
         if (off < 0) return hy_fail(ctx, HY_ERR_INVALID, "pager: empty brick requested");
-        HY_CUDA(ctx, cudaMemcpyAsync(pg->vol->pool +
-                                         size_t(pg->ncoarse + slots[i]) * pg->vol->slot_stride,
-                                     pg->store->host + off, pg->store->slot_stride,
-                                     cudaMemcpyHostToDevice, pg->copy));
+        if (off + (long long)v->slot_stride > (long long)pg->store->host_bytes || slots[i] < 0 ||
+            slots[i] >= pg->nslots)
+            return hy_fail(ctx, HY_ERR_STATE, "pager: brick move out of range");
+        items[i] = GatherItem{off, slots[i], 0};
     }
+    GatherItem *dev = pg->gather_dev + size_t(buf) * pg->nslots;
+    HY_CUDA(ctx, cudaMemcpyAsync(dev, items, n * sizeof(GatherItem), cudaMemcpyHostToDevice,
+                                 stream));
+    HY_CUDA(ctx, cudaEventRecord(pg->gathered[buf], stream));
+    gather_bricks_kernel<<<n, 256, 0, stream>>>(pg->store->host_dev, dev, v->pool, pg->ncoarse,
+                                                (long long)v->slot_stride);
+    HY_CUDA(ctx, cudaGetLastError());
     pg->stats.uploads += n;
     pg->stats.upload_bytes += (int64_t)n * (int64_t)pg->store->slot_stride;
     return HY_OK;
@@ -850,16 +867,16 @@ extern "C" int hy_pager_create(hy_ctx *ctx, hy_store *store, const hy_pager_desc
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&pg->copy, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&pg->copied, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&pg->cull_stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&pg->rendered, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc(&pg->cheb_dev, v->nbricks * sizeof(int));
     if (e == cudaSuccess)
         e = cudaMemcpy(pg->cheb_dev, v->cheb.data(), v->nbricks * sizeof(int),
                        cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaEventRecord(pg->rendered, ctx->stream);
     for (int i = 0; i < 2 && e == cudaSuccess; ++i)
         e = cudaHostAlloc(reinterpret_cast<void **>(&pg->gather_stage[i]),
                           pg->nslots * sizeof(GatherItem), cudaHostAllocDefault);
-    if (e == cudaSuccess) e = cudaMalloc(&pg->gather_dev, pg->nslots * sizeof(GatherItem));
+    if (e == cudaSuccess) e = cudaMalloc(&pg->gather_dev, 2 * pg->nslots * sizeof(GatherItem));
+    for (int i = 0; i < 2 && e == cudaSuccess; ++i)
+        e = cudaEventCreateWithFlags(&pg->gathered[i], cudaEventDisableTiming);
     if (e != cudaSuccess) return fail(hy_cuda_fail(ctx, e, "pager: allocation"));
     std::vector<RegEntry> reg(nreg);
     if (pg->coarse) {
@@ -915,11 +932,12 @@ extern "C" int hy_pager_destroy(hy_pager *pg) {
         cudaStreamSynchronize(pg->cull_stream);
         cudaStreamDestroy(pg->cull_stream);
     }
-    if (pg->rendered) cudaEventDestroy(pg->rendered);
     if (pg->cheb_dev) cudaFree(pg->cheb_dev);
     for (int i = 0; i < 2; ++i)
         if (pg->gather_stage[i]) cudaFreeHost(pg->gather_stage[i]);
     if (pg->gather_dev) cudaFree(pg->gather_dev);
+    for (int i = 0; i < 2; ++i)
+        if (pg->gathered[i]) cudaEventDestroy(pg->gathered[i]);
     for (int i = 0; i < 2; ++i) {
         if (pg->marched[i]) cudaEventDestroy(pg->marched[i]);
         if (pg->staged[i]) cudaEventDestroy(pg->staged[i]);
@@ -1013,7 +1031,7 @@ int render_lossless(hy_pager *pg, const hy_shader_params *p, const hy_camera *ca
         }
         // this half of the cache is free once the pass of batch k-2 has run
         HY_CUDA(ctx, cudaStreamWaitEvent(pg->copy, pg->marched[half], 0));
-        int r = upload_bricks(pg, bricks.data(), slots.data(), int(bricks.size()));
+        int r = move_bricks(pg, bricks.data(), slots.data(), int(bricks.size()), pg->copy, half);
         if (r) return r;
         HY_CUDA(ctx, cudaEventRecord(pg->copied, pg->copy));
         return HY_OK;
@@ -1081,13 +1099,10 @@ int render_realtime(hy_pager *pg, const hy_shader_params *p, const hy_view &view
     pg->stats.misses += int64_t(missing.size());
     const int budget = pg->desc.max_uploads_per_frame > 0 ? pg->desc.max_uploads_per_frame
                                                            : int(missing.size());
-    // fresh slots: nothing reads them; reused slots: the previous frame may
-    std::vector<int> fresh_b, fresh_s, reused_b, reused_s;
-    for (int i = 0; i < int(missing.size()) && int(fresh_b.size() + reused_b.size()) < budget;
-         ++i) {
+    std::vector<int> move_b, move_s;
+    for (int i = 0; i < int(missing.size()) && int(move_b.size()) < budget; ++i) {
         const int b = missing[i].second;
         int slot;
-        bool reused = false;
         if (pg->next_free < pg->nslots) {
             slot = pg->next_free++;
         } else if (!redundant.empty()) {
@@ -1096,42 +1111,19 @@ int render_realtime(hy_pager *pg, const hy_shader_params *p, const hy_view &view
             slot = pg->page[old];
             pg->page[old] = -1;
             ++pg->stats.evictions;
-            reused = true;
         } else {
             break;  // no slot: the brick stays absent this frame
         }
         pg->owner[slot] = b;
         pg->page[b] = slot;
-        (reused ? reused_b : fresh_b).push_back(b);
-        (reused ? reused_s : fresh_s).push_back(slot);
+        move_b.push_back(b);
+        move_s.push_back(slot);
     }
     // one gather kernel on the render stream moves every brick of the frame:
     // it runs after the previous frame's render, so reused slots are free
-    const int nmove = int(fresh_b.size() + reused_b.size());
-    if (nmove) {
-        const int buf = pg->frame_buf;
-        HY_CUDA(ctx, cudaEventSynchronize(pg->staged[buf]));  // last use of this staging
-        GatherItem *items = pg->gather_stage[buf];
-        int k = 0;
-        for (int pass = 0; pass < 2; ++pass) {
-            const std::vector<int> &bs = pass ? reused_b : fresh_b;
-            const std::vector<int> &ss = pass ? reused_s : fresh_s;
-            for (size_t i = 0; i < bs.size(); ++i) {
-                const long long off = pg->store->offset[bs[i]];
-                if (off < 0 || off + (long long)v->slot_stride > (long long)pg->store->host_bytes ||
-                    ss[i] < 0 || ss[i] >= pg->nslots)
-                    return hy_fail(ctx, HY_ERR_STATE, "pager: brick move out of range");
-                items[k++] = GatherItem{off, ss[i], 0};
-            }
-        }
-        HY_CUDA(ctx, cudaMemcpyAsync(pg->gather_dev, items, nmove * sizeof(GatherItem),
-                                     cudaMemcpyHostToDevice, ctx->stream));
-        gather_bricks_kernel<<<nmove, 256, 0, ctx->stream>>>(
-            pg->store->host_dev, pg->gather_dev, v->pool, pg->ncoarse, (long long)v->slot_stride);
-        HY_CUDA(ctx, cudaGetLastError());
-        pg->stats.uploads += nmove;
-        pg->stats.upload_bytes += (int64_t)nmove * (int64_t)pg->store->slot_stride;
-    }
+    rc = move_bricks(pg, move_b.data(), move_s.data(), int(move_b.size()), ctx->stream,
+                     pg->frame_buf);
+    if (rc) return rc;
     rc = upload_page_table(pg, pg->frame_buf);
     if (rc) return rc;
     pg->frame_buf ^= 1;
@@ -1144,10 +1136,7 @@ int render_realtime(hy_pager *pg, const hy_shader_params *p, const hy_view &view
         for (int b : visible) fallback += pg->page[b] < 0;
     pg->stats.fallback = fallback;
     ++pg->stats.passes;
-    rc = hy_render_device(ctx, v, p, &view, W, H, rgba_dev, nullptr, nullptr);
-    if (rc) return rc;
-    HY_CUDA(ctx, cudaEventRecord(pg->rendered, ctx->stream));
-    return HY_OK;
+    return hy_render_device(ctx, v, p, &view, W, H, rgba_dev, nullptr, nullptr);
 }
 
 }  // namespace
