@@ -166,7 +166,9 @@ int hy_stage(hy_ctx *ctx, size_t bytes, void **out);
 
 // launchers (hy_render.cu)
 int hy_launch_render(hy_ctx *ctx, const hy::ShadeArgs &args);
-int hy_launch_pass(hy_ctx *ctx, const hy::ShadeArgs &args, int pass);
+// reset_counter = false: the sample counter keeps counting from the previous
+// passes (a pager frame made of several passes)
+int hy_launch_pass(hy_ctx *ctx, const hy::ShadeArgs &args, int pass, bool reset_counter = true);
 int hy_finish_stats(hy_ctx *ctx);
 int hy_fill_args(hy_ctx *ctx, const hy_volume *vol, const hy_shader_params *p, const hy_view *view,
                  int W, int H, hy::ShadeArgs *a);

@@ -1019,7 +1019,10 @@ int render_lossless(hy_pager *pg, const hy_shader_params *p, const hy_camera *ca
     rc = hy_fill_args(ctx, v, p, &view, W, H, &a);
     if (rc) return rc;
     a.film = pg->film;
-    a.count = 0;
+    // samples of the whole frame: the counter is cleared once, the passes add
+    a.count = p->count_samples ? 1 : 0;
+    if (a.count)
+        HY_CUDA(ctx, cudaMemsetAsync(ctx->counter_dev, 0, sizeof(unsigned long long), ctx->stream));
     std::vector<int> bricks, slots;
     auto queue_batch = [&](int k) -> int {
         bricks.clear();
@@ -1049,7 +1052,7 @@ int render_lossless(hy_pager *pg, const hy_shader_params *p, const hy_camera *ca
         for (size_t i = 0; i < cur.size(); ++i) pg->page[cur[i]] = cur_slots[i];
         rc = upload_page_table(pg, k & 1);
         if (rc) return rc;
-        rc = hy_launch_pass(ctx, a, k == 0 ? HY_PASS_RAY_EMIT : HY_PASS_RAY_MARCH);
+        rc = hy_launch_pass(ctx, a, k == 0 ? HY_PASS_RAY_EMIT : HY_PASS_RAY_MARCH, false);
         if (rc) return rc;
         HY_CUDA(ctx, cudaEventRecord(pg->marched[k & 1], ctx->stream));
         ++pg->stats.passes;

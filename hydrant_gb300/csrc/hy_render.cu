@@ -372,8 +372,8 @@ int hy_launch_render(hy_ctx *ctx, const ShadeArgs &a) {
     return HY_OK;
 }
 
-int hy_launch_pass(hy_ctx *ctx, const ShadeArgs &a, int pass) {
-    if (a.count && pass <= HY_PASS_RAY_MARCH)
+int hy_launch_pass(hy_ctx *ctx, const ShadeArgs &a, int pass, bool reset_counter) {
+    if (reset_counter && a.count && pass <= HY_PASS_RAY_MARCH)
         HY_CUDA(ctx, cudaMemsetAsync(ctx->counter_dev, 0, sizeof(unsigned long long), ctx->stream));
     HY_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
     switch (a.shader) {

@@ -80,16 +80,19 @@ def _oracle_lossless(ov, tf, op, c10, v20, W, H, B):
     order = orc.lossless_order(ov, c10, ids)
     batches = [order[i:i + B] for i in range(0, len(order), B)] or [order[:0]]
     film = None
+    samples = 0
     for k, batch in enumerate(batches):
         ov.set_present(orc.present_mask(ov, batch))
         if k == 0:
-            film = orc.render(ov, tf, op, v20, W, H, want_film=True)["film"]
+            r = orc.render(ov, tf, op, v20, W, H, want_film=True)
+            film = r["film"]
+            samples += r["samples"]
         else:
-            orc.march_film(ov, tf, op, film, W, H)
+            samples += orc.march_film(ov, tf, op, film, W, H)
     ov.set_present(np.ones(ov.grid[0] * ov.grid[1] * ov.grid[2], np.uint8))
     fb = film.shape[-1] // 4
     v = film.view(np.float32).reshape(H, W, fb)[..., 8:12]
-    return write_to(v), len(batches)
+    return write_to(v), len(batches), samples
 
 
 @pytest.mark.parametrize("shader", ["Volume", "Isosurface", "Blocks"])
@@ -102,7 +105,8 @@ def test_lossless_pager_matches_oracle(ctx, tubes, shader, slots):
         W, H = 72, 56
         for cam in CAMS[:3]:
             c = wl.make_camera(wl.Camera(cam[0], cam[1]))
-            p = hy.shader_params(shader=shader, density=0.4, sample_rate=0.5, isovalue=0.5)
+            p = hy.shader_params(shader=shader, density=0.4, sample_rate=0.5, isovalue=0.5,
+                                 count_samples=True)
             if shader == "Isosurface":
                 hy.iso_lighting(vol, c, p)
             out = torch.zeros(W * H * 4, dtype=torch.uint8, device="cuda")
@@ -110,9 +114,12 @@ def test_lossless_pager_matches_oracle(ctx, tubes, shader, slots):
             ctx.synchronize()
             got = out.cpu().numpy().reshape(H, W, 4)
             view = view_array(hy.camera_view(vol, c))
-            ref, nb = _oracle_lossless(ov, wl.TF9, orc.params_from(p), cam10(c), view, W, H, slots)
+            ref, nb, ref_samples = _oracle_lossless(ov, wl.TF9, orc.params_from(p), cam10(c), view,
+                                                    W, H, slots)
             d = np.abs(got.astype(int) - ref.astype(int))
             assert d.max() <= 1, f"{shader} {cam}: {d.max()} LSB"
+            # the frame's samples, summed over its passes, as in the batch replay
+            assert ctx.stats().samples == ref_samples, f"{shader} {cam}: samples"
         st = pg.stats()
         if slots == 25:
             assert st["passes"] > st["frames"]  # several batches per frame
