@@ -396,7 +396,9 @@ def main_ours(args):
         torch.distributed.barrier()
 
     # ---- e2e: the host-buffer entry point (device -> host images per step) --
-    host = np.empty(batch.nbytes, np.uint8)
+    # pinned host output (the images' destination in a serving process)
+    host_t = torch.empty(batch.nbytes, dtype=torch.uint8, pin_memory=True)
+    host = host_t.numpy()
     for _ in range(max(1, args.warmup // 2)):
         batch.render()
     if ws > 1:
@@ -460,7 +462,7 @@ def main_ours(args):
             "e2e": {"value": e2e, "unit": "Gsamples/s",
                     "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": batch.nbytes,
-                    "path": "hy_batch_render (host output buffer)"},
+                    "path": "hy_batch_render (pinned host output buffer)"},
             "roofline": {
                 "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": achieved / hbm, "peak_kind": peak_kind,
