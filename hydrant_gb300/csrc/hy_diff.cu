@@ -325,18 +325,9 @@ __device__ __forceinline__ void diff_adjoint_sample(const DiffArgs &a, const flo
 
 // The adjoint walks a ray's segments back to front; a segment's recomputed
 // positions, values and transmittances sit in per-thread arrays.
-// SEG_SMEM: the segment arrays live in dynamic shared memory, [array][step]
-// [thread] (consecutive threads, consecutive banks), for K <= kSmemK; else in
-// per-thread local memory.  The transfer function and its gradient sums sit
-// in front of them.
-constexpr int kSmemK = 16;
-
-template <bool SEG_SMEM>
 __global__ void __launch_bounds__(128) diff_backward_kernel(const __grid_constant__ DiffArgs a) {
-    extern __shared__ float4 dyn[];
-    float4 *tf = dyn;
-    float4 *gtf = dyn + a.ntf;
-    float *seg = reinterpret_cast<float *>(gtf + a.ntf);
+    __shared__ float4 tf[kMaxKnots];
+    __shared__ float4 gtf[kMaxKnots];
     for (int i = threadIdx.x; i < a.ntf; i += blockDim.x) {
         tf[i] = a.tf[i];
         gtf[i] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -353,37 +344,23 @@ __global__ void __launch_bounds__(128) diff_backward_kernel(const __grid_constan
         const float sx = dx * a.step, sy = dy * a.step, sz = dz * a.step;
         float4 R = make_float4(0.f, 0.f, 0.f, 0.f);
         const int K = a.K;
-        // per step of a segment: position (3), v.w before it, sample value
-        float loc[5][SEG_SMEM ? 1 : kMaxK];
-        const int nt = blockDim.x, tid = threadIdx.x;
-        auto put = [&](int arr, int st, float v) {
-            if constexpr (SEG_SMEM)
-                seg[(arr * K + st) * nt + tid] = v;
-            else
-                loc[arr][st] = v;
-        };
-        auto get = [&](int arr, int st) -> float {
-            if constexpr (SEG_SMEM)
-                return seg[(arr * K + st) * nt + tid];
-            else
-                return loc[arr][st];
-        };
+        float px[kMaxK], py[kMaxK], pz[kMaxK], pw[kMaxK], pv[kMaxK];
         const int nseg = (nsteps + K - 1) / K;
         GradAcc G;
         const float4 *cps = a.ckpt + ray * a.max_ckpt;
-        for (int sg = nseg - 1; sg >= 0; --sg) {
-            const float4 c = cps[sg];
+        for (int seg = nseg - 1; seg >= 0; --seg) {
+            const float4 c = cps[seg];
             float ox = c.x, oy = c.y, oz = c.z, vw = c.w;
-            const int cnt = min(K, nsteps - sg * K);
+            const int cnt = min(K, nsteps - seg * K);
             // recompute the segment: positions, values and v.w before each sample
-            for (int st = 0; st < cnt; ++st) {
-                put(0, st, ox);
-                put(1, st, oy);
-                put(2, st, oz);
-                put(3, st, vw);
+            for (int s = 0; s < cnt; ++s) {
+                px[s] = ox;
+                py[s] = oy;
+                pz[s] = oz;
+                pw[s] = vw;
                 const float ipx = floorf(ox), ipy = floorf(oy), ipz = floorf(oz);
                 const float val = diff_sample(a, ox - ipx, oy - ipy, oz - ipz);
-                put(4, st, val);
+                pv[s] = val;
                 int i, j;
                 float al;
                 bool inb;
@@ -394,9 +371,8 @@ __global__ void __launch_bounds__(128) diff_backward_kernel(const __grid_constan
                 oy = oy + sy;
                 oz = oz + sz;
             }
-            for (int st = cnt - 1; st >= 0; --st)
-                diff_adjoint_sample(a, tf, gtf, G, g, R, get(0, st), get(1, st), get(2, st),
-                                    get(4, st), 1.f - get(3, st));
+            for (int s = cnt - 1; s >= 0; --s)
+                diff_adjoint_sample(a, tf, gtf, G, g, R, px[s], py[s], pz[s], pv[s], 1.f - pw[s]);
         }
         G.flush_knots(gtf);
         G.flush_cell(a.dvol);
@@ -509,13 +485,7 @@ extern "C" int hy_diff_backward(hy_ctx *ctx, const hy_diff_params *p, const floa
     a.dtf = dtf_dev;
     HY_CUDA(ctx, cudaSetDevice(ctx->device));
     HY_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
-    const size_t tf_bytes = 2 * size_t(a.ntf) * sizeof(float4);
-    if (a.K <= kSmemK) {
-        const size_t smem = tf_bytes + 5 * size_t(a.K) * 128 * sizeof(float);
-        diff_backward_kernel<true><<<diff_grid(a), 128, smem, ctx->stream>>>(a);
-    } else {
-        diff_backward_kernel<false><<<diff_grid(a), 128, tf_bytes, ctx->stream>>>(a);
-    }
+    diff_backward_kernel<<<diff_grid(a), 128, 0, ctx->stream>>>(a);
     HY_CUDA(ctx, cudaGetLastError());
     HY_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
     ctx->stats_pending = true;
