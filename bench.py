@@ -221,6 +221,30 @@ def cpu_sample(args, w, vox, nthreads, budget_rows=None):
     return ov, (oview, op, view, y0, y0 + rows)
 
 
+def rows_parity(ctx, vol, w, ov, spec, tf, nthreads):
+    """The GPU's image of the CPU-baseline view against the oracle on the
+    baseline's rows: max LSB difference of RGBA8 and max abs difference of
+    the pre-quantisation floats (the bar is <= 1 LSB and <= 1e-4)."""
+    import numpy as np
+
+    import hydrant_gb300 as hy
+    from hydrant_gb300 import workloads as wl
+    from oracle import oracle as orc
+
+    oview, op, view, y0, y1 = spec
+    ref = orc.render(ov, tf, op, oview, view.width, view.height, nthreads=nthreads, want_v=True,
+                     want_aux=False, rows=(y0, y1))
+    cam = wl.make_camera(view.camera)
+    p = hy.shader_params(**w.params)
+    if p.shader == hy._abi.SHADER_ISOSURFACE:
+        hy.iso_lighting(vol, cam, p)
+    g = hy.render(ctx, vol, p, hy.camera_view(vol, cam), view.width, view.height, want_v=True)
+    lsb = int(np.abs(g.rgba[y0:y1].astype(int) - ref["rgba"][y0:y1].astype(int)).max())
+    fab = float(np.abs(g.v[y0:y1].astype(np.float64) - ref["v"][y0:y1]).max())
+    return {"rows": f"{y0}..{y1} of the {view.width}x{view.height} view", "max_lsb": lsb,
+            "max_abs": fab, "bar": "<= 1 LSB, <= 1e-4"}
+
+
 def run_cpu_sample(ov, spec, tf, nthreads):
     from oracle import oracle as orc
 
@@ -420,6 +444,7 @@ def main_ours(args):
     tps = profile_traffic_per_sample(int(tuned.get("block_queue", 1)))
     if rank == 0:
         cpu = None
+        parity = None
         if not args.no_cpu_baseline:
             nth = os.cpu_count() or 1
             ov, spec = cpu_sample(args, w, vox, nth)
@@ -428,6 +453,7 @@ def main_ours(args):
             cpu = {"value": s / dt / 1e9, "unit": "Gsamples/s", "cores": nth, "kind": "port",
                    "sample": f"rows {y0}..{y1} of the {view.width}x{view.height} view, {s} samples, "
                              f"{dt:.2f} s"}
+            parity = rows_parity(ctx, vol, w, ov, spec, w.tf, nth)
         out_json = {
             "metric": "Gsamples/s",
             "value": value,
@@ -470,6 +496,7 @@ def main_ours(args):
                 "note": "8 B/sample algorithmic footprint; the kernel is issue bound",
             },
             "cpu_baseline": cpu,
+            "parity_vs_oracle": parity,
             "gpu_launches": args.steps,
             "clocks": ck,
             "setup_s": {"generate": t_gen, "upload_and_brick": t_up},
