@@ -335,3 +335,22 @@ def test_ingest_raw_equals_device_bricking(ctx, tmp_path, dtype):
         vol.close()
     with pytest.raises(hy.HydrantError):
         hy.Store.ingest_raw(ctx, raw, (70, 45, 39), 16, 1)
+
+
+def test_coarse_level_of_f32_store_matches_oracle(ctx):
+    """f32 coarse voxels are the mean of their cube in double, rounded once."""
+    vox = hy.synth_blobs_f32(8, (40, 36, 30), 6)
+    vol = hy.Volume(ctx, vox, 8, 1)
+    ov = orc.OracleVolume(vox, 8, 1)
+    ov.build_coarse(1)
+    store = hy.Store.from_volume(vol)
+    try:
+        store.build_coarse(1)
+        g = store.coarse_grid
+        assert g == (3, 3, 2)
+        for cb in range(g[0] * g[1] * g[2]):
+            np.testing.assert_array_equal(store.coarse_brick(cb, np.float32), ov.coarse_brick(cb),
+                                          err_msg=f"coarse brick {cb}")
+    finally:
+        store.close()
+        vol.close()
