@@ -230,10 +230,12 @@ int hy_shade_pass(hy_ctx *ctx, const hy_volume *vol, const hy_shader_params *par
 
 /* ---- out-of-core volumes: brick store, culling, pager ------------------------
  * A store keeps every non-empty padded brick of a dataset in pinned host
- * memory (the decoded form of the varch archive the reference streams from,
- * lossless_block_paging.cc:149-167).  A pager owns a paged volume whose brick
- * pool is a fixed cache of `slots` device slots and keeps it filled from the
- * store, with one of the reference's two policies. */
+ * memory mapped into the device's address space (the decoded form of the
+ * varch archive the reference streams from, lossless_block_paging.cc:
+ * 149-167).  A pager owns a paged volume whose brick pool is a fixed cache of
+ * `slots` device slots and keeps it filled from the store, with one of the
+ * reference's two policies; a gather kernel reads each batch's or frame's
+ * bricks straight from the mapped store into their slots. */
 typedef struct hy_store hy_store;
 typedef struct hy_pager hy_pager;
 
@@ -313,7 +315,8 @@ int hy_pager_present(const hy_pager *pager, uint8_t *mask);
  *    distance of their centres to inverse(iet) * eye (as the reference
  *    computes it), uploaded in batches of `slots`; the first batch's pass
  *    emits, later ones resume (ray_march); only the current batch is in the
- *    page table.  Uploads of batch k+1 overlap the march of batch k.
+ *    page table.  Uploads of batch k+1 overlap the march of batch k.  With
+ *    count_samples the frame's samples over all its passes are counted.
  *  REALTIME: RtBlockPagingServer::update (rt_block_paging.cc:296-326): the
  *    nearest `slots` visible bricks are required; missing ones, nearest first,
  *    go to never-used slots and then to slots of bricks no longer required
