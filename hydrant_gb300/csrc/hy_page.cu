@@ -705,28 +705,17 @@ struct GatherItem {
 };
 
 // One block per brick: the slot is filled straight from the mapped pinned
-// store (the GPU reads host memory over the C2C link).  Each thread keeps
-// four independent 16-byte loads in flight (host memory is far away);
-// slot_stride is a multiple of 256 bytes.
-constexpr int kGatherThreads = 256;
-__global__ void __launch_bounds__(kGatherThreads)
-    gather_bricks_kernel(const unsigned char *__restrict__ store,
-                         const GatherItem *__restrict__ items, unsigned char *__restrict__ pool,
-                         long long slot0, long long stride) {
+// store (the GPU reads host memory over the C2C link), 16 bytes per thread
+// and iteration; slot_stride is a multiple of 256 bytes.
+__global__ void gather_bricks_kernel(const unsigned char *__restrict__ store,
+                                     const GatherItem *__restrict__ items,
+                                     unsigned char *__restrict__ pool, long long slot0,
+                                     long long stride) {
     const GatherItem it = items[blockIdx.x];
     const uint4 *src = reinterpret_cast<const uint4 *>(store + it.src);
     uint4 *dst = reinterpret_cast<uint4 *>(pool + (slot0 + it.dst) * stride);
     const int n = int(stride / 16);
-    int i = threadIdx.x;
-    for (; i + 3 * kGatherThreads < n; i += 4 * kGatherThreads) {
-        const uint4 a = src[i], b = src[i + kGatherThreads], c = src[i + 2 * kGatherThreads],
-                    d = src[i + 3 * kGatherThreads];
-        dst[i] = a;
-        dst[i + kGatherThreads] = b;
-        dst[i + 2 * kGatherThreads] = c;
-        dst[i + 3 * kGatherThreads] = d;
-    }
-    for (; i < n; i += kGatherThreads) dst[i] = src[i];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src[i];
 }
 
 }  // namespace
@@ -822,7 +811,7 @@ int move_bricks(hy_pager *pg, const int *bricks, const int *slots, int n, cudaSt
     HY_CUDA(ctx, cudaMemcpyAsync(dev, items, n * sizeof(GatherItem), cudaMemcpyHostToDevice,
                                  stream));
     HY_CUDA(ctx, cudaEventRecord(pg->gathered[buf], stream));
-    gather_bricks_kernel<<<n, kGatherThreads, 0, stream>>>(pg->store->host_dev, dev, v->pool, pg->ncoarse,
+    gather_bricks_kernel<<<n, 256, 0, stream>>>(pg->store->host_dev, dev, v->pool, pg->ncoarse,
                                                 (long long)v->slot_stride);
     HY_CUDA(ctx, cudaGetLastError());
     pg->stats.uploads += n;
