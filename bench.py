@@ -126,14 +126,15 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def profile_traffic_per_sample(block_queue: int):
-    """DRAM bytes per brick sample of the batch kernel, from the committed ncu
-    summary (one capture of 4 views of the same volume; traffic grows with
-    the samples processed, so it is scaled to a full launch by samples)."""
+def profile_per_sample(block_queue: int, what: str = "dram_bytes_per_sample"):
+    """A per-sample figure of the batch kernel (DRAM bytes, warp instructions)
+    from the committed ncu summary (one capture of 4 views of the same volume;
+    both grow with the samples processed, so they scale to a full launch by
+    samples)."""
     p = ROOT / "profiles" / "batch_kernel_multiview.txt"
     if not p.exists():
         return None
-    tag = f"dram_bytes_per_sample[block_queue={block_queue}]:"
+    tag = f"{what}[block_queue={block_queue}]:"
     for line in p.read_text().splitlines():
         if line.startswith(tag):
             try:
@@ -141,6 +142,23 @@ def profile_traffic_per_sample(block_queue: int):
             except ValueError:
                 return None
     return None
+
+
+def issue_roofline(inst_per_sample, samples, launch_s, clocks, device):
+    """The march is instruction-issue bound: warp instructions per second
+    (the profiled instructions per sample x samples / launch time) against
+    the peak of one instruction per cycle on each of the SMs' 4 schedulers at
+    the median SM clock sampled during the timed region."""
+    if not inst_per_sample or not clocks or not clocks.get("sm_mhz"):
+        return None
+    import torch
+
+    sms = torch.cuda.get_device_properties(device).multi_processor_count
+    peak = sms * 4 * clocks["sm_mhz"] * 1e6 / 1e9
+    achieved = inst_per_sample * samples / launch_s / 1e9
+    return {"achieved": achieved, "peak": peak, "unit": "G warp instructions/s",
+            "frac": achieved / peak, "warp_instructions_per_sample": inst_per_sample,
+            "note": "peak = SMs x 4 schedulers x median SM clock"}
 
 
 class Clocks:
@@ -441,7 +459,8 @@ def main_ours(args):
     hbm, peak_kind = measured_peaks()
     mean_launch_s = t / args.steps  # one batch kernel per step
     achieved = samples * BYTES_PER_SAMPLE / mean_launch_s / 1e9
-    tps = profile_traffic_per_sample(int(tuned.get("block_queue", 1)))
+    tps = profile_per_sample(int(tuned.get("block_queue", 1)))
+    ipsm = profile_per_sample(int(tuned.get("block_queue", 1)), "warp_instructions_per_sample")
     if rank == 0:
         cpu = None
         parity = None
@@ -495,6 +514,7 @@ def main_ours(args):
                 "traffic": (tps * samples) if tps else None,
                 "note": "8 B/sample algorithmic footprint; the kernel is issue bound",
             },
+            "issue_roofline": issue_roofline(ipsm, samples, mean_launch_s, ck, local),
             "cpu_baseline": cpu,
             "parity_vs_oracle": parity,
             "gpu_launches": args.steps,
