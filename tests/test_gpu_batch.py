@@ -113,3 +113,32 @@ def test_batch_rejects_bad_input(ctx, tubes):
             b.set_config(tile_w=5)
     finally:
         b.close()
+
+
+@pytest.fixture(scope="module")
+def blobs_bs64(ctx):
+    # 64^3 bricks + 1-voxel apron: the compile-time brick edge (P = 66) kernels
+    vol = hy.Volume(ctx, hy.synth_blobs_u8(3, (150, 130, 140), 20), 64, 1)
+    ctx.set_transfer_fn(wl.TF9)
+    yield vol
+    vol.close()
+
+
+@pytest.mark.parametrize("mode", ["Default", "Partition", "Paging"])
+def test_batch_equals_per_view_p66(ctx, blobs_bs64, mode):
+    """Default mode runs the lean march (no theta / phi), the others the full
+    one; both must give the per-view images and samples exactly."""
+    kw = dict(shader="Volume", mode=mode, density=0.05, sample_rate=0.25, rank=0.3)
+    views, cams = _views(blobs_bs64, SIZES, seed=17)
+    ref, ref_samples = _per_view(ctx, blobs_bs64, kw, views, cams)
+    b = hy.Batch(ctx, blobs_bs64, hy.shader_params(**kw), views)
+    try:
+        b.set_counting(True)
+        for cfg in [(8, 1, 4, 0, 1), (8, 1, 8, 0, 0), (16, 2, 4, 0, 1)]:
+            b.set_config(*cfg)
+            got = b.render()
+            assert ctx.stats().samples == ref_samples
+            for i, (g, r) in enumerate(zip(got, ref)):
+                assert np.array_equal(g, r), f"view {i} differs with config {cfg}"
+    finally:
+        b.close()
