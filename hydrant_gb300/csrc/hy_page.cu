@@ -866,7 +866,12 @@ extern "C" int hy_pager_create(hy_ctx *ctx, hy_store *store, const hy_pager_desc
     }
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&pg->copy, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&pg->copied, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&pg->cull_stream, cudaStreamNonBlocking);
+    // the cull runs while the previous frame's render grid still has blocks
+    // waiting; the highest priority lets its few blocks go first
+    int prio_low = 0, prio_high = 0;
+    if (e == cudaSuccess) e = cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
+    if (e == cudaSuccess)
+        e = cudaStreamCreateWithPriority(&pg->cull_stream, cudaStreamNonBlocking, prio_high);
     if (e == cudaSuccess) e = cudaMalloc(&pg->cheb_dev, v->nbricks * sizeof(int));
     if (e == cudaSuccess)
         e = cudaMemcpy(pg->cheb_dev, v->cheb.data(), v->nbricks * sizeof(int),
