@@ -597,9 +597,12 @@ def main_paging(args):
     # every visible brick is sampled, so the count does not depend on what
     # the cache holds; without it the second pass starts from a warmer cache.
     samples = 0
+    last_pass_ms = 0.0
     for f in range(frames):
         pg.render(pc, hy.camera_orbit((3.0 * f, 30.0, 2.2)), res, res, out.data_ptr())
-        samples += ctx.stats().samples
+        st_f = ctx.stats()
+        samples += st_f.samples
+        last_pass_ms += st_f.ms
     lookups = d["hits"] + d["misses"]
     outj = {
         "metric": "frames/s", "value": frames / wall, "unit": "frames/s", "n_gpus": 1,
@@ -618,6 +621,7 @@ def main_paging(args):
         "cache_hit_rate": (d["hits"] / lookups) if lookups else None,
         "uploads_per_frame": d["uploads"] / frames,
         "passes_per_frame": d["passes"] / frames,
+        "last_pass_ms_per_frame": last_pass_ms / frames,
         "upload_gb_per_s": d["upload_bytes"] / wall / 1e9,
         "evictions": d["evictions"], "visible_last_frame": st["visible"],
         "coarse_bricks_per_frame": fallback / frames,
