@@ -20,7 +20,7 @@ HY_ERR_TIMEOUT = -4
 HY_ERR_UNSUPPORTED = -5
 HY_ERR_STATE = -6
 
-SHADER_VOLUME, SHADER_BLOCKS, SHADER_ISOSURFACE = 0, 1, 2
+SHADER_VOLUME, SHADER_BLOCKS, SHADER_ISOSURFACE, SHADER_PAGING = 0, 1, 2, 3
 VOLUME_DEFAULT, VOLUME_PARTITION, VOLUME_PAGING = 0, 1, 2
 BLOCKS_VOLUME, BLOCKS_SOLID = 0, 1
 ISO_COLOR, ISO_NORMAL, ISO_POSITION = 0, 1, 2

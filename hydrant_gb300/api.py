@@ -22,11 +22,13 @@ from ._abi import (
     lib,
 )
 
-SHADERS = {"Volume": _abi.SHADER_VOLUME, "Blocks": _abi.SHADER_BLOCKS, "Isosurface": _abi.SHADER_ISOSURFACE}
+SHADERS = {"Volume": _abi.SHADER_VOLUME, "Blocks": _abi.SHADER_BLOCKS,
+           "Isosurface": _abi.SHADER_ISOSURFACE, "Paging": _abi.SHADER_PAGING}
 MODES = {
     _abi.SHADER_VOLUME: {"Default": 0, "Partition": 1, "Paging": 2},
     _abi.SHADER_BLOCKS: {"Volume": 0, "Solid": 1},
     _abi.SHADER_ISOSURFACE: {"Color": 0, "Normal": 1, "Position": 2},
+    _abi.SHADER_PAGING: {"Default": 0},
 }
 
 

@@ -174,7 +174,7 @@ const void *pick_c(const ShadeArgs &a) {
 
 template <int SHADER>
 const void *pick_shader(const ShadeArgs &a) {
-    if constexpr (SHADER == HY_SHADER_BLOCKS) {
+    if constexpr (SHADER == HY_SHADER_BLOCKS || SHADER == HY_SHADER_PAGING) {
         return pick_c<SHADER, 0, HY_DTYPE_U8, false>(a);
     } else {
         const bool padded = a.vol.pad > 0;
@@ -195,6 +195,8 @@ const void *pick_kernel(const ShadeArgs &a) {
             return pick_shader<HY_SHADER_VOLUME>(a);
         case HY_SHADER_BLOCKS:
             return pick_shader<HY_SHADER_BLOCKS>(a);
+        case HY_SHADER_PAGING:
+            return pick_shader<HY_SHADER_PAGING>(a);
         default:
             return pick_shader<HY_SHADER_ISOSURFACE>(a);
     }

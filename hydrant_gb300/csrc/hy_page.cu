@@ -1069,7 +1069,7 @@ int render_lossless(hy_pager *pg, const hy_shader_params *p, const hy_camera *ca
     }
     for (int b : prev) pg->page[b] = -1;
     uchar4 clear = make_uchar4(a.clear_u8[0], a.clear_u8[1], a.clear_u8[2], 0);
-    const int stride = p->shader == HY_SHADER_BLOCKS ? 3 : 4;
+    const int stride = (p->shader == HY_SHADER_BLOCKS || p->shader == HY_SHADER_PAGING) ? 3 : 4;
     film_rgba_kernel<<<(W * H + 255) / 256, 256, 0, ctx->stream>>>(
         static_cast<const float4 *>(pg->film), stride, W * H, reinterpret_cast<uchar4 *>(rgba_dev),
         clear);

@@ -91,7 +91,7 @@ __global__ void __launch_bounds__(kThreads) render_kernel(const __grid_constant_
 
 template <int SHADER>
 __device__ __forceinline__ size_t film_bytes() {
-    return SHADER == HY_SHADER_BLOCKS ? 48 : 64;
+    return (SHADER == HY_SHADER_BLOCKS || SHADER == HY_SHADER_PAGING) ? 48 : 64;
 }
 
 template <int SHADER>
@@ -100,7 +100,8 @@ __device__ __forceinline__ void store_film(void *film, size_t idx, const Px &p) 
     q[0] = make_float4(p.ox, p.oy, p.oz, p.dx);
     q[1] = make_float4(p.dy, p.dz, __int_as_float(p.nsteps), __int_as_float(p.step_size));
     q[2] = make_float4(p.vx, p.vy, p.vz, p.vw);
-    if (SHADER != HY_SHADER_BLOCKS) q[3] = make_float4(p.e0, p.e1, p.e2, p.e3);
+    if (SHADER != HY_SHADER_BLOCKS && SHADER != HY_SHADER_PAGING)
+        q[3] = make_float4(p.e0, p.e1, p.e2, p.e3);
 }
 
 template <int SHADER>
@@ -121,7 +122,7 @@ __device__ __forceinline__ Px load_film(const void *film, size_t idx) {
     p.vy = c.y;
     p.vz = c.z;
     p.vw = c.w;
-    if (SHADER != HY_SHADER_BLOCKS) {
+    if (SHADER != HY_SHADER_BLOCKS && SHADER != HY_SHADER_PAGING) {
         float4 d = q[3];
         p.e0 = d.x;
         p.e1 = d.y;
@@ -196,8 +197,9 @@ __global__ void __launch_bounds__(kThreads) pixel_pass_kernel(const __grid_const
 }
 
 // fetch_kernel_impl (cuda_shading.cu:80-94): VolumeShaderKernel::fetch
-// (volume_shader.cu:23-30) and IsosurfaceShaderKernel::fetch
-// (isosurface_shader.cu:41-48).  The Blocks shader has no fetch.
+// (volume_shader.cu:23-30), IsosurfaceShaderKernel::fetch
+// (isosurface_shader.cu:41-48) and PagingShaderKernel::fetch
+// (paging_shader.cu:16-22, uchar3 pixels).  The Blocks shader has no fetch.
 template <int SHADER>
 __global__ void __launch_bounds__(kThreads) fetch_pass_kernel(const __grid_constant__ ShadeArgs A) {
     int x, y;
@@ -216,6 +218,11 @@ __global__ void __launch_bounds__(kThreads) fetch_pass_kernel(const __grid_const
         d[2] = saturate_u8(p.vz);
         d[3] = 0;
         *reinterpret_cast<float *>(d + 4) = p.e3;
+    } else if (SHADER == HY_SHADER_PAGING) {
+        unsigned char *d = static_cast<unsigned char *>(A.dst) + idx * 3;
+        d[0] = saturate_u8(p.vx);
+        d[1] = saturate_u8(p.vy);
+        d[2] = saturate_u8(p.vz);
     }
 }
 
@@ -244,7 +251,7 @@ void launch_fused(const ShadeArgs &a, cudaStream_t s) {
 // 64^3 or 128^3 bricks get a compile-time brick edge (immediate offsets).
 template <int SHADER>
 int dispatch_fused(const ShadeArgs &a, cudaStream_t s) {
-    if constexpr (SHADER == HY_SHADER_BLOCKS) {
+    if constexpr (SHADER == HY_SHADER_BLOCKS || SHADER == HY_SHADER_PAGING) {
         launch_fused<SHADER, 0, HY_DTYPE_U8, false>(a, s);
     } else {
         const bool padded = a.vol.pad > 0;
@@ -309,8 +316,10 @@ int hy_fill_args(hy_ctx *ctx, const hy_volume *vol, const hy_shader_params *p, c
     if (!vol->uploaded) return hy_fail(ctx, HY_ERR_STATE, "render: volume not uploaded");
     if (W <= 0 || H <= 0 || (long long)W * H > (1ll << 31))
         return hy_fail(ctx, HY_ERR_INVALID, "render: bad resolution");
-    if (p->shader < HY_SHADER_VOLUME || p->shader > HY_SHADER_ISOSURFACE)
+    if (p->shader < HY_SHADER_VOLUME || p->shader > HY_SHADER_PAGING)
         return hy_fail(ctx, HY_ERR_INVALID, "render: unknown shader");
+    if (p->shader == HY_SHADER_PAGING && p->composite)
+        return hy_fail(ctx, HY_ERR_UNSUPPORTED, "render: the Paging shader has no compositing");
     if (!(p->sample_rate > 0.f)) return hy_fail(ctx, HY_ERR_INVALID, "render: sample_rate <= 0");
     if (p->shader == HY_SHADER_VOLUME && ctx->ntf <= 0)
         return hy_fail(ctx, HY_ERR_STATE, "render: Volume shader needs a transfer function");
@@ -360,6 +369,9 @@ int hy_launch_render(hy_ctx *ctx, const ShadeArgs &a) {
         case HY_SHADER_BLOCKS:
             dispatch_fused<HY_SHADER_BLOCKS>(a, ctx->stream);
             break;
+        case HY_SHADER_PAGING:
+            dispatch_fused<HY_SHADER_PAGING>(a, ctx->stream);
+            break;
         default:
             dispatch_fused<HY_SHADER_ISOSURFACE>(a, ctx->stream);
             break;
@@ -382,6 +394,9 @@ int hy_launch_pass(hy_ctx *ctx, const ShadeArgs &a, int pass, bool reset_counter
             break;
         case HY_SHADER_BLOCKS:
             dispatch_pass<HY_SHADER_BLOCKS>(a, pass, ctx->stream);
+            break;
+        case HY_SHADER_PAGING:
+            dispatch_pass<HY_SHADER_PAGING>(a, pass, ctx->stream);
             break;
         default:
             dispatch_pass<HY_SHADER_ISOSURFACE>(a, pass, ctx->stream);

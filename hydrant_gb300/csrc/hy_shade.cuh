@@ -456,6 +456,47 @@ __device__ __forceinline__ long long blocks_main(Px &p, const ShadeArgs &A) {
     return samples;
 }
 
+// PagingShaderKernel::main (paging_shader.cu:26-61): the paging debug view.
+// Each non-empty brick a ray enters adds one constant colour -- green 0.5 for
+// a resident fine brick (registry id >= lowest_blkcnt), red 0.2 for a coarse
+// stand-in -- and the ray skips to that brick's exit; opacity > 0.95 or an
+// absent brick (page fault) ends the ray (nsteps is left as it is there).
+__device__ __forceinline__ long long paging_main(Px &p, const ShadeArgs &A) {
+    const DevVolume &V = A.vol;
+    long long samples = 0;
+    const float cdu = 1.f / gmax(gmax(fabsf(p.dx), fabsf(p.dy)), fabsf(p.dz));
+    const float rx = 1.f / p.dx, ry = 1.f / p.dy, rz = 1.f / p.dz;
+    const float fgx = float(V.gx), fgy = float(V.gy), fgz = float(V.gz);
+    const float opacity_threshold = 0.95f;
+    const float sx = p.dx * A.step, sy = p.dy * A.step, sz = p.dz * A.step;
+    while (p.nsteps > 0) {
+        float ipx = floorf(p.ox), ipy = floorf(p.oy), ipz = floorf(p.oz);
+        int bid = thumb_index(V, fgx, fgy, fgz, ipx, ipy, ipz);
+        const int2 in = __ldg(&V.info[bid]);
+        if (in.x) {
+            p.nsteps -= skip_nblock_steps(p, rx, ry, rz, ipx, ipy, ipz, in.x, cdu, A.step);
+        } else {
+            if (in.y == -1) break;  // page fault
+            const bool fine = in.y >= A.lowest_blkcnt;
+            const float cx = fine ? 0.f * .5f : 1.f * .2f, cy = fine ? 1.f * .5f : 0.f * .2f,
+                        cz = fine ? 0.f * .5f : 0.f * .2f, cw = fine ? 1.f * .5f : 1.f * .2f;
+            p.nsteps -= skip_nblock_steps(p, rx, ry, rz, ipx, ipy, ipz, 1, cdu, A.step);
+            ++samples;
+            const float t = 1.f - p.vw;
+            p.vx = p.vx + cx * t;
+            p.vy = p.vy + cy * t;
+            p.vz = p.vz + cz * t;
+            p.vw = p.vw + cw * t;
+            if (p.vw > opacity_threshold) break;
+        }
+        p.ox = p.ox + sx;
+        p.oy = p.oy + sy;
+        p.oz = p.oz + sz;
+        p.nsteps -= 1;
+    }
+    return samples;
+}
+
 // linear_to_srgb of the isosurface shader: double-precision constants
 // (isosurface_shader.cu:25-32).
 __device__ __forceinline__ float iso_linear_to_srgb(float linear) {
@@ -576,6 +617,7 @@ __device__ __forceinline__ long long run_main(Px &p, const ShadeArgs &A, const V
                                              const Shared &S) {
     if (SHADER == HY_SHADER_VOLUME) return volume_main<PC, DT, PADDED, LEAN>(p, A, S);
     if (SHADER == HY_SHADER_BLOCKS) return blocks_main(p, A);
+    if (SHADER == HY_SHADER_PAGING) return paging_main(p, A);
     return iso_main<PC, DT, PADDED>(p, A, Vw, S);
 }
 

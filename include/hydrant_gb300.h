@@ -43,9 +43,12 @@ extern "C" {
 #define HY_ERR_UNSUPPORTED (-5) /* combination not built */
 #define HY_ERR_STATE (-6)       /* object not ready (e.g. no transfer function) */
 
-/* Shaders: the three REGISTER_SHADER_BUILDER registrations on the path
- * (volume_shader.cu:84-88, blocks_shader.cu:53-57, isosurface_shader.cu:128-132). */
-enum { HY_SHADER_VOLUME = 0, HY_SHADER_BLOCKS = 1, HY_SHADER_ISOSURFACE = 2 };
+/* Shaders: the REGISTER_SHADER_BUILDER registrations on the path
+ * (volume_shader.cu:84-88, blocks_shader.cu:53-57, isosurface_shader.cu:128-132,
+ * paging_shader.cu:63-68).  Paging is the paging debug view: a constant
+ * colour per brick, green for resident fine bricks, red for coarse ones
+ * (registry ids below lowest_blkcnt); it has no modes and no compositing. */
+enum { HY_SHADER_VOLUME = 0, HY_SHADER_BLOCKS = 1, HY_SHADER_ISOSURFACE = 2, HY_SHADER_PAGING = 3 };
 /* VolumeRenderMode (ui/volume.schema.hpp:11-14) */
 enum { HY_VOLUME_DEFAULT = 0, HY_VOLUME_PARTITION = 1, HY_VOLUME_PAGING = 2 };
 /* BlocksRenderMode (ui/blocks.schema.hpp:10-11) */
@@ -142,6 +145,10 @@ typedef struct hy_iso_fetch_pixel {
     uint8_t pad_;
     float depth;
 } hy_iso_fetch_pixel; /* IsosurfaceFetchPixel, 8 B */
+
+typedef struct hy_paging_fetch_pixel {
+    uint8_t val[3];
+} hy_paging_fetch_pixel; /* PagingFetchPixel (paging_shader.hpp:11-14), 3 B */
 
 /* Dataset meta the renderers read (basic_renderer.hpp:104-118,
  * lossless_block_paging.cc:17-22): raw dims, block size, apron. */

@@ -14,11 +14,12 @@
 //     (renderer.schema.hpp), BasicRendererParams {device, comm_rank,
 //     sample_rate, max_steps, clear_color} (basic_renderer.schema.hpp), and
 //     the Volume / Blocks / Isosurface params (ui/*.schema.hpp).
-// The built-in renderers "Volume", "Blocks" and "Isosurface" follow
-// volume.cc, blocks.cc and isosurface.cc: offline_render pages the dataset
-// through the lossless pager (Blocks reads only the thumbnails: one emit
-// pass), realtime_render renders one frame through the realtime pager with
-// the mem_limit_mb cache (and the dataset's coarse level as fallback).
+// The built-in renderers "Volume", "Blocks", "Isosurface" and "Paging"
+// follow volume.cc, blocks.cc, isosurface.cc and paging.cc: offline_render
+// pages the dataset through the lossless pager (Blocks reads only the
+// thumbnails: one emit pass; Paging returns an unrendered film, as there),
+// realtime_render renders one frame through the realtime pager with the
+// mem_limit_mb cache (and the dataset's coarse level as fallback).
 //
 // Differences from the reference, by design:
 //   * images are RGBA8 (A = saturated opacity; RGB as the reference writes);
@@ -478,7 +479,34 @@ private:
     }
 };
 
+// PagingRenderer (src/slave/renderers/paging/paging.cc; paging.schema.hpp):
+// the paging debug view.  Its offline render is an unrendered (clear) film,
+// as in the reference (paging.cc:60-65); a realtime frame shows the realtime
+// cache: green bricks resident, red ones drawn from the coarse level.
+class PagingRenderer : public BasicRenderer {
+public:
+    void update(json::Value const &p) override {
+        BasicRenderer::update(p);
+        mem_limit_mb = size_t(p.number_or("mem_limit_mb", double(mem_limit_mb)));
+    }
+    Image offline_render(CameraConfig const &camera) override {
+        (void)camera;
+        Image img;
+        img.width = resolution[0];
+        img.height = resolution[1];
+        img.rgba.assign(size_t(img.width) * img.height * 4, 0);
+        return img;
+    }
+    Image realtime_render(CameraConfig const &camera) override {
+        return frame(realtime(mem_limit_mb), base_params(HY_SHADER_PAGING), camera);
+    }
+
+private:
+    size_t mem_limit_mb = 2048;
+};
+
 HYGB_REGISTER_RENDERER(VolumeRenderer, "Volume");
+HYGB_REGISTER_RENDERER(PagingRenderer, "Paging");
 HYGB_REGISTER_RENDERER(BlocksRenderer, "Blocks");
 HYGB_REGISTER_RENDERER(IsosurfaceRenderer, "Isosurface");
 

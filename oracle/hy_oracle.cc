@@ -748,6 +748,40 @@ int64_t blocks_main(const Ctx &c, Px &px) {
     return samples;
 }
 
+// PagingShaderKernel::main (paging_shader.cu:26-61): a constant colour per
+// non-empty brick entered (green 0.5 if its registry id >= lowest_blkcnt,
+// red 0.2 otherwise), then a skip to the brick's exit; opacity > 0.95 or a
+// page fault ends the ray without touching nsteps.
+int64_t paging_main(const Ctx &c, Px &px) {
+    const orc_volume *v = c.vol;
+    int64_t samples = 0;
+    const float cdu = 1.f / comp_max(f3(std::fabs(px.ray.d.x), std::fabs(px.ray.d.y),
+                                        std::fabs(px.ray.d.z)));
+    const float opacity_threshold = 0.95f;
+    Ray &ray = px.ray;
+    while (px.nsteps > 0) {
+        F3 ip = floor3(ray.o);
+        int bid = thumb_index(v, ip);
+        if (int cd = v->cheb[bid]) {
+            px.nsteps -= skip_nblock_steps(ray, ip, cd, cdu, c.step);
+        } else {
+            int pgid = v->vaddr[bid];
+            if (pgid == -1) break;  // page fault
+            F4 col = pgid >= c.p.lowest_blkcnt ? F4{0.f * .5f, 1.f * .5f, 0.f * .5f, 1.f * .5f}
+                                               : F4{1.f * .2f, 0.f * .2f, 0.f * .2f, 1.f * .2f};
+            px.nsteps -= skip_nblock_steps(ray, ip, 1, cdu, c.step);
+            ++samples;
+            float t = 1.f - px.v.w;
+            px.v = F4{px.v.x + col.x * t, px.v.y + col.y * t, px.v.z + col.z * t,
+                      px.v.w + col.w * t};
+            if (px.v.w > opacity_threshold) break;
+        }
+        ray.o = add(ray.o, muls(ray.d, c.step));
+        px.nsteps -= 1;
+    }
+    return samples;
+}
+
 float iso_linear_to_srgb(float linear) {
     // isosurface_shader.cu:25-32 (double-precision constants)
     if (double(linear) <= 0.0031308) return float(12.92 * double(linear));
@@ -836,6 +870,8 @@ int64_t run_main(const Ctx &c, Px &px) {
             return volume_main(c, px);
         case 1:
             return blocks_main(c, px);
+        case 3:
+            return paging_main(c, px);
         default:
             return iso_main(c, px);
     }
@@ -929,7 +965,7 @@ void write_film(const Ctx &c, const Px &px, void *film, size_t idx) {
 }
 
 void read_film(const Ctx &c, Px &px, const void *film, size_t idx) {
-    size_t bytes = c.p.shader == 1 ? 48 : 64;
+    size_t bytes = (c.p.shader == 1 || c.p.shader == 3) ? 48 : 64;
     float buf[16] = {};
     std::memcpy(buf, static_cast<const char *>(film) + idx * bytes, bytes);
     px = Px{};

@@ -90,7 +90,8 @@ int main() {
 
     // built-in renderers are registered
     auto names = hygb::RendererFactory::list_candidates();
-    CHECK(names.size() == 3 && names[0] == "Blocks" && names[1] == "Isosurface" && names[2] == "Volume");
+    CHECK(names.size() == 4 && names[0] == "Blocks" && names[1] == "Isosurface" &&
+          names[2] == "Paging" && names[3] == "Volume");
 
     if (failures) return 1;
     std::printf("ok\n");

@@ -51,6 +51,7 @@ def test_renderer_driver_compiles(tmp_path):
                                            [0, 0, 1, 1], [1, 0, 1, 1], [0, 0, 0, 0]]}}),
     ("Isosurface", {"mode": "Color", "isovalue": 0.5, "mem_limit_mb": 4}),
     ("Blocks", {"mode": "Volume", "density": 0.05}),
+    ("Paging", {"mem_limit_mb": 4}),
 ])
 def test_renderer_factory_renders_like_the_c_abi(ctx, tmp_path, renderer, params):
     torch = pytest.importorskip("torch")
@@ -76,11 +77,11 @@ def test_renderer_factory_renders_like_the_c_abi(ctx, tmp_path, renderer, params
 
     # the same frames through the Python binding
     cam = hy.camera_orbit((30, 40, 2.2))
-    shader = {"Volume": "Volume", "Isosurface": "Isosurface", "Blocks": "Blocks"}[renderer]
+    shader = renderer
     kw = dict(shader=shader, sample_rate=params.get("sample_rate", 1.0),
               density=params.get("density", 1.0 if renderer != "Blocks" else 1e-2),
               isovalue=params.get("isovalue", 0.5))
-    kw["mode"] = params["mode"]
+    kw["mode"] = params.get("mode", "Default")
     if renderer == "Volume":
         ctx.set_transfer_fn(np.array(params["transfer_fn"]["values"], np.float32))
     slots_off = min(4 * 2**20 // store.info.slot_bytes, 4096)
@@ -103,8 +104,12 @@ def test_renderer_factory_renders_like_the_c_abi(ctx, tmp_path, renderer, params
             pg.close()
 
     try:
-        assert np.array_equal(got["offline"], frame(_abi.PAGER_LOSSLESS, slots_off))
         assert np.array_equal(got["realtime"], frame(_abi.PAGER_REALTIME, slots_rt))
+        if renderer == "Paging":  # the reference's offline Paging frame is not rendered
+            assert not got["offline"].any() and not got["updated"].any()
+            assert (got["realtime"][..., 1] > 0).any()
+            return
+        assert np.array_equal(got["offline"], frame(_abi.PAGER_LOSSLESS, slots_off))
         upd = frame(_abi.PAGER_LOSSLESS, slots_off, clear=(0.25, 0.5, 1.0))
         assert np.array_equal(got["updated"], upd)
         assert (got["offline"][..., 3] > 0).any()

@@ -58,6 +58,7 @@ def tubes(ctx):
     dict(shader="Blocks", mode="Volume", density=1e-2),
     dict(shader="Volume", density=0.5, composite=True),
     dict(shader="Isosurface", mode="Normal", composite=True),
+    dict(shader="Paging"),
 ])
 def test_batch_equals_per_view(ctx, tubes, kw):
     views, cams = _views(tubes, SIZES)

@@ -220,8 +220,9 @@ def test_coarse_level_matches_oracle(tubes_coarse):
     assert ov.lowest_blkcnt == 9 ** 3
 
 
-@pytest.mark.parametrize("mode", ["Default", "Paging"])
-def test_realtime_coarse_fallback_matches_oracle(ctx, tubes_coarse, mode):
+@pytest.mark.parametrize("shader,mode", [("Volume", "Default"), ("Volume", "Paging"),
+                                         ("Paging", "Default")])
+def test_realtime_coarse_fallback_matches_oracle(ctx, tubes_coarse, shader, mode):
     """Absent bricks sample the coarse level instead of stopping the ray; the
     Paging mode colours coarse samples red and fine ones green."""
     torch = pytest.importorskip("torch")
@@ -234,7 +235,7 @@ def test_realtime_coarse_fallback_matches_oracle(ctx, tubes_coarse, mode):
         saw_fallback = False
         for f in range(5):
             c = wl.make_camera(wl.Camera("orbit", (20 + 30 * f, 35, 2.2)))
-            p = hy.shader_params(shader="Volume", mode=mode, density=0.4, sample_rate=0.5,
+            p = hy.shader_params(shader=shader, mode=mode, density=0.4, sample_rate=0.5,
                                  count_samples=True)
             out = torch.zeros(W * H * 4, dtype=torch.uint8, device="cuda")
             pg.render(p, c, W, H, out.data_ptr())
@@ -249,7 +250,7 @@ def test_realtime_coarse_fallback_matches_oracle(ctx, tubes_coarse, mode):
             got = out.cpu().numpy().reshape(H, W, 4)
             d = np.abs(got.astype(int) - ref["rgba"].astype(int))
             assert d.max() <= 1, f"frame {f}: {d.max()} LSB"
-            if mode == "Paging" and st["fallback"] > 0:
+            if "Paging" in (shader, mode) and st["fallback"] > 0:
                 assert (got[..., 0] > 0).any() and (got[..., 1] > 0).any()
         assert saw_fallback
     finally:

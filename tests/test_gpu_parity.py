@@ -157,10 +157,10 @@ def test_camera_helpers_match_oracle(blobs64):
 
 
 def _film_dtype(shader):
-    return 48 if shader == "Blocks" else 64
+    return 48 if shader in ("Blocks", "Paging") else 64
 
 
-@pytest.mark.parametrize("shader", ["Volume", "Blocks", "Isosurface"])
+@pytest.mark.parametrize("shader", ["Volume", "Blocks", "Isosurface", "Paging"])
 def test_pass_level_film(tubes128, shader):
     """hy_shade_pass RAY_EMIT / PIXEL / FETCH on a reference-layout film."""
     torch = pytest.importorskip("torch")
@@ -190,7 +190,11 @@ def test_pass_level_film(tubes128, shader):
                       dst.data_ptr())
         ctx.synchronize()
         fetched = dst.cpu().numpy()
-        if shader == "Volume":
+        if shader == "Paging":  # uchar3 saturate(v)
+            f = fetched[: H * W * 3].reshape(H, W, 3)
+            sat = np.clip(ref["v"][..., :3] * np.float32(255), 0, 255).astype(np.uint8)
+            np.testing.assert_array_equal(f, sat)
+        elif shader == "Volume":
             f = fetched.view(np.float32)[: H * W * 8].reshape(H, W, 8)
             np.testing.assert_array_equal(f[..., 0:4], ref["aux"])       # theta, phi
             np.testing.assert_array_equal(f[..., 4:8], ref["v"])         # val
@@ -214,3 +218,15 @@ def test_tubes_c1_isosurface_full(ctx):
             assert_parity(g, r, what=f"config 1 blocks {mode}")
     finally:
         c.close()
+
+
+def test_paging_shader(tubes128, blobs64):
+    """The paging debug view: one colour per brick entered, every brick of a
+    resident volume is a fine one (green)."""
+    for c, cam in ((tubes128, camera(a=(20, 30, 2.2))), (blobs64, camera())):
+        g, r, _, _ = c.render_both(cam, 80, 64, shader="Paging")
+        assert_parity(g, r, what="paging shader")
+        assert g.rgba[..., 1].any() and not g.rgba[..., 0].any()
+    with pytest.raises(hy.HydrantError):
+        p = hy.shader_params(shader="Paging", composite=True)
+        hy.render(tubes128.ctx, tubes128.vol, p, hy.camera_view(tubes128.vol, camera()), 8, 8)

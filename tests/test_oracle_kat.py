@@ -312,3 +312,31 @@ def test_coarse_fallback_of_constant_volume_equals_fine_render():
     red = orc.render(ov, TF9, p, view, 24, 24)["v"]
     hit = red[..., 3] > 0
     assert hit.any() and not red[..., 1][hit].any() and (red[..., 0][hit] > 0).all()
+
+
+def test_paging_shader_one_colour_per_brick():
+    # a constant volume: every brick non-empty and resident (registry ids >= 0
+    # = lowest_blkcnt), so each brick a ray enters adds green 0.5 once:
+    # v.w = 1 - 0.5^k after k bricks, v.g = v.w, red and blue stay 0; the
+    # ray stops once v.w > 0.95 (k = 5)
+    vox = np.full((64, 64, 64), 100, np.uint8)
+    ov = orc.OracleVolume(vox, 8, 1)
+    view = orc.camera_view(ov, orc.camera_orbit((30, 40, 2.2)))
+    p = params(shader=3)
+    r = orc.render(ov, TF9, p, view, 32, 32)
+    v = r["v"].astype(np.float64)
+    hit = v[..., 3] > 0
+    assert hit.sum() > 100
+    assert not v[..., 0].any() and not v[..., 2].any()
+    np.testing.assert_array_equal(v[..., 1], v[..., 3])
+    allowed = {1 - 0.5 ** k for k in range(1, 6)}
+    assert set(np.unique(v[..., 3][hit]).tolist()) <= allowed
+    assert (v[..., 3] == 1 - 0.5 ** 5).any()
+    # with a coarse level, absent bricks are red 0.2
+    ov.build_coarse(1)
+    ov.set_present(np.zeros(ov.grid[0] * ov.grid[1] * ov.grid[2], np.uint8))
+    p.lowest_blkcnt = ov.lowest_blkcnt
+    red = orc.render(ov, TF9, p, view, 32, 32)["v"]
+    hit = red[..., 3] > 0
+    assert hit.any() and not red[..., 1][hit].any()
+    np.testing.assert_array_equal(red[..., 0], red[..., 3])
