@@ -184,7 +184,7 @@ def render(vol: OracleVolume, tf, params: OrcParams, view: np.ndarray, width: in
     v = np.zeros((height, width, 4), np.float32) if want_v else None
     rgba = np.zeros((height, width, 4), np.uint8)
     aux = np.zeros((height, width, 4), np.float32) if want_aux else None
-    fb = 48 if params.shader == 1 else 64
+    fb = 48 if params.shader in (1, 3) else 64  # StdVec4Pixel films: Blocks, Paging
     film = np.zeros((height, width, fb), np.uint8) if want_film else None
     view = np.ascontiguousarray(view, np.float32)
     if rows is None:
