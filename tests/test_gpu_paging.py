@@ -355,3 +355,38 @@ def test_coarse_level_of_f32_store_matches_oracle(ctx):
     finally:
         store.close()
         vol.close()
+
+
+def test_realtime_pager_on_f32_store_matches_oracle(ctx):
+    """An f32 dataset through the realtime pager with a coarse level and a
+    cache too small for the view: resident bricks fine, the rest coarse."""
+    torch = pytest.importorskip("torch")
+    vox = hy.synth_blobs_f32(9, (64, 64, 64), 10)
+    vol = hy.Volume(ctx, vox, 16, 1)
+    ov = orc.OracleVolume(vox, 16, 1)
+    ov.build_coarse(1)
+    store = hy.Store.from_volume(vol)
+    store.build_coarse(1)
+    ctx.set_transfer_fn(wl.TF9)
+    pg = hy.Pager(ctx, store, 12, _abi.PAGER_REALTIME, 5)
+    nb = ov.grid[0] * ov.grid[1] * ov.grid[2]
+    try:
+        W, H = 56, 48
+        for f in range(3):
+            c = wl.make_camera(wl.Camera("orbit", (10 + 40 * f, 25, 2.0)))
+            p = hy.shader_params(shader="Volume", density=0.5, sample_rate=0.5)
+            out = torch.zeros(W * H * 4, dtype=torch.uint8, device="cuda")
+            pg.render(p, c, W, H, out.data_ptr())
+            ctx.synchronize()
+            ov.set_present(pg.present())
+            op = orc.params_from(p)
+            op.lowest_blkcnt = ov.lowest_blkcnt
+            ref = orc.render(ov, wl.TF9, op, view_array(hy.camera_view(vol, c)), W, H)["rgba"]
+            got = out.cpu().numpy().reshape(H, W, 4)
+            assert np.abs(got.astype(int) - ref.astype(int)).max() <= 1, f"frame {f}"
+        assert pg.stats()["fallback"] > 0
+    finally:
+        ov.set_present(np.ones(nb, np.uint8))
+        pg.close()
+        store.close()
+        vol.close()
