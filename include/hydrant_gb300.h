@@ -308,6 +308,9 @@ int hy_store_ingest_raw(hy_ctx *ctx, const char *raw_path, const hy_volume_desc 
 int hy_cull(const hy_volume *vol, const hy_view *view, const float rect[4], int32_t limit,
             int32_t *ids_out, float *dist2_out, int32_t *n_out);
 
+/* The store must outlive the pager (the pager's kernels read the store's
+ * pinned memory); hy_pager_destroy waits for the pager's queued work.  A
+ * coarse level must be built before the pager is created. */
 int hy_pager_create(hy_ctx *ctx, hy_store *store, const hy_pager_desc *desc, hy_pager **out);
 int hy_pager_destroy(hy_pager *pager);
 /* The paged volume (for hy_cull / hy_render); owned by the pager. */
