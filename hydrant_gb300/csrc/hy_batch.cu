@@ -314,6 +314,17 @@ int layout(hy_batch *b) {
 
 int launch(hy_batch *b, uint8_t *out) {
     hy_ctx *ctx = b->ctx;
+    // the batch renders with the context's current transfer function: a new
+    // table (hy_tf_set may have reallocated it) or knot count means new
+    // kernel arguments, shared-memory size and graph
+    if (b->base.tf != ctx->tf_dev || b->base.ntf != ctx->ntf) {
+        if (b->params.shader == HY_SHADER_VOLUME && ctx->ntf <= 0)
+            return hy_fail(ctx, HY_ERR_STATE, "batch: Volume shader needs a transfer function");
+        b->base.tf = ctx->tf_dev;
+        b->base.ntf = ctx->ntf;
+        int rc = layout(b);
+        if (rc) return rc;
+    }
     const int count = b->params.count_samples ? 1 : 0;
     if (!b->exec || b->graph_out != out || b->graph_count != count) {
         drop_graph(b);

@@ -400,6 +400,8 @@ typedef struct hy_batch_config {
                               tile and its warps shade neighbouring warp tiles */
 } hy_batch_config;
 
+/* The batch keeps `vol`, which must outlive it; every render uses the
+ * context's transfer function as set at that time (hy_tf_set). */
 int hy_batch_create(hy_ctx *ctx, const hy_volume *vol, const hy_shader_params *params,
                     const hy_batch_view *views, int32_t nviews, hy_batch **out);
 int hy_batch_destroy(hy_batch *batch);

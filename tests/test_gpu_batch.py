@@ -143,3 +143,28 @@ def test_batch_equals_per_view_p66(ctx, blobs_bs64, mode):
                 assert np.array_equal(g, r), f"view {i} differs with config {cfg}"
     finally:
         b.close()
+
+
+def test_batch_follows_the_transfer_function(ctx, tubes):
+    """A batch renders with the context's current transfer function, also
+    after hy_tf_set grew the table (a new device allocation) or shrank it."""
+    torch = pytest.importorskip("torch")
+    views, cams = _views(tubes, SIZES[:4], seed=23)
+    kw = dict(shader="Volume", density=0.5, sample_rate=0.5)
+    ctx.set_transfer_fn(wl.TF9)
+    b = hy.Batch(ctx, tubes, hy.shader_params(**kw), views)
+    try:
+        out = torch.empty(b.nbytes, dtype=torch.uint8, device="cuda")
+        rng = np.random.default_rng(4)
+        for n in (300, 5, 9):  # larger than any earlier table, then smaller
+            tf = rng.uniform(0, 1, (n, 4)).astype(np.float32)
+            tf[0] = 0
+            ctx.set_transfer_fn(tf)
+            ref, _ = _per_view(ctx, tubes, kw, views, cams)
+            b.render_device(out.data_ptr())
+            ctx.synchronize()
+            for g, r in zip(b.split(out.cpu().numpy()), ref):
+                assert np.array_equal(g, r), f"{n} knots"
+    finally:
+        ctx.set_transfer_fn(wl.TF9)
+        b.close()
