@@ -290,6 +290,9 @@ extern "C" int hy_volume_destroy(hy_volume *vol) {
 
 extern "C" int hy_volume_upload(hy_volume *vol, const void *host_voxels) {
     if (!vol || !host_voxels) return HY_ERR_INVALID;
+    if (vol->uploaded || vol->paged)
+        return hy_fail(vol->ctx, HY_ERR_STATE,
+                       "volume: already has its bricks (create a new volume for new data)");
     HY_CUDA(vol->ctx, cudaSetDevice(vol->ctx->device));
     if (vol->desc.dtype == HY_DTYPE_U8) return upload_impl<unsigned char>(vol, host_voxels);
     return upload_impl<float>(vol, host_voxels);

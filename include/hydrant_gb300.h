@@ -196,7 +196,8 @@ int hy_volume_destroy(hy_volume *vol);
  * device with a replicate-edge apron, builds the chebyshev and mean
  * thumbnails and makes every non-empty brick resident.  Replaces the
  * decode + Texture3D::source upload of LosslessBlockPagingServer (
- * src/slave/paging/lossless_block_paging.cc:137-174) for resident volumes. */
+ * src/slave/paging/lossless_block_paging.cc:137-174) for resident volumes.
+ * Once per volume (HY_ERR_STATE after that): new data is a new volume. */
 int hy_volume_upload(hy_volume *vol, const void *host_voxels);
 int hy_volume_get_info(const hy_volume *vol, hy_volume_info *out);
 /* Copy the per-brick thumbnails to the host (grid x fastest). */

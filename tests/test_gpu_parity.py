@@ -230,3 +230,18 @@ def test_paging_shader(tubes128, blobs64):
     with pytest.raises(hy.HydrantError):
         p = hy.shader_params(shader="Paging", composite=True)
         hy.render(tubes128.ctx, tubes128.vol, p, hy.camera_view(tubes128.vol, camera()), 8, 8)
+
+
+def test_second_upload_is_rejected(ctx):
+    vox = hy.synth_blobs_u8(0, (32, 32, 32), 4)
+    vol = hy.Volume(ctx, vox, 16, 1)
+    try:
+        rc = hy.lib().hy_volume_upload(vol.handle, vox.ctypes.data_as(hy._abi.C.c_void_p))
+        assert rc == hy._abi.HY_ERR_STATE
+        # the volume still renders
+        ctx.set_transfer_fn(wl.TF9)
+        r = hy.render(ctx, vol, hy.shader_params(shader="Volume"), hy.camera_view(vol, camera()),
+                      16, 16)
+        assert r.rgba.shape == (16, 16, 4)
+    finally:
+        vol.close()
