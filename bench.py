@@ -459,8 +459,13 @@ def main_ours(args):
     hbm, peak_kind = measured_peaks()
     mean_launch_s = t / args.steps  # one batch kernel per step
     achieved = samples * BYTES_PER_SAMPLE / mean_launch_s / 1e9
-    tps = profile_per_sample(int(tuned.get("block_queue", 1)))
-    ipsm = profile_per_sample(int(tuned.get("block_queue", 1)), "warp_instructions_per_sample")
+    # the profiled per-sample figures hold for the Volume shader on the blob
+    # volume they were captured on, not for the other workloads
+    tps = ipsm = None
+    if args.workload == "multiview":
+        tps = profile_per_sample(int(tuned.get("block_queue", 1)))
+        ipsm = profile_per_sample(int(tuned.get("block_queue", 1)),
+                                  "warp_instructions_per_sample")
     if rank == 0:
         cpu = None
         parity = None

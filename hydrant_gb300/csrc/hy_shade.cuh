@@ -24,6 +24,36 @@ __device__ __forceinline__ float fsign(float x) { return float((0.f < x) - (x < 
 // float -> int: truncation, saturating, NaN -> 0 (the hardware conversion;
 // the oracle defines the same, C++ leaves these cases undefined).
 __device__ __forceinline__ int f2i(float x) { return int(x); }
+
+// Two-lane float arithmetic (sm_100 and later).  Each lane rounds exactly as
+// the scalar __fmul_rn / __fadd_rn / __fmaf_rn does, so packing two
+// independent operations of the march changes no result, only the number of
+// instructions issued.  There is no packed subtract: a - b is fma(b, -1, a),
+// whose product is exact, so its one rounding is that of a - b (signed zeros,
+// infinities and NaN included).
+// One rule keeps it exact: a packed product is never an operand of a packed
+// add.  The assembler fuses a packed multiply whose only use is a packed add
+// (or fma(p, 1, q)) into one fused multiply-add, even for .rn instructions
+// and with contraction disabled -- measured on GB300: 161,347 of 2,097,152
+// lanes of fl(fl(a*b) + fl(c*d)) came out fused, while packed products summed
+// by scalar adds, and scalar products summed by a packed add, matched bit for
+// bit.  So products here are summed by scalar __fadd_rn.  HY_F32X2=0 builds
+// the scalar forms.
+#ifndef HY_F32X2
+#define HY_F32X2 1
+#endif
+__device__ __forceinline__ float2 f2(float x, float y) { return make_float2(x, y); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
+    return __ffma2_rn(b, make_float2(-1.f, -1.f), a);
+}
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+// x * w + y * v per lane, products rounded separately (the reference's lerp
+// x*(1-a) + y*a with w = 1-a, v = a): packed products, scalar sums
+__device__ __forceinline__ float2 lerp2(float2 x, float2 w, float2 y, float2 v) {
+    const float2 p = mul2(x, w), q = mul2(y, v);
+    return f2(__fadd_rn(p.x, q.x), __fadd_rn(p.y, q.y));
+}
 // Steps skipped over empty bricks.  The reference's value is a small
 // non-negative integer; NaN / negative / huge (degenerate rays only) are
 // pinned to [0, 2^30] so nsteps can never overflow and the loop always ends.
@@ -130,6 +160,13 @@ __device__ __forceinline__ float u8_norm(unsigned int u) {
     const float x = __uint2float_rn(u);
     return __fmaf_rn(x, hi, __fmul_rn(x, lo));
 }
+// two voxels at once, same operations per lane
+__device__ __forceinline__ float2 u8_norm2(unsigned int a, unsigned int b) {
+    constexpr float hi = 1.f / 255.f;
+    constexpr float lo = float(1.0 / 255.0 - double(1.f / 255.f));
+    const float2 x = f2(__uint2float_rn(a), __uint2float_rn(b));
+    return fma2(x, f2(hi, hi), mul2(x, f2(lo, lo)));
+}
 __device__ __forceinline__ float lut_at(const float *__restrict__ lut, unsigned int u) {
     return lut[u];
 }
@@ -143,18 +180,33 @@ __device__ __forceinline__ float sample_brick(const BrickRef &b, int Prt, float 
                                               float lz, const float *__restrict__ lut) {
     const int P = PC ? PC : Prt;
     const float fd = float(P);
+#if HY_F32X2
+    // x and y in packed pairs, z alone; per lane the scalar sequence below
+    const float2 kl = mul2(f2(b.k, b.k), f2(lx, ly));
+    const float2 fxy0 = mul2(f2(fd, fd), f2(__fadd_rn(kl.x, b.bx), __fadd_rn(kl.y, b.by)));
+    float fx = fxy0.x, fy = fxy0.y, fz = fd * (b.k * lz + b.bz);
+#else
     float mx = b.k * lx + b.bx, my = b.k * ly + b.by, mz = b.k * lz + b.bz;
     float fx = fd * mx, fy = fd * my, fz = fd * mz;
+#endif
     if (!INTERIOR) {
         if (!(fx >= 0.f && fx < fd)) fx = fx - fd * floorf(fx / fd);
         if (!(fy >= 0.f && fy < fd)) fy = fy - fd * floorf(fy / fd);
         if (!(fz >= 0.f && fz < fd)) fz = fz - fd * floorf(fz / fd);
     }
+#if HY_F32X2
+    const float ux = fx - .5f, uy = fy - .5f, uz = fz - .5f;  // fx, fy are products
+    const float flx = floorf(ux), fly = floorf(uy), flz = floorf(uz);
+    const float2 axy = sub2(f2(ux, uy), f2(flx, fly));
+    const float az = uz - flz;
+#else
     float ux = fx - .5f, uy = fy - .5f, uz = fz - .5f;
     float flx = floorf(ux), fly = floorf(uy), flz = floorf(uz);
     float ax = ux - flx, ay = uy - fly, az = uz - flz;
+#endif
     int ix = int(flx), iy = int(fly), iz = int(flz);
-    float v000, v100, v010, v110, v001, v101, v011, v111;
+    // the eight taps in z pairs: c<y><x> holds the taps at (x, y) of layers z and z+1
+    float2 c00, c01, c10, c11;
     if (INTERIOR ||
         (ix >= 0 && ix <= P - 2 && iy >= 0 && iy <= P - 2 && iz >= 0 && iz <= P - 2)) {
         // a compile-time brick edge (<= 130) keeps the offset in 32 bits
@@ -162,24 +214,27 @@ __device__ __forceinline__ float sample_brick(const BrickRef &b, int Prt, float 
                                   : ((long long)iz * P + iy) * P + ix;
         if (DT == HY_DTYPE_U8) {
             const unsigned char *q = b.base + base;
-            v000 = u8_value<0>(__ldg(q), lut);
-            v100 = u8_value<1>(__ldg(q + 1), lut);
-            v010 = u8_value<2>(__ldg(q + P), lut);
-            v110 = u8_value<3>(__ldg(q + P + 1), lut);
-            v001 = u8_value<4>(__ldg(q + P * P), lut);
-            v101 = u8_value<5>(__ldg(q + P * P + 1), lut);
-            v011 = u8_value<6>(__ldg(q + P * P + P), lut);
-            v111 = u8_value<7>(__ldg(q + P * P + P + 1), lut);
+#if HY_F32X2
+            c00 = u8_norm2(__ldg(q), __ldg(q + P * P));
+            c01 = u8_norm2(__ldg(q + 1), __ldg(q + P * P + 1));
+            c10 = u8_norm2(__ldg(q + P), __ldg(q + P * P + P));
+            c11 = u8_norm2(__ldg(q + P + 1), __ldg(q + P * P + P + 1));
+#else
+            c00.x = u8_value<0>(__ldg(q), lut);
+            c01.x = u8_value<1>(__ldg(q + 1), lut);
+            c10.x = u8_value<2>(__ldg(q + P), lut);
+            c11.x = u8_value<3>(__ldg(q + P + 1), lut);
+            c00.y = u8_value<4>(__ldg(q + P * P), lut);
+            c01.y = u8_value<5>(__ldg(q + P * P + 1), lut);
+            c10.y = u8_value<6>(__ldg(q + P * P + P), lut);
+            c11.y = u8_value<7>(__ldg(q + P * P + P + 1), lut);
+#endif
         } else {
             const float *q = reinterpret_cast<const float *>(b.base) + base;
-            v000 = __ldg(q);
-            v100 = __ldg(q + 1);
-            v010 = __ldg(q + P);
-            v110 = __ldg(q + P + 1);
-            v001 = __ldg(q + P * P);
-            v101 = __ldg(q + P * P + 1);
-            v011 = __ldg(q + P * P + P);
-            v111 = __ldg(q + P * P + P + 1);
+            c00 = f2(__ldg(q), __ldg(q + P * P));
+            c01 = f2(__ldg(q + 1), __ldg(q + P * P + 1));
+            c10 = f2(__ldg(q + P), __ldg(q + P * P + P));
+            c11 = f2(__ldg(q + P + 1), __ldg(q + P * P + P + 1));
         }
     } else {
         int jx = iclamp(int(ceilf(ux)), 0, P - 1), jy = iclamp(int(ceilf(uy)), 0, P - 1),
@@ -191,34 +246,39 @@ __device__ __forceinline__ float sample_brick(const BrickRef &b, int Prt, float 
                         r01 = ((long long)jz * P + iy) * P, r11 = ((long long)jz * P + jy) * P;
         if (DT == HY_DTYPE_U8) {
             const unsigned char *q = b.base;
-            v000 = lut_at(lut, __ldg(q + r00 + ix));
-            v100 = lut_at(lut, __ldg(q + r00 + jx));
-            v010 = lut_at(lut, __ldg(q + r10 + ix));
-            v110 = lut_at(lut, __ldg(q + r10 + jx));
-            v001 = lut_at(lut, __ldg(q + r01 + ix));
-            v101 = lut_at(lut, __ldg(q + r01 + jx));
-            v011 = lut_at(lut, __ldg(q + r11 + ix));
-            v111 = lut_at(lut, __ldg(q + r11 + jx));
+            c00 = f2(lut_at(lut, __ldg(q + r00 + ix)), lut_at(lut, __ldg(q + r01 + ix)));
+            c01 = f2(lut_at(lut, __ldg(q + r00 + jx)), lut_at(lut, __ldg(q + r01 + jx)));
+            c10 = f2(lut_at(lut, __ldg(q + r10 + ix)), lut_at(lut, __ldg(q + r11 + ix)));
+            c11 = f2(lut_at(lut, __ldg(q + r10 + jx)), lut_at(lut, __ldg(q + r11 + jx)));
         } else {
             const float *q = reinterpret_cast<const float *>(b.base);
-            v000 = __ldg(q + r00 + ix);
-            v100 = __ldg(q + r00 + jx);
-            v010 = __ldg(q + r10 + ix);
-            v110 = __ldg(q + r10 + jx);
-            v001 = __ldg(q + r01 + ix);
-            v101 = __ldg(q + r01 + jx);
-            v011 = __ldg(q + r11 + ix);
-            v111 = __ldg(q + r11 + jx);
+            c00 = f2(__ldg(q + r00 + ix), __ldg(q + r01 + ix));
+            c01 = f2(__ldg(q + r00 + jx), __ldg(q + r01 + jx));
+            c10 = f2(__ldg(q + r10 + ix), __ldg(q + r11 + ix));
+            c11 = f2(__ldg(q + r10 + jx), __ldg(q + r11 + jx));
         }
     }
+#if HY_F32X2
+    // lerp along x of both z layers at once, then along y, then z:
+    // X0 = (x0_0, x0_1), X1 = (x1_0, x1_1), Y = (y0, y1)
+    const float2 bxy = sub2(f2(1.f, 1.f), axy);
+    const float bz = 1.f - az;
+    const float2 bx2 = f2(bxy.x, bxy.x), ax2 = f2(axy.x, axy.x);
+    const float2 X0 = lerp2(c00, bx2, c01, ax2);
+    const float2 X1 = lerp2(c10, bx2, c11, ax2);
+    const float2 Y = lerp2(X0, f2(bxy.y, bxy.y), X1, f2(axy.y, axy.y));
+    const float2 Z = mul2(Y, f2(bz, az));
+    return __fadd_rn(Z.x, Z.y);
+#else
     const float bx = 1.f - ax, by = 1.f - ay, bz = 1.f - az;
-    float x0_0 = v000 * bx + v100 * ax;
-    float x1_0 = v010 * bx + v110 * ax;
-    float x0_1 = v001 * bx + v101 * ax;
-    float x1_1 = v011 * bx + v111 * ax;
+    float x0_0 = c00.x * bx + c01.x * ax;
+    float x1_0 = c10.x * bx + c11.x * ax;
+    float x0_1 = c00.y * bx + c01.y * ax;
+    float x1_1 = c10.y * bx + c11.y * ax;
     float y0 = x0_0 * by + x1_0 * ay;
     float y1 = x0_1 * by + x1_1 * ay;
     return y0 * bz + y1 * az;
+#endif
 }
 
 // TransferFn lookup: 1-D, normalised, Border, Linear (transfer_fn.hpp:16-23,
@@ -239,7 +299,14 @@ __device__ __forceinline__ float4 sample_tf(const float4 *__restrict__ tf, int n
     int j = min(fi + 1, n - 1);
     float4 x = tf[i], y = tf[j];
     float b = 1.f - a;
+#if HY_F32X2
+    const float2 bb = f2(b, b), aa = f2(a, a);
+    const float2 rg = lerp2(f2(x.x, x.y), bb, f2(y.x, y.y), aa);
+    const float2 ba = lerp2(f2(x.z, x.w), bb, f2(y.z, y.w), aa);
+    return make_float4(rg.x, rg.y, ba.x, ba.y);
+#else
     return make_float4(x.x * b + y.x * a, x.y * b + y.y * a, x.z * b + y.z * a, x.w * b + y.w * a);
+#endif
 }
 
 struct Shared {
@@ -298,8 +365,14 @@ struct BrickCursor {
     // brick-local coordinates of o, relocating first when o left the cell
     __device__ __forceinline__ void update(const DevVolume &V, float ox, float oy, float oz,
                                            float &lx, float &ly, float &lz) {
+#if HY_F32X2
+        const float2 lxy = sub2(f2(ox, oy), f2(ipx, ipy));
+        lx = lxy.x;
+        ly = lxy.y;
+#else
         lx = ox - ipx;
         ly = oy - ipy;
+#endif
         lz = oz - ipz;
         if (unit_interval(lx) & unit_interval(ly) & unit_interval(lz)) return;
         locate(V, ox, oy, oz);
@@ -360,8 +433,14 @@ struct VolumeMarch {
             }
             ub.w = ub.w * A.density;  // opacity scale; exact identity at 1
             const float w = ub.w;
+#if HY_F32X2
+            const float2 uxy = mul2(f2(ub.x, ub.y), f2(w, w));
+            ub.x = uxy.x;
+            ub.y = uxy.y;
+#else
             ub.x = ub.x * w;
             ub.y = ub.y * w;
+#endif
             ub.z = ub.z * w;
             if (!LEAN) {
                 p.e0 = p.e0 + ub.x * p.e3;
@@ -370,10 +449,19 @@ struct VolumeMarch {
                 p.e3 = p.e3 * (1.f - ub.w);
             }
             const float t = 1.f - p.vw;
+#if HY_F32X2
+            const float2 txy = mul2(f2(ub.x, ub.y), f2(t, t));
+            const float2 tzw = mul2(f2(ub.z, ub.w), f2(t, t));
+            p.vx = __fadd_rn(p.vx, txy.x);
+            p.vy = __fadd_rn(p.vy, txy.y);
+            p.vz = __fadd_rn(p.vz, tzw.x);
+            p.vw = __fadd_rn(p.vw, tzw.y);
+#else
             p.vx = p.vx + ub.x * t;
             p.vy = p.vy + ub.y * t;
             p.vz = p.vz + ub.z * t;
             p.vw = p.vw + ub.w * t;
+#endif
             if (p.vw >= HY_T93) {
                 p.step_size = 16;
             } else if (p.vw >= HY_T85) {
@@ -387,7 +475,7 @@ struct VolumeMarch {
             sy = (p.dy * A.step) * fs;
             sz = (p.dz * A.step) * fs;
         }
-        p.ox = p.ox + sx;
+        p.ox = p.ox + sx;  // sx..sz are products: scalar adds
         p.oy = p.oy + sy;
         p.oz = p.oz + sz;
         p.nsteps -= p.step_size;
