@@ -88,6 +88,8 @@ def workload(args):
     if args.res:
         w.views = [v for v in w.views if v.width == args.res] or w.views[:1]
         w.views = w.views[: max(1, args.views)]
+        # the cameras of the set that render at this resolution
+        w.name = f"multiview_c3_{w.dim[0]}cube_{len(w.views)}views_at_{args.res}px"
     return w
 
 
