@@ -77,11 +77,15 @@ __device__ __forceinline__ void diff_cell(const DiffArgs &a, float lx, float ly,
                                           Cell &c) {
     const int P = a.n + 2;
     const float fd = float(P);
-    const float fx = fd * (a.k * lx + a.b), fy = fd * (a.k * ly + a.b), fz = fd * (a.k * lz + a.b);
-    const float ux = fx - .5f, uy = fy - .5f, uz = fz - .5f;
+    // x and y in packed pairs (products summed by scalar adds), z alone
+    const float2 kl = mul2(f2(a.k, a.k), f2(lx, ly));
+    const float2 fxy = mul2(f2(fd, fd), f2(__fadd_rn(kl.x, a.b), __fadd_rn(kl.y, a.b)));
+    const float fz = fd * (a.k * lz + a.b);
+    const float ux = fxy.x - .5f, uy = fxy.y - .5f, uz = fz - .5f;
     const float flx = floorf(ux), fly = floorf(uy), flz = floorf(uz);
-    c.ax = ux - flx;
-    c.ay = uy - fly;
+    const float2 axy = sub2(f2(ux, uy), f2(flx, fly));
+    c.ax = axy.x;
+    c.ay = axy.y;
     c.az = uz - flz;
     const int ix = int(flx), iy = int(fly), iz = int(flz);
     // padded index i -> raw clamp(i - 1, 0, n - 1)
@@ -97,18 +101,19 @@ __device__ __forceinline__ void diff_cell(const DiffArgs &a, float lx, float ly,
 }
 
 __device__ __forceinline__ float diff_fetch(const DiffArgs &a, const Cell &c) {
-    const float v000 = __ldg(a.vol + c.r00 + c.x0), v100 = __ldg(a.vol + c.r00 + c.x1);
-    const float v010 = __ldg(a.vol + c.r10 + c.x0), v110 = __ldg(a.vol + c.r10 + c.x1);
-    const float v001 = __ldg(a.vol + c.r01 + c.x0), v101 = __ldg(a.vol + c.r01 + c.x1);
-    const float v011 = __ldg(a.vol + c.r11 + c.x0), v111 = __ldg(a.vol + c.r11 + c.x1);
-    const float bx = 1.f - c.ax, by = 1.f - c.ay, bz = 1.f - c.az;
-    const float x0_0 = v000 * bx + v100 * c.ax;
-    const float x1_0 = v010 * bx + v110 * c.ax;
-    const float x0_1 = v001 * bx + v101 * c.ax;
-    const float x1_1 = v011 * bx + v111 * c.ax;
-    const float yy0 = x0_0 * by + x1_0 * c.ay;
-    const float yy1 = x0_1 * by + x1_1 * c.ay;
-    return yy0 * bz + yy1 * c.az;
+    // taps in z pairs: c<y><x> = (v_xy0, v_xy1); the lerps of sample_brick
+    const float2 c00 = f2(__ldg(a.vol + c.r00 + c.x0), __ldg(a.vol + c.r01 + c.x0));
+    const float2 c01 = f2(__ldg(a.vol + c.r00 + c.x1), __ldg(a.vol + c.r01 + c.x1));
+    const float2 c10 = f2(__ldg(a.vol + c.r10 + c.x0), __ldg(a.vol + c.r11 + c.x0));
+    const float2 c11 = f2(__ldg(a.vol + c.r10 + c.x1), __ldg(a.vol + c.r11 + c.x1));
+    const float2 bxy = sub2(f2(1.f, 1.f), f2(c.ax, c.ay));
+    const float bz = 1.f - c.az;
+    const float2 bx2 = f2(bxy.x, bxy.x), ax2 = f2(c.ax, c.ax);
+    const float2 X0 = lerp2(c00, bx2, c01, ax2);  // (x0_0, x0_1)
+    const float2 X1 = lerp2(c10, bx2, c11, ax2);  // (x1_0, x1_1)
+    const float2 Y = lerp2(X0, f2(bxy.y, bxy.y), X1, f2(c.ay, c.ay));
+    const float2 Z = mul2(Y, f2(bz, c.az));
+    return __fadd_rn(Z.x, Z.y);
 }
 
 __device__ __forceinline__ float diff_sample(const DiffArgs &a, float lx, float ly, float lz) {
@@ -162,8 +167,10 @@ __device__ __forceinline__ float4 tf_eval(const float4 *tf, int n, float s, int 
     j = min(fi + 1, n - 1);
     const float4 p = tf[i], q = tf[j];
     const float bb = 1.f - al;
-    return make_float4(p.x * bb + q.x * al, p.y * bb + q.y * al, p.z * bb + q.z * al,
-                       p.w * bb + q.w * al);
+    const float2 b2 = f2(bb, bb), a2 = f2(al, al);
+    const float2 rg = lerp2(f2(p.x, p.y), b2, f2(q.x, q.y), a2);
+    const float2 ba = lerp2(f2(p.z, p.w), b2, f2(q.z, q.w), a2);
+    return make_float4(rg.x, rg.y, ba.x, ba.y);
 }
 
 __device__ __forceinline__ void pixel_of(const DiffArgs &a, int &x, int &y, int &view) {
@@ -201,14 +208,15 @@ __global__ void __launch_bounds__(128) diff_forward_kernel(const __grid_constant
         float4 ub = tf_eval(tf, a.ntf, val, i, j, al, inb);
         ub.w = ub.w * a.density;
         const float w = ub.w;
-        ub.x = ub.x * w;
-        ub.y = ub.y * w;
+        const float2 uxy = mul2(f2(ub.x, ub.y), f2(w, w));
         ub.z = ub.z * w;
         const float t = 1.f - v.w;
-        v.x = v.x + ub.x * t;
-        v.y = v.y + ub.y * t;
-        v.z = v.z + ub.z * t;
-        v.w = v.w + ub.w * t;
+        // packed products, scalar sums (see mul2)
+        const float2 txy = mul2(uxy, f2(t, t)), tzw = mul2(f2(ub.z, ub.w), f2(t, t));
+        v.x = __fadd_rn(v.x, txy.x);
+        v.y = __fadd_rn(v.y, txy.y);
+        v.z = __fadd_rn(v.z, tzw.x);
+        v.w = __fadd_rn(v.w, tzw.y);
         ox = ox + sx;
         oy = oy + sy;
         oz = oz + sz;
@@ -266,31 +274,36 @@ __device__ __forceinline__ void diff_adjoint_sample(const DiffArgs &a, const flo
     // The gradient arithmetic has no float-exact counterpart to follow, so it
     // uses fused multiply-adds (the file is compiled with contraction off).
     // dL/dc = T g ; transmittance term through later samples
-    const float gcx = T * g.x, gcy = T * g.y, gcz = T * g.z, gcw = T * g.w;
+    const float2 gcxy = mul2(f2(T, T), f2(g.x, g.y)), gczw = mul2(f2(T, T), f2(g.z, g.w));
+    const float gcx = gcxy.x, gcy = gcxy.y, gcz = gczw.x, gcw = gczw.y;
     const float gdot = __fmaf_rn(g.w, R.w, __fmaf_rn(g.z, R.z, __fmaf_rn(g.y, R.y, g.x * R.x)));
     const float da =
         __fmaf_rn(-T, gdot, __fmaf_rn(gcz, q.z, __fmaf_rn(gcy, q.y, __fmaf_rn(gcx, q.x, gcw))));
     // R_n = c_n + (1 - a_n) R_{n+1}
     const float om = 1.f - aa;
-    R = make_float4(__fmaf_rn(om, R.x, q.x * aa), __fmaf_rn(om, R.y, q.y * aa),
-                    __fmaf_rn(om, R.z, q.z * aa), __fmaf_rn(om, R.w, aa));
+    const float2 om2 = f2(om, om);
+    const float2 Rxy = fma2(om2, f2(R.x, R.y), mul2(f2(q.x, q.y), f2(aa, aa)));
+    const float2 Rzw = fma2(om2, f2(R.z, R.w), f2(q.z * aa, aa));
+    R = make_float4(Rxy.x, Rxy.y, Rzw.x, Rzw.y);
     if (!inb) return;
     // gradient of the TF output (r, g, b, A)
-    const float4 gq = make_float4(gcx * aa, gcy * aa, gcz * aa, da * a.density);
+    const float2 gqxy = mul2(gcxy, f2(aa, aa)), gqzw = mul2(f2(gcz, da), f2(aa, a.density));
+    const float4 gq = make_float4(gqxy.x, gqxy.y, gqzw.x, gqzw.y);
     const float bb = 1.f - al;
     if (i != G.ki || j != G.kj) {
         G.flush_knots(gtf);
         G.ki = i;
         G.kj = j;
     }
-    G.acc_i.x = __fmaf_rn(gq.x, bb, G.acc_i.x);
-    G.acc_i.y = __fmaf_rn(gq.y, bb, G.acc_i.y);
-    G.acc_i.z = __fmaf_rn(gq.z, bb, G.acc_i.z);
-    G.acc_i.w = __fmaf_rn(gq.w, bb, G.acc_i.w);
-    G.acc_j.x = __fmaf_rn(gq.x, al, G.acc_j.x);
-    G.acc_j.y = __fmaf_rn(gq.y, al, G.acc_j.y);
-    G.acc_j.z = __fmaf_rn(gq.z, al, G.acc_j.z);
-    G.acc_j.w = __fmaf_rn(gq.w, al, G.acc_j.w);
+    {
+        const float2 b2 = f2(bb, bb), a2 = f2(al, al);
+        const float2 ixy = fma2(gqxy, b2, f2(G.acc_i.x, G.acc_i.y));
+        const float2 izw = fma2(gqzw, b2, f2(G.acc_i.z, G.acc_i.w));
+        const float2 jxy = fma2(gqxy, a2, f2(G.acc_j.x, G.acc_j.y));
+        const float2 jzw = fma2(gqzw, a2, f2(G.acc_j.z, G.acc_j.w));
+        G.acc_i = make_float4(ixy.x, ixy.y, izw.x, izw.y);
+        G.acc_j = make_float4(jxy.x, jxy.y, jzw.x, jzw.y);
+    }
     // d TF / d s = (knot_j - knot_i) * n
     const float4 kj = tf[j], ki = tf[i];
     const float fn = float(a.ntf);
@@ -311,16 +324,22 @@ __device__ __forceinline__ void diff_adjoint_sample(const DiffArgs &a, const flo
     // trilinear weights w = (x-weight) * (y-weight) * (z-weight), times ds
     const float ax = c.ax, ay = c.ay, az = c.az;
     const float bx = 1.f - ax, by = 1.f - ay, bz = 1.f - az;
-    const float d00 = ds * (by * bz), d10 = ds * (ay * bz), d01 = ds * (by * az),
-                d11 = ds * (ay * az);
-    G.cacc[0] = __fmaf_rn(bx, d00, G.cacc[0]);
-    G.cacc[1] = __fmaf_rn(ax, d00, G.cacc[1]);
-    G.cacc[2] = __fmaf_rn(bx, d10, G.cacc[2]);
-    G.cacc[3] = __fmaf_rn(ax, d10, G.cacc[3]);
-    G.cacc[4] = __fmaf_rn(bx, d01, G.cacc[4]);
-    G.cacc[5] = __fmaf_rn(ax, d01, G.cacc[5]);
-    G.cacc[6] = __fmaf_rn(bx, d11, G.cacc[6]);
-    G.cacc[7] = __fmaf_rn(ax, d11, G.cacc[7]);
+    const float2 ds2 = f2(ds, ds), yw = f2(by, ay);
+    const float2 dz0 = mul2(ds2, mul2(yw, f2(bz, bz)));  // (d00, d10)
+    const float2 dz1 = mul2(ds2, mul2(yw, f2(az, az)));  // (d01, d11)
+    const float2 xw = f2(bx, ax);
+    const float2 c01 = fma2(xw, f2(dz0.x, dz0.x), f2(G.cacc[0], G.cacc[1]));
+    const float2 c23 = fma2(xw, f2(dz0.y, dz0.y), f2(G.cacc[2], G.cacc[3]));
+    const float2 c45 = fma2(xw, f2(dz1.x, dz1.x), f2(G.cacc[4], G.cacc[5]));
+    const float2 c67 = fma2(xw, f2(dz1.y, dz1.y), f2(G.cacc[6], G.cacc[7]));
+    G.cacc[0] = c01.x;
+    G.cacc[1] = c01.y;
+    G.cacc[2] = c23.x;
+    G.cacc[3] = c23.y;
+    G.cacc[4] = c45.x;
+    G.cacc[5] = c45.y;
+    G.cacc[6] = c67.x;
+    G.cacc[7] = c67.y;
 }
 
 // The adjoint walks a ray's segments back to front; a segment's recomputed

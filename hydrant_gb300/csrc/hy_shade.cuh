@@ -616,7 +616,6 @@ __device__ __forceinline__ long long iso_main(Px &p, const ShadeArgs &A, const V
     long long samples = 0;
     const float cdu = 1.f / gmax(gmax(fabsf(p.dx), fabsf(p.dy)), fabsf(p.dz));
     const float rx = 1.f / p.dx, ry = 1.f / p.dy, rz = 1.f / p.dz;
-    const float fgx = float(V.gx), fgy = float(V.gy), fgz = float(V.gz);
     const float prev_value = 0.0f;
     const float iso = A.isovalue;
     const float prev_sign = fsign(prev_value - iso);
