@@ -65,6 +65,8 @@ def parse_args():
                     help="paging: the realtime cache or lossless batches (offline frames)")
     ap.add_argument("--lossless-batch", type=int, default=4096,
                     help="paging, lossless: bricks per batch (the reference caps it at 4096)")
+    ap.add_argument("--cache-gib", type=float, default=8.0,
+                    help="paging workload: device brick cache of the realtime pager")
     ap.add_argument("--max-uploads", type=int, default=0,
                     help="paging: brick uploads per frame (0 = every missing brick)")
     ap.add_argument("--launch-shape", default="",
@@ -571,7 +573,7 @@ def main_paging(args):
         slots = args.lossless_batch
         pg = hy.Pager(ctx, store, slots, _abi.PAGER_LOSSLESS)
     else:
-        slots = int((8 * 2**30) // si.slot_bytes)
+        slots = int((args.cache_gib * 2**30) // si.slot_bytes)
         pg = hy.Pager(ctx, store, slots, _abi.PAGER_REALTIME, args.max_uploads)
     p = hy.shader_params(shader="Volume", sample_rate=0.25, density=5e-3)
     pc = hy.shader_params(shader="Volume", sample_rate=0.25, density=5e-3, count_samples=True)
@@ -617,7 +619,8 @@ def main_paging(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
         "config": {"workload": f"paging_{dim[0]}x{dim[1]}x{dim[2]}_{res}px", "block_size": 64,
-                   "pager": args.pager, "cache_gib": 8 if args.pager == "realtime" else None,
+                   "pager": args.pager,
+                   "cache_gib": args.cache_gib if args.pager == "realtime" else None,
                    "cache_slots": slots, "store_bricks": si.nonempty,
                    "store_gb": si.pool_bytes / 1e9, "store_build_s": t_store,
                    "coarse_level": args.coarse_level, "coarse_build_s": t_coarse,
