@@ -76,10 +76,25 @@ def parse_args():
                     help="use the default batch launch shape (profiling)")
     ap.add_argument("--cpu-sample-rows", type=int, default=0,
                     help="rows of the CPU-baseline sample (0 = auto)")
+    ap.add_argument("--shader", choices=["Volume", "Blocks", "Isosurface"], default="",
+                    help="tubes / volume / multiview: render with this shader instead")
+    ap.add_argument("--mode", default="",
+                    help="with --shader: its mode (Volume: Default / Partition / Paging; "
+                         "Blocks: Volume / Solid; Isosurface: Color / Normal / Position)")
+    ap.add_argument("--composite", action="store_true",
+                    help="per-brick partial images composited front to back (sort-last)")
+    ap.add_argument("--sample-rate", type=float, default=0.0,
+                    help="override the workload's sample rate (step = du / 4 / rate)")
+    ap.add_argument("--density", type=float, default=None,
+                    help="override the workload's density")
     return ap.parse_args()
 
 
 def workload(args):
+    return with_overrides(args, base_workload(args))
+
+
+def base_workload(args):
     from hydrant_gb300 import workloads as wl
 
     if args.workload == "volume":
@@ -92,6 +107,32 @@ def workload(args):
         w.views = w.views[: max(1, args.views)]
         # the cameras of the set that render at this resolution
         w.name = f"multiview_c3_{w.dim[0]}cube_{len(w.views)}views_at_{args.res}px"
+    return w
+
+
+def with_overrides(args, w):
+    """The configuration's other shader / mode / compositing variants on the
+    same volume and cameras (e.g. the tubes with Blocks.Volume and per-brick
+    sort-last compositing), named in the workload."""
+    tags = []
+    if args.shader:
+        w.params["shader"] = args.shader
+        w.params.pop("mode", None)
+        tags.append(args.shader)
+    if args.mode:
+        w.params["mode"] = args.mode
+        tags.append(args.mode)
+    if args.composite:
+        w.params["composite"] = True
+        tags.append("composite")
+    if args.sample_rate > 0:
+        w.params["sample_rate"] = args.sample_rate
+        tags.append(f"rate{args.sample_rate:g}")
+    if args.density is not None:
+        w.params["density"] = args.density
+        tags.append(f"density{args.density:g}")
+    if tags:
+        w.name = "_".join([w.name] + tags)
     return w
 
 
@@ -466,7 +507,9 @@ def main_ours(args):
     # the profiled per-sample figures hold for the Volume shader on the blob
     # volume they were captured on, not for the other workloads
     tps = ipsm = None
-    if args.workload == "multiview":
+    overridden = (args.shader or args.mode or args.composite or args.sample_rate > 0
+                  or args.density is not None)
+    if args.workload == "multiview" and not overridden:
         tps = profile_per_sample(int(tuned.get("block_queue", 1)))
         ipsm = profile_per_sample(int(tuned.get("block_queue", 1)),
                                   "warp_instructions_per_sample")
