@@ -414,7 +414,9 @@ int fill_diff(hy_ctx *ctx, const hy_diff_params *p, const float *vol, const floa
         return hy_fail(ctx, HY_ERR_INVALID, "diff: volume edge must be <= 1290 (n^3 < 2^31)");
     if (nviews <= 0 || nviews > kMaxDiffViews)
         return hy_fail(ctx, HY_ERR_INVALID, "diff: 1..64 views");
-    if (W <= 0 || H <= 0) return hy_fail(ctx, HY_ERR_INVALID, "diff: bad resolution");
+    // the launch grid is W/16 x H/8 tiles (at most 65535 tile rows) per view
+    if (W <= 0 || H <= 0 || (long long)W * H > (1ll << 31) || (H + 7) / 8 > 65535)
+        return hy_fail(ctx, HY_ERR_INVALID, "diff: bad resolution");
     if (p->ntf <= 0 || p->ntf > kMaxKnots) return hy_fail(ctx, HY_ERR_INVALID, "diff: 1..256 knots");
     if (p->ckpt_k <= 0 || p->ckpt_k > kMaxK)
         return hy_fail(ctx, HY_ERR_INVALID, "diff: checkpoint interval 1..64");

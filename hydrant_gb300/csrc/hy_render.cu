@@ -333,7 +333,8 @@ int hy_fill_args(hy_ctx *ctx, const hy_volume *vol, const hy_shader_params *p, c
     if (!vol || !p) return hy_fail(ctx, HY_ERR_INVALID, "render: null volume or params");
     if (vol->ctx != ctx) return hy_fail(ctx, HY_ERR_INVALID, "render: volume of another context");
     if (!vol->uploaded) return hy_fail(ctx, HY_ERR_STATE, "render: volume not uploaded");
-    if (W <= 0 || H <= 0 || (long long)W * H > (1ll << 31))
+    // the launch grid is W/16 x H/8 tiles (at most 65535 tile rows)
+    if (W <= 0 || H <= 0 || (long long)W * H > (1ll << 31) || (H + kTileH - 1) / kTileH > 65535)
         return hy_fail(ctx, HY_ERR_INVALID, "render: bad resolution");
     if (p->shader < HY_SHADER_VOLUME || p->shader > HY_SHADER_PAGING)
         return hy_fail(ctx, HY_ERR_INVALID, "render: unknown shader");

@@ -245,3 +245,17 @@ def test_second_upload_is_rejected(ctx):
         assert r.rgba.shape == (16, 16, 4)
     finally:
         vol.close()
+
+
+def test_resolution_limits(tubes128):
+    """Sizes the launch grid cannot cover are refused before any launch; the
+    context stays usable."""
+    c = tubes128
+    p = hy.shader_params(shader="Volume", sample_rate=0.25)
+    view = hy.camera_view(c.vol, camera())
+    # (host buffers stay small: the C side refuses these before any copy)
+    for w, h in ((0, 8), (8, 0), (1, 65535 * 8 + 1)):
+        with pytest.raises(hy.HydrantError):
+            hy.render(c.ctx, c.vol, p, view, w, h)
+    r = hy.render(c.ctx, c.vol, p, view, 8, 8)
+    assert r.rgba.shape == (8, 8, 4)
