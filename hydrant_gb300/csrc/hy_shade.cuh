@@ -147,10 +147,11 @@ __device__ __forceinline__ BrickRef load_brick(const DevVolume &V, int reg) {
 // so it lies at least 1/510 ulp from a rounding boundary while hi + lo and
 // the rounding of u * lo are off by ~2^-48: q is the correctly rounded
 // quotient for every u in 0..255 (also checked exhaustively,
-// tests/test_u8_normalisation.py).  Taps below HY_U8_ARITH_TAPS use it, the
-// others the shared-memory table (whose lookups conflict on banks when
-// neighbouring lanes read distant values); all eight arithmetic measured
-// fastest.
+// tests/test_u8_normalisation.py).  The interior sampler normalises every
+// tap this way (two taps per packed instruction); in the scalar build
+// (HY_F32X2=0) taps below HY_U8_ARITH_TAPS do, the others read the
+// shared-memory table (whose lookups conflict on banks when neighbouring
+// lanes read distant values) -- all eight arithmetic measured fastest.
 #ifndef HY_U8_ARITH_TAPS
 #define HY_U8_ARITH_TAPS 8
 #endif
