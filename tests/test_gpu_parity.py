@@ -114,6 +114,26 @@ def test_f32_volume(ctx):
         c.close()
 
 
+@pytest.mark.parametrize("dtype", ["u8", "f32"])
+def test_unpadded_volume(ctx, dtype):
+    """No apron: every sample goes through the wrapping, clamping sampler
+    (a tap past the brick face wraps to the opposite face, as the reference's
+    Wrap address mode does), in every shader."""
+    vox = (hy.synth_tubes_u8(2, (48, 40, 56), 10) if dtype == "u8"
+           else hy.synth_blobs_f32(5, (48, 40, 56), 14))
+    c = Case(ctx, vox, 16, 0)
+    try:
+        for kw in (dict(shader="Volume", sample_rate=1.0, density=1.0),
+                   dict(shader="Volume", sample_rate=0.5, density=0.3, composite=True),
+                   dict(shader="Isosurface", isovalue=0.4),
+                   dict(shader="Isosurface", isovalue=0.4, composite=True),
+                   dict(shader="Blocks", mode="Volume", density=0.5)):
+            g, r, _, _ = c.render_both(camera(a=(35, 20, 2.1)), 72, 56, **kw)
+            assert_parity(g, r, what=f"unpadded {dtype} {kw}")
+    finally:
+        c.close()
+
+
 @pytest.mark.parametrize("wh", [(1, 1), (37, 23), (17, 9), (300, 7)])
 def test_ragged_resolutions(blobs64, wh):
     g, r, _, _ = blobs64.render_both(camera(), wh[0], wh[1], shader="Volume", density=1.0)
