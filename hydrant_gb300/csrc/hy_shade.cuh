@@ -390,17 +390,23 @@ struct BrickCursor {
 struct VolumeMarch {
     BrickCursor c;
     float cdu, rx, ry, rz;
-    float sx, sy, sz;
-    int cur_ss;
+    float sx, sy, sz;  // (d * step) * step_size, redone only when step_size changes
 
-    __device__ __forceinline__ void init(const Px &p) {
+    __device__ __forceinline__ void set_step(const Px &p, float step) {
+        const float fs = float(p.step_size);
+        sx = (p.dx * step) * fs;
+        sy = (p.dy * step) * fs;
+        sz = (p.dz * step) * fs;
+    }
+
+    // p.step_size is 1 for a new ray, or what a film pass left
+    __device__ __forceinline__ void init(const Px &p, float step) {
         cdu = 1.f / gmax(gmax(fabsf(p.dx), fabsf(p.dy)), fabsf(p.dz));
         rx = 1.f / p.dx;
         ry = 1.f / p.dy;
         rz = 1.f / p.dz;
         c.reset();
-        cur_ss = 0;
-        sx = sy = sz = 0.f;
+        set_step(p, step);
     }
 
     // One iteration of `while (nsteps > 0)`; false when the ray breaks out
@@ -464,17 +470,16 @@ struct VolumeMarch {
             p.vw = p.vw + ub.w * t;
 #endif
             if (p.vw >= HY_T93) {
-                p.step_size = 16;
+                if (p.step_size != 16) {
+                    p.step_size = 16;
+                    set_step(p, A.step);
+                }
             } else if (p.vw >= HY_T85) {
-                p.step_size = 4;
+                if (p.step_size != 4) {
+                    p.step_size = 4;
+                    set_step(p, A.step);
+                }
             }
-        }
-        if (p.step_size != cur_ss) {  // (d * step) * step_size, recomputed only when it changes
-            cur_ss = p.step_size;
-            const float fs = float(cur_ss);
-            sx = (p.dx * A.step) * fs;
-            sy = (p.dy * A.step) * fs;
-            sz = (p.dz * A.step) * fs;
         }
         p.ox = p.ox + sx;  // sx..sz are products: scalar adds
         p.oy = p.oy + sy;
@@ -488,7 +493,7 @@ template <int PC, int DT, bool PADDED, bool LEAN = false>
 __device__ __forceinline__ long long volume_main(Px &p, const ShadeArgs &A, const Shared &S) {
     unsigned int samples = 0;
     VolumeMarch m;
-    m.init(p);
+    m.init(p, A.step);
     while (p.nsteps > 0)
         if (!m.step<PC, DT, PADDED, LEAN>(p, A, S, samples)) break;
     return samples;
