@@ -106,9 +106,9 @@ __global__ void __launch_bounds__(kMaxBlockThreads, HY_BATCH_MIN_BLOCKS)
     __shared__ unsigned int s_t0;
     const ShadeArgs &A = B.A;
     float4 *tf = smem;
-    float *lut = reinterpret_cast<float *>(smem + A.ntf);
+    float *lut = reinterpret_cast<float *>(smem + A.ntf + kTfPad);
     int *starts = reinterpret_cast<int *>(lut + 256);
-    for (int i = threadIdx.x; i < A.ntf; i += blockDim.x) tf[i] = A.tf[i];
+    stage_tf(A.tf, A.ntf, tf);
     for (int i = threadIdx.x; i < 256; i += blockDim.x) lut[i] = float(i) / 255.f;
     for (int i = threadIdx.x; i < B.nviews; i += blockDim.x) starts[i] = B.starts[i];
     __syncthreads();
@@ -295,7 +295,7 @@ int layout(hy_batch *b) {
     HY_CUDA(ctx, cudaMemcpyAsync(b->starts_dev, b->starts.data(), b->starts.size() * sizeof(int),
                                  cudaMemcpyHostToDevice, ctx->stream));
     HY_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    b->smem = size_t(b->base.ntf) * sizeof(float4) + 256 * sizeof(float) +
+    b->smem = size_t(b->base.ntf + kTfPad) * sizeof(float4) + 256 * sizeof(float) +
               b->in.size() * sizeof(int);
     HY_CUDA(ctx, allow_smem(b->kernel, b->smem));
     const int threads = b->cfg.block_warps * 32;
@@ -651,7 +651,7 @@ extern "C" int hy_render_views_noalloc(hy_ctx *ctx, const hy_volume *vol,
     args.out = rgba_dev;
     const void *kernel = pick_kernel(base);
     const int threads = cfg.block_warps * 32;
-    const size_t smem = size_t(base.ntf) * sizeof(float4) + 256 * sizeof(float) +
+    const size_t smem = size_t(base.ntf + kTfPad) * sizeof(float4) + 256 * sizeof(float) +
                         size_t(nviews) * sizeof(int);
     int per_sm = 0, sms = 0;
     HY_CUDA(ctx, allow_smem(kernel, smem));

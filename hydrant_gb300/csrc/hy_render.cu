@@ -23,7 +23,7 @@ namespace {
 constexpr int kTileW = 16, kTileH = 8, kThreads = 128;
 
 __device__ __forceinline__ void load_shared(const ShadeArgs &A, float4 *tf, float *lut) {
-    for (int i = threadIdx.x; i < A.ntf; i += blockDim.x) tf[i] = A.tf[i];
+    stage_tf(A.tf, A.ntf, tf);
     for (int i = threadIdx.x; i < 256; i += blockDim.x) lut[i] = float(i) / 255.f;
     __syncthreads();
 }
@@ -54,7 +54,7 @@ template <int SHADER, int PC, int DT, bool PADDED, int COMPOSITE, bool LEAN>
 __device__ __forceinline__ void render_body(const ShadeArgs &A) {
     extern __shared__ float4 smem[];
     float4 *tf = smem;
-    float *lut = reinterpret_cast<float *>(smem + A.ntf);
+    float *lut = reinterpret_cast<float *>(smem + A.ntf + kTfPad);
     load_shared(A, tf, lut);
     const Shared S{tf, A.ntf, float(A.ntf), lut};
     int x, y;
@@ -155,7 +155,7 @@ template <int SHADER, int DT>
 __global__ void __launch_bounds__(kThreads) emit_pass_kernel(const __grid_constant__ ShadeArgs A) {
     extern __shared__ float4 smem[];
     float4 *tf = smem;
-    float *lut = reinterpret_cast<float *>(smem + A.ntf);
+    float *lut = reinterpret_cast<float *>(smem + A.ntf + kTfPad);
     load_shared(A, tf, lut);
     const Shared S{tf, A.ntf, float(A.ntf), lut};
     int x, y;
@@ -177,7 +177,7 @@ template <int SHADER, int DT>
 __global__ void __launch_bounds__(kThreads) march_pass_kernel(const __grid_constant__ ShadeArgs A) {
     extern __shared__ float4 smem[];
     float4 *tf = smem;
-    float *lut = reinterpret_cast<float *>(smem + A.ntf);
+    float *lut = reinterpret_cast<float *>(smem + A.ntf + kTfPad);
     load_shared(A, tf, lut);
     const Shared S{tf, A.ntf, float(A.ntf), lut};
     int x, y;
@@ -242,7 +242,9 @@ __global__ void __launch_bounds__(kThreads) fetch_pass_kernel(const __grid_const
     }
 }
 
-size_t smem_bytes(const ShadeArgs &a) { return size_t(a.ntf) * sizeof(float4) + 256 * sizeof(float); }
+size_t smem_bytes(const ShadeArgs &a) {
+    return size_t(a.ntf + kTfPad) * sizeof(float4) + 256 * sizeof(float);
+}
 
 dim3 grid_of(const ShadeArgs &a) {
     return dim3((a.view.W + kTileW - 1) / kTileW, (a.view.H + kTileH - 1) / kTileH);

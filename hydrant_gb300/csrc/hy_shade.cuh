@@ -282,23 +282,33 @@ __device__ __forceinline__ float sample_brick(const BrickRef &b, int Prt, float 
 #endif
 }
 
+// The transfer function's knots in shared memory with the end knots
+// repeated: tfs[0] = knot 0, tfs[i + 1] = knot i, tfs[n + 1] = knot n - 1
+// (n + kTfPad entries).
+// Nothing is staged without knots (the Isosurface and Blocks shaders run
+// without a transfer function and never call sample_tf).
+constexpr int kTfPad = 2;
+__device__ __forceinline__ void stage_tf(const float4 *__restrict__ tf, int n, float4 *tfs) {
+    if (n <= 0) return;
+    for (int i = threadIdx.x; i < n + kTfPad; i += blockDim.x) tfs[i] = tf[min(max(i - 1, 0), n - 1)];
+}
+
 // TransferFn lookup: 1-D, normalised, Border, Linear (transfer_fn.hpp:16-23,
-// cpu_sampler.hpp:117-124, 137-140), knots in shared memory.
-__device__ __forceinline__ float4 sample_tf(const float4 *__restrict__ tf, int n, float fn,
+// cpu_sampler.hpp:117-124, 137-140), knots staged by stage_tf.
+__device__ __forceinline__ float4 sample_tf(const float4 *__restrict__ tfs, int n, float fn,
                                             float s) {
     float fx = fn * s;
     if (!(0.f <= fx && fx <= fn)) return make_float4(0.f, 0.f, 0.f, 0.f);
-    // fx in [0, n] so floor(fx - 0.5) is in [-1, n-1]: the lower index only
-    // needs the clamp at 0.  The upper one is ceil(u) = floor(u) + 1, or
-    // floor(u) when u is integral -- where a == 0 and the knot it picks is
-    // weighted by 0, so floor(u) + 1 (clamped at n-1) gives the same floats.
+    // fx in [0, n] so fi = floor(fx - 0.5) is in [-1, n-1] and the clamped
+    // neighbours knot[max(fi, 0)], knot[min(fi + 1, n - 1)] are tfs[fi + 1],
+    // tfs[fi + 2].  The upper one is ceil(u) = floor(u) + 1, or floor(u) when
+    // u is integral -- where a == 0 and the knot it picks is weighted by 0,
+    // so floor(u) + 1 gives the same floats.
     float u = fx - .5f;
     float flr = floorf(u);
     float a = u - flr;
-    const int fi = int(flr);
-    int i = max(fi, 0);
-    int j = min(fi + 1, n - 1);
-    float4 x = tf[i], y = tf[j];
+    const float4 *k = tfs + (int(flr) + 1);
+    float4 x = k[0], y = k[1];
     float b = 1.f - a;
 #if HY_F32X2
     const float2 bb = f2(b, b), aa = f2(a, a);

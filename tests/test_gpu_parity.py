@@ -279,3 +279,31 @@ def test_resolution_limits(tubes128):
             hy.render(c.ctx, c.vol, p, view, w, h)
     r = hy.render(c.ctx, c.vol, p, view, 8, 8)
     assert r.rgba.shape == (8, 8, 4)
+
+
+def test_no_transfer_function_needed(ctx):
+    """The Isosurface and Blocks shaders read no transfer function: a context
+    that never set one renders them exactly as one that did (nothing is
+    staged from an empty knot array); the Volume shader is refused there."""
+    vox = hy.synth_tubes_u8(1, (64, 64, 64), 8)
+    bare = hy.Context(0)
+    vol_bare = hy.Volume(bare, vox, 32, 1)
+    vol = hy.Volume(ctx, vox, 32, 1)
+    try:
+        for kw in (dict(shader="Isosurface", isovalue=0.5),
+                   dict(shader="Isosurface", isovalue=0.5, composite=True),
+                   dict(shader="Blocks", mode="Volume", density=0.5)):
+            p = hy.shader_params(**kw)
+            if kw["shader"] == "Isosurface":
+                hy.iso_lighting(vol, camera(), p)
+            a = hy.render(bare, vol_bare, p, hy.camera_view(vol_bare, camera()), 48, 40)
+            b = hy.render(ctx, vol, p, hy.camera_view(vol, camera()), 48, 40)
+            assert np.array_equal(a.rgba, b.rgba), kw
+            assert a.rgba[..., 3].any(), kw
+        with pytest.raises(hy.HydrantError):
+            hy.render(bare, vol_bare, hy.shader_params(shader="Volume"),
+                      hy.camera_view(vol_bare, camera()), 8, 8)
+    finally:
+        vol.close()
+        vol_bare.close()
+        bare.close()
