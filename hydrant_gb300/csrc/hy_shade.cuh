@@ -295,10 +295,14 @@ __device__ __forceinline__ void stage_tf(const float4 *__restrict__ tf, int n, f
 
 // TransferFn lookup: 1-D, normalised, Border, Linear (transfer_fn.hpp:16-23,
 // cpu_sampler.hpp:117-124, 137-140), knots staged by stage_tf.
+// NONNEG: s is +0, positive or NaN (a trilinear sample of u8 voxels: values
+// u/255 >= 0 and weights a, 1-a >= 0 give products and sums >= +0), so the
+// Border test 0 <= fx <= n reduces to !(fx <= n), which NaN fails as well.
+template <bool NONNEG = false>
 __device__ __forceinline__ float4 sample_tf(const float4 *__restrict__ tfs, int n, float fn,
                                             float s) {
     float fx = fn * s;
-    if (!(0.f <= fx && fx <= fn)) return make_float4(0.f, 0.f, 0.f, 0.f);
+    if (NONNEG ? !(fx <= fn) : !(0.f <= fx && fx <= fn)) return make_float4(0.f, 0.f, 0.f, 0.f);
     // fx in [0, n] so fi = floor(fx - 0.5) is in [-1, n-1] and the clamped
     // neighbours knot[max(fi, 0)], knot[min(fi + 1, n - 1)] are tfs[fi + 1],
     // tfs[fi + 2].  The upper one is ceil(u) = floor(u) + 1, or floor(u) when
@@ -436,7 +440,7 @@ struct VolumeMarch {
         } else {
             float s = sample_brick<PC, DT, PADDED>(c.br, V.P, lx, ly, lz, S.lut);
             ++samples;
-            float4 ub = sample_tf(S.tf, S.ntf, S.fntf, s);
+            float4 ub = sample_tf<DT == HY_DTYPE_U8>(S.tf, S.ntf, S.fntf, s);
             if (LEAN) {
             } else if (A.mode == HY_VOLUME_PARTITION) {
                 float r = A.rank;
@@ -479,14 +483,12 @@ struct VolumeMarch {
             p.vz = p.vz + ub.z * t;
             p.vw = p.vw + ub.w * t;
 #endif
-            if (p.vw >= HY_T93) {
-                if (p.step_size != 16) {
-                    p.step_size = 16;
-                    set_step(p, A.step);
-                }
-            } else if (p.vw >= HY_T85) {
-                if (p.step_size != 4) {
-                    p.step_size = 4;
+            // v.w > 0.93 -> 16, else v.w > 0.85 -> 4 (volume_shader.cu:71-75),
+            // nested so that the common case (v.w below both) tests once
+            if (p.vw >= HY_T85) {
+                const int ss = p.vw >= HY_T93 ? 16 : 4;
+                if (p.step_size != ss) {
+                    p.step_size = ss;
                     set_step(p, A.step);
                 }
             }
