@@ -100,8 +100,7 @@ __device__ __forceinline__ int find_view(const int *starts, int n, int t) {
 // LEAN: Volume shader in Default mode without compositing (theta / phi are
 // not needed for an RGBA image; see VolumeMarch::step).
 template <int SHADER, int PC, int DT, bool PADDED, int COMPOSITE, bool LEAN>
-__global__ void __launch_bounds__(kMaxBlockThreads, HY_BATCH_MIN_BLOCKS)
-    batch_kernel(const __grid_constant__ BatchArgs B) {
+__device__ __forceinline__ void batch_body(const BatchArgs &B) {
     extern __shared__ float4 smem[];
     __shared__ unsigned int s_t0;
     const ShadeArgs &A = B.A;
@@ -161,15 +160,40 @@ __global__ void __launch_bounds__(kMaxBlockThreads, HY_BATCH_MIN_BLOCKS)
     }
 }
 
+template <int SHADER, int PC, int DT, bool PADDED, int COMPOSITE>
+__global__ void __launch_bounds__(kMaxBlockThreads, HY_BATCH_MIN_BLOCKS)
+    batch_kernel(const __grid_constant__ BatchArgs B) {
+    batch_body<SHADER, PC, DT, PADDED, COMPOSITE, false>(B);
+}
+
+// The lean march over u8 bricks with an apron holds its state in 56
+// registers (40 bytes spill), so nine 4-warp blocks fit on an SM: 36
+// resident warps hide more of the L1 latency of the tap loads than 32 do
+// (64-view step: 178.2 vs 182.0 ms).  f32 and apron-less volumes spill far
+// more at 56 and keep 64.  (__maxnreg__ excludes __launch_bounds__; the
+// batch launches at most kMaxBlockThreads threads per block.)
+#ifndef HY_BATCH_LEAN_REGS
+#define HY_BATCH_LEAN_REGS 56
+#endif
+template <int DT, bool PADDED>
+constexpr int lean_regs() {
+    return (DT == HY_DTYPE_U8 && PADDED) ? HY_BATCH_LEAN_REGS : 64;
+}
+template <int SHADER, int PC, int DT, bool PADDED>
+__global__ void __maxnreg__((lean_regs<DT, PADDED>()))
+    batch_lean_kernel(const __grid_constant__ BatchArgs B) {
+    batch_body<SHADER, PC, DT, PADDED, 0, true>(B);
+}
+
 template <int SHADER, int PC, int DT, bool PADDED>
 const void *pick_c(const ShadeArgs &a) {
     if (a.composite)
-        return reinterpret_cast<const void *>(&batch_kernel<SHADER, PC, DT, PADDED, 1, false>);
+        return reinterpret_cast<const void *>(&batch_kernel<SHADER, PC, DT, PADDED, 1>);
     if constexpr (SHADER == HY_SHADER_VOLUME) {
         if (a.mode == HY_VOLUME_DEFAULT)
-            return reinterpret_cast<const void *>(&batch_kernel<SHADER, PC, DT, PADDED, 0, true>);
+            return reinterpret_cast<const void *>(&batch_lean_kernel<SHADER, PC, DT, PADDED>);
     }
-    return reinterpret_cast<const void *>(&batch_kernel<SHADER, PC, DT, PADDED, 0, false>);
+    return reinterpret_cast<const void *>(&batch_kernel<SHADER, PC, DT, PADDED, 0>);
 }
 
 template <int SHADER>
