@@ -636,6 +636,11 @@ __device__ __forceinline__ long long iso_main(Px &p, const ShadeArgs &A, const V
     const float rx = 1.f / p.dx, ry = 1.f / p.dy, rz = 1.f / p.dz;
     const float prev_value = 0.0f;
     const float iso = A.isovalue;
+    // sign(value - iso) != sign(prev_value - iso), prev_value = 0 (never
+    // updated, isosurface_shader.cu:58-70).  The rounded difference of two
+    // floats has the sign of the exact one (and is 0 only when they are
+    // equal), so per sign of -iso the test is one comparison; NaN values
+    // (sign 0) and a NaN isovalue behave as with fsign.
     const float prev_sign = fsign(prev_value - iso);
     const float sx = p.dx * A.step, sy = p.dy * A.step, sz = p.dz * A.step;
     BrickCursor c;
@@ -651,7 +656,10 @@ __device__ __forceinline__ long long iso_main(Px &p, const ShadeArgs &A, const V
             if (c.pg == -1) break;  // page fault: resume in the next march pass
             float value = sample_brick<PC, DT, PADDED>(br, V.P, l0x, l0y, l0z, S.lut);
             ++samples;
-            if (fsign(value - iso) != prev_sign) {
+            const bool crossed = prev_sign < 0.f   ? !(value < iso)
+                                 : prev_sign > 0.f ? !(value > iso)
+                                                   : (value < iso || value > iso);
+            if (crossed) {
                 const float dt = A.step;
                 p.vx = A.surface[0];
                 p.vy = A.surface[1];

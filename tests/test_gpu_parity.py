@@ -108,8 +108,10 @@ def test_f32_volume(ctx):
     try:
         g, r, _, _ = c.render_both(camera(), 80, 64, shader="Volume", sample_rate=1.0, density=1.0)
         assert_parity(g, r, what="f32 volume")
-        g, r, _, _ = c.render_both(camera(), 64, 64, shader="Isosurface", isovalue=0.3)
-        assert_parity(g, r, what="f32 iso")
+        # isovalues of every sign: the crossing test compares against sign(0 - iso)
+        for iso in (0.3, 0.0, -0.2):
+            g, r, _, _ = c.render_both(camera(), 64, 64, shader="Isosurface", isovalue=iso)
+            assert_parity(g, r, what=f"f32 iso {iso}")
     finally:
         c.close()
 
