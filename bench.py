@@ -559,7 +559,7 @@ def main_ours(args):
             "e2e": {"value": e2e, "unit": "Gsamples/s",
                     "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": batch.nbytes,
-                    "path": "hy_batch_render (pinned host output buffer)"},
+                    "path": "hy_batch_render into a pinned, mapped host buffer: the kernel writes the pixels across the host link while it marches"},
             "roofline": {
                 "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": achieved / hbm, "peak_kind": peak_kind,

@@ -484,10 +484,31 @@ extern "C" int hy_batch_render_device(hy_batch *b, uint8_t *rgba_dev) {
     return launch(b, rgba_dev);
 }
 
+// A host buffer that is pinned and mapped into the device's address space
+// (cudaHostAlloc, or cudaHostRegister with mapping -- what a serving process
+// allocates for its frames) is written by the kernel itself: the pixels
+// cross the host link while the march runs, with no staging copy after it.
+// Any other host buffer gets the image through a device staging buffer and
+// one copy.
+static uint8_t *mapped_device_ptr(uint8_t *host) {
+    cudaPointerAttributes pa{};
+    if (cudaPointerGetAttributes(&pa, host) != cudaSuccess) {
+        cudaGetLastError();  // not a pointer the runtime knows
+        return nullptr;
+    }
+    return pa.type == cudaMemoryTypeHost ? static_cast<uint8_t *>(pa.devicePointer) : nullptr;
+}
+
 extern "C" int hy_batch_render(hy_batch *b, uint8_t *rgba_host) {
     if (!b) return HY_ERR_INVALID;
     if (!rgba_host) return hy_fail(b->ctx, HY_ERR_INVALID, "batch: null output");
     hy_ctx *ctx = b->ctx;
+    HY_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (uint8_t *direct = mapped_device_ptr(rgba_host)) {
+        int rc = launch(b, direct);
+        if (rc) return rc;
+        return hy_finish_stats(ctx);
+    }
     void *stage = nullptr;
     int rc = hy_stage(ctx, size_t(b->out_bytes), &stage);
     if (rc) return rc;

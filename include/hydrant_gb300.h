@@ -414,7 +414,10 @@ int hy_batch_get_config(const hy_batch *batch, hy_batch_config *out);
 int hy_batch_set_counting(hy_batch *batch, int32_t count_samples);
 /* Device output, asynchronous on the context's stream. */
 int hy_batch_render_device(hy_batch *batch, uint8_t *rgba_dev);
-/* Host output; returns when the images are on the host. */
+/* Host output; returns when the images are on the host.  A pinned host
+ * buffer mapped into the device's address space (cudaHostAlloc, or
+ * cudaHostRegister with mapping) is written by the kernel itself, with no
+ * staging copy; any other buffer receives one copy from device memory. */
 int hy_batch_render(hy_batch *batch, uint8_t *rgba_host);
 /* Times every launch shape (queue per warp or per block, tile 8x4/4x8/16x2,
  * grab 1/2/4, 2/4/8 warps per block) on this batch and keeps the fastest;

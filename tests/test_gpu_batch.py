@@ -168,3 +168,28 @@ def test_batch_follows_the_transfer_function(ctx, tubes):
     finally:
         ctx.set_transfer_fn(wl.TF9)
         b.close()
+
+
+def test_batch_renders_into_pinned_host_memory(ctx, tubes):
+    """A pinned, mapped host buffer is written by the kernel directly (no
+    staging copy): the bytes equal those rendered into pageable host memory
+    and into device memory, and a second render into the same buffer (the
+    graph replayed) again equals them."""
+    torch = pytest.importorskip("torch")
+    views, cams = _views(tubes, SIZES)
+    p = hy.shader_params(shader="Volume", density=0.5, sample_rate=0.5)
+    b = hy.Batch(ctx, tubes, p, views)
+    try:
+        pageable = np.concatenate([g.reshape(-1) for g in b.render()])
+        dev = torch.empty(b.nbytes, dtype=torch.uint8, device="cuda:0")
+        b.render_device(dev.data_ptr())
+        torch.cuda.synchronize()
+        pinned = torch.zeros(b.nbytes, dtype=torch.uint8, pin_memory=True)
+        for _ in range(2):
+            pinned.zero_()
+            ctx.check(hy.lib().hy_batch_render(b.handle, hy._abi.C.c_void_p(pinned.data_ptr())))
+            assert np.array_equal(pinned.numpy(), pageable)
+        assert np.array_equal(dev.cpu().numpy(), pageable)
+        assert pageable.any()
+    finally:
+        b.close()
