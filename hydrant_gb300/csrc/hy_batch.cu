@@ -480,6 +480,7 @@ extern "C" int hy_batch_set_counting(hy_batch *b, int32_t count_samples) {
 
 extern "C" int hy_batch_render_device(hy_batch *b, uint8_t *rgba_dev) {
     if (!b) return HY_ERR_INVALID;
+    if (!hy_aligned(rgba_dev, 4)) return hy_fail(b->ctx, HY_ERR_INVALID, "batch: misaligned output (4-byte)");
     if (!rgba_dev) return hy_fail(b->ctx, HY_ERR_INVALID, "batch: null output");
     return launch(b, rgba_dev);
 }
@@ -488,23 +489,15 @@ extern "C" int hy_batch_render_device(hy_batch *b, uint8_t *rgba_dev) {
 // (cudaHostAlloc, or cudaHostRegister with mapping -- what a serving process
 // allocates for its frames) is written by the kernel itself: the pixels
 // cross the host link while the march runs, with no staging copy after it.
-// Any other host buffer gets the image through a device staging buffer and
-// one copy.
-static uint8_t *mapped_device_ptr(uint8_t *host) {
-    cudaPointerAttributes pa{};
-    if (cudaPointerGetAttributes(&pa, host) != cudaSuccess) {
-        cudaGetLastError();  // not a pointer the runtime knows
-        return nullptr;
-    }
-    return pa.type == cudaMemoryTypeHost ? static_cast<uint8_t *>(pa.devicePointer) : nullptr;
-}
+// Any other host buffer (or one not 4-byte aligned) gets the image through a
+// device staging buffer and one copy.
 
 extern "C" int hy_batch_render(hy_batch *b, uint8_t *rgba_host) {
     if (!b) return HY_ERR_INVALID;
     if (!rgba_host) return hy_fail(b->ctx, HY_ERR_INVALID, "batch: null output");
     hy_ctx *ctx = b->ctx;
     HY_CUDA(ctx, cudaSetDevice(ctx->device));
-    if (uint8_t *direct = mapped_device_ptr(rgba_host)) {
+    if (uint8_t *direct = hy_mapped_device_ptr(rgba_host, 4)) {
         int rc = launch(b, direct);
         if (rc) return rc;
         return hy_finish_stats(ctx);
@@ -524,6 +517,7 @@ extern "C" int hy_batch_autotune(hy_batch *b, uint8_t *rgba_dev, int32_t reps,
                                  hy_batch_config *best_out) {
     if (!b || !rgba_dev) return HY_ERR_INVALID;
     hy_ctx *ctx = b->ctx;
+    if (!hy_aligned(rgba_dev, 4)) return hy_fail(ctx, HY_ERR_INVALID, "batch: misaligned output (4-byte)");
     if (reps <= 0) reps = 3;
     const int tws[] = {8, 4, 16};
     const int grabs[] = {1, 2, 4};
@@ -627,6 +621,8 @@ extern "C" int hy_render_views_noalloc(hy_ctx *ctx, const hy_volume *vol,
                                        const hy_batch_view *views, int32_t nviews,
                                        uint8_t *rgba_dev) {
     if (!ctx) return HY_ERR_INVALID;
+    if (!hy_aligned(rgba_dev, 4))
+        return hy_fail(ctx, HY_ERR_INVALID, "noalloc: misaligned output (4-byte)");
     if (!views || !rgba_dev) return hy_fail(ctx, HY_ERR_INVALID, "noalloc: null views or output");
     if (nviews <= 0 || nviews > kNoAllocMaxViews)
         return hy_fail(ctx, HY_ERR_INVALID,

@@ -468,6 +468,11 @@ extern "C" int hy_diff_forward(hy_ctx *ctx, const hy_diff_params *p, const float
                                int32_t W, int32_t H, float *image_dev, float *ckpt_dev,
                                int32_t *nsteps_dev) {
     if (!ctx) return HY_ERR_INVALID;
+    // float4 records: knots, image, checkpoints; scalars: volume, step counts
+    if (!hy_aligned(tf_dev, 16) || !hy_aligned(image_dev, 16) || !hy_aligned(ckpt_dev, 16) ||
+        !hy_aligned(vol_dev, 4) || !hy_aligned(nsteps_dev, 4))
+        return hy_fail(ctx, HY_ERR_INVALID,
+                       "diff: misaligned buffer (knots, image, checkpoints 16-byte; others 4)");
     if (!image_dev) return hy_fail(ctx, HY_ERR_INVALID, "diff: null image");
     DiffArgs a;
     int rc = fill_diff(ctx, p, vol_dev, tf_dev, views, nviews, W, H, a);
@@ -494,6 +499,11 @@ extern "C" int hy_diff_backward(hy_ctx *ctx, const hy_diff_params *p, const floa
                                 const float *ckpt_dev, const int32_t *nsteps_dev,
                                 float *dvol_dev, float *dtf_dev) {
     if (!ctx) return HY_ERR_INVALID;
+    if (!hy_aligned(tf_dev, 16) || !hy_aligned(dimage_dev, 16) || !hy_aligned(ckpt_dev, 16) ||
+        !hy_aligned(vol_dev, 4) || !hy_aligned(nsteps_dev, 4) || !hy_aligned(dvol_dev, 4) ||
+        !hy_aligned(dtf_dev, 4))
+        return hy_fail(ctx, HY_ERR_INVALID,
+                       "diff: misaligned buffer (knots, image, checkpoints 16-byte; others 4)");
     if (!dimage_dev || !ckpt_dev || !nsteps_dev || !dvol_dev || !dtf_dev)
         return hy_fail(ctx, HY_ERR_INVALID, "diff: null argument");
     DiffArgs a;

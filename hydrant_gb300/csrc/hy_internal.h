@@ -155,6 +155,17 @@ void hy_chebyshev_transform(const std::vector<unsigned char> &nonempty, const in
 // error helpers (hy_api.cc)
 int hy_fail(hy_ctx *ctx, int code, const std::string &msg);
 int hy_cuda_fail(hy_ctx *ctx, cudaError_t e, const char *what);
+// The kernels store RGBA8 pixels as uchar4 and float images, films and
+// transfer functions as float4: device buffers a caller passes must be 4- or
+// 16-byte aligned, and the entry points check that before anything else.
+inline bool hy_aligned(const void *p, uintptr_t a) {
+    return (reinterpret_cast<uintptr_t>(p) & (a - 1)) == 0;
+}
+// The device address of a pinned host buffer mapped into the device's
+// address space (cudaHostAlloc, cudaHostRegister with mapping) when it is
+// `align`-byte aligned, else null.
+uint8_t *hy_mapped_device_ptr(void *host, uintptr_t align);
+
 #define HY_CUDA(ctx, call)                                   \
     do {                                                     \
         cudaError_t e_ = (call);                             \

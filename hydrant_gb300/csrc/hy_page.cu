@@ -1153,6 +1153,7 @@ extern "C" int hy_pager_render(hy_pager *pg, const hy_shader_params *p, const hy
                                int32_t W, int32_t H, uint8_t *rgba_dev) {
     if (!pg || !p || !cam || !rgba_dev) return HY_ERR_INVALID;
     hy_ctx *ctx = pg->ctx;
+    if (!hy_aligned(rgba_dev, 4)) return hy_fail(ctx, HY_ERR_INVALID, "pager: misaligned output (4-byte)");
     if (p->composite) return hy_fail(ctx, HY_ERR_UNSUPPORTED, "pager: composite not supported");
     HY_CUDA(ctx, cudaSetDevice(ctx->device));
     hy_view view;

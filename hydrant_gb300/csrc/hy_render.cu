@@ -453,6 +453,9 @@ extern "C" int hy_render_device(hy_ctx *ctx, const hy_volume *vol, const hy_shad
                                 const hy_view *view, int32_t W, int32_t H, uint8_t *rgba_dev,
                                 float *v_dev, float *aux_dev) {
     if (!ctx) return HY_ERR_INVALID;
+    if (!hy_aligned(rgba_dev, 4) || !hy_aligned(v_dev, 16) || !hy_aligned(aux_dev, 16))
+        return hy_fail(ctx, HY_ERR_INVALID,
+                       "render: misaligned output (rgba 4-byte, float images 16-byte)");
     if (!view || !rgba_dev) return hy_fail(ctx, HY_ERR_INVALID, "render: null view or output");
     ShadeArgs a;
     int rc = hy_fill_args(ctx, vol, p, view, W, H, &a);
@@ -461,6 +464,17 @@ extern "C" int hy_render_device(hy_ctx *ctx, const hy_volume *vol, const hy_shad
     a.vout = reinterpret_cast<float4 *>(v_dev);
     a.aux = reinterpret_cast<float4 *>(aux_dev);
     return hy_launch_render(ctx, a);
+}
+
+uint8_t *hy_mapped_device_ptr(void *host, uintptr_t align) {
+    if (!host || !hy_aligned(host, align)) return nullptr;
+    cudaPointerAttributes pa{};
+    if (cudaPointerGetAttributes(&pa, host) != cudaSuccess) {
+        cudaGetLastError();  // not a pointer the runtime knows
+        return nullptr;
+    }
+    if (pa.type != cudaMemoryTypeHost || !hy_aligned(pa.devicePointer, align)) return nullptr;
+    return static_cast<uint8_t *>(pa.devicePointer);
 }
 
 extern "C" int hy_render(hy_ctx *ctx, const hy_volume *vol, const hy_shader_params *p,
@@ -472,25 +486,40 @@ extern "C" int hy_render(hy_ctx *ctx, const hy_volume *vol, const hy_shader_para
     int rc = hy_fill_args(ctx, vol, p, view, W, H, &a);
     if (rc) return rc;
     HY_CUDA(ctx, cudaSetDevice(ctx->device));
+    // outputs in pinned, mapped host memory are written by the kernel itself
+    // (as in hy_batch_render); the others are staged in device memory and
+    // copied once
+    uint8_t *rgba_d = hy_mapped_device_ptr(rgba_out, 4);
+    uint8_t *v_d = v_out ? hy_mapped_device_ptr(v_out, 16) : nullptr;
+    uint8_t *aux_d = aux_out ? hy_mapped_device_ptr(aux_out, 16) : nullptr;
     const size_t npx = size_t(W) * H;
     const size_t rgba_b = (npx * 4 + 255) / 256 * 256, f4_b = npx * 16;
-    const size_t total = rgba_b + (v_out ? f4_b : 0) + (aux_out ? f4_b : 0);
-    void *stage = nullptr;
-    rc = hy_stage(ctx, total, &stage);
-    if (rc) return rc;
-    char *base = static_cast<char *>(stage);
-    a.rgba = reinterpret_cast<uchar4 *>(base);
-    size_t off = rgba_b;
-    if (v_out) {
-        a.vout = reinterpret_cast<float4 *>(base + off);
-        off += f4_b;
+    const size_t total =
+        (rgba_d ? 0 : rgba_b) + (v_out && !v_d ? f4_b : 0) + (aux_out && !aux_d ? f4_b : 0);
+    char *base = nullptr;
+    if (total) {
+        void *stage = nullptr;
+        rc = hy_stage(ctx, total, &stage);
+        if (rc) return rc;
+        base = static_cast<char *>(stage);
     }
-    if (aux_out) a.aux = reinterpret_cast<float4 *>(base + off);
+    size_t off = 0;
+    auto place = [&](uint8_t *direct, size_t bytes) -> char * {
+        if (direct) return reinterpret_cast<char *>(direct);
+        char *q = base + off;
+        off += bytes;
+        return q;
+    };
+    a.rgba = reinterpret_cast<uchar4 *>(place(rgba_d, rgba_b));
+    if (v_out) a.vout = reinterpret_cast<float4 *>(place(v_d, f4_b));
+    if (aux_out) a.aux = reinterpret_cast<float4 *>(place(aux_d, f4_b));
     rc = hy_launch_render(ctx, a);
     if (rc) return rc;
-    HY_CUDA(ctx, cudaMemcpyAsync(rgba_out, a.rgba, npx * 4, cudaMemcpyDeviceToHost, ctx->stream));
-    if (v_out) HY_CUDA(ctx, cudaMemcpyAsync(v_out, a.vout, f4_b, cudaMemcpyDeviceToHost, ctx->stream));
-    if (aux_out)
+    if (!rgba_d)
+        HY_CUDA(ctx, cudaMemcpyAsync(rgba_out, a.rgba, npx * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    if (v_out && !v_d)
+        HY_CUDA(ctx, cudaMemcpyAsync(v_out, a.vout, f4_b, cudaMemcpyDeviceToHost, ctx->stream));
+    if (aux_out && !aux_d)
         HY_CUDA(ctx, cudaMemcpyAsync(aux_out, a.aux, f4_b, cudaMemcpyDeviceToHost, ctx->stream));
     return hy_finish_stats(ctx);
 }
@@ -499,6 +528,11 @@ extern "C" int hy_shade_pass(hy_ctx *ctx, const hy_volume *vol, const hy_shader_
                              int32_t pass, const hy_view *view, void *film_dev, int32_t W,
                              int32_t H, void *dst_dev, const uint8_t clear_rgb[3]) {
     if (!ctx) return HY_ERR_INVALID;
+    // films hold float4 records; the Volume fetch pixel is two float4, the
+    // Isosurface one stores a float at byte 4 (16 covers both)
+    if (!hy_aligned(film_dev, 16) || (pass == HY_PASS_FETCH && !hy_aligned(dst_dev, 16)))
+        return hy_fail(ctx, HY_ERR_INVALID,
+                       "pass: misaligned film or fetch destination (16-byte)");
     if (pass < HY_PASS_RAY_EMIT || pass > HY_PASS_FETCH)
         return hy_fail(ctx, HY_ERR_INVALID, "pass: unknown pass");
     if (!film_dev) return hy_fail(ctx, HY_ERR_INVALID, "pass: null film");

@@ -309,3 +309,55 @@ def test_no_transfer_function_needed(ctx):
         vol.close()
         vol_bare.close()
         bare.close()
+
+
+def test_misaligned_device_buffers_are_refused(ctx, tubes128):
+    """uchar4 / float4 outputs need 4- / 16-byte aligned device buffers; an
+    entry point refuses a misaligned one before anything else.  Each call
+    below also lacks its volume or parameters, so even without the check it
+    would stop before launching anything."""
+    torch = pytest.importorskip("torch")
+    buf = torch.empty(1 << 16, dtype=torch.uint8, device="cuda:0")
+    base = buf.data_ptr()
+    lib, Cv = hy.lib(), hy._abi.C.c_void_p
+    p = hy.shader_params(shader="Volume")
+    view = hy.camera_view(tubes128.vol, camera())
+    cases = [
+        lambda: lib.hy_render_device(ctx.handle, None, hy._abi.C.byref(p), hy._abi.C.byref(view),
+                                     8, 8, Cv(base + 2), None, None),
+        lambda: lib.hy_render_device(ctx.handle, None, hy._abi.C.byref(p), hy._abi.C.byref(view),
+                                     8, 8, Cv(base), Cv(base + 4096 + 8), None),
+        lambda: lib.hy_shade_pass(ctx.handle, None, hy._abi.C.byref(p), hy._abi.PASS_RAY_EMIT,
+                                  hy._abi.C.byref(view), Cv(base + 4), 8, 8, None, None),
+        lambda: lib.hy_diff_forward(ctx.handle, None, Cv(base), Cv(base), hy._abi.C.byref(view), 1,
+                                    8, 8, Cv(base + 4), Cv(base), Cv(base)),
+    ]
+    for call in cases:
+        with pytest.raises(hy.HydrantError, match="misaligned"):
+            ctx.check(call())
+    # the context is intact
+    r = hy.render(ctx, tubes128.vol, p, view, 8, 8)
+    assert r.rgba.shape == (8, 8, 4)
+
+
+def test_render_into_pinned_host_memory(tubes128):
+    """hy_render writes pinned, mapped host buffers directly: RGBA, float and
+    aux images equal those rendered into pageable host memory."""
+    torch = pytest.importorskip("torch")
+    c = tubes128
+    p = hy.shader_params(shader="Volume", sample_rate=0.5, density=0.5)
+    view = hy.camera_view(c.vol, camera())
+    W, H = 40, 24
+    ref = hy.render(c.ctx, c.vol, p, view, W, H, want_v=True, want_aux=True)
+    rgba = torch.zeros(H * W * 4, dtype=torch.uint8, pin_memory=True)
+    v = torch.zeros(H * W * 4, dtype=torch.float32, pin_memory=True)
+    aux = torch.zeros(H * W * 4, dtype=torch.float32, pin_memory=True)
+    Cv = hy._abi.C.c_void_p
+    for pointers in ((rgba, v, aux), (rgba, None, None)):
+        c.ctx.check(hy.lib().hy_render(c.ctx.handle, c.vol.handle, hy._abi.C.byref(p),
+                                       hy._abi.C.byref(view), W, H,
+                                       *[Cv(t.data_ptr()) if t is not None else None
+                                         for t in pointers]))
+        assert np.array_equal(rgba.numpy().reshape(H, W, 4), ref.rgba)
+    assert np.array_equal(v.numpy().reshape(H, W, 4), ref.v)
+    assert np.array_equal(aux.numpy().reshape(H, W, 4), ref.aux)
