@@ -442,6 +442,29 @@ def main_ours(args):
     ctx.synchronize()
     t_plain = sum(a.elapsed_time(b) for a, b in evs) / 1e3
 
+    # ---- the reference's pass structure per view: the emit pass marches
+    # into a film in HBM (64 B/px for the Volume shader), the pixel pass
+    # writes the RGB8 image (raycaster.hpp:32-123) -- pass-level ABI --------
+    t_passes = None
+    if not args.composite:
+        max_px = max(W * H for _, W, H in views)
+        film = torch.empty(max_px * 64, dtype=torch.uint8, device=dev)
+        rgb = torch.empty(max_px * 3, dtype=torch.uint8, device=dev)
+
+        def passes_step():
+            for (view, W, H), p in zip(views, params):
+                hy.shade_pass(ctx, vol, p, hy._abi.PASS_RAY_EMIT, view, film.data_ptr(), W, H)
+                hy.shade_pass(ctx, vol, p, hy._abi.PASS_PIXEL, None, film.data_ptr(), W, H,
+                              rgb.data_ptr())
+
+        for _ in range(args.warmup):
+            passes_step()
+        ctx.synchronize()
+        evs = _timed_steps(torch, stream, args.steps, passes_step, flush)
+        ctx.synchronize()
+        t_passes = sum(a.elapsed_time(b) for a, b in evs) / 1e3
+        del film, rgb
+
     # ---- batched path: one persistent launch per step, graph replay -------
     batch = hy.Batch(ctx, vol, params[0], views, lighting)
     out = torch.empty(batch.nbytes, dtype=torch.uint8, device=dev)
@@ -480,6 +503,8 @@ def main_ours(args):
     t = sum(step_ms) / 1e3
     if ws > 1:
         t, t_plain = max_over_ranks([t, t_plain], dev)
+        if t_passes is not None:
+            (t_passes,) = max_over_ranks([t_passes], dev)
         torch.distributed.barrier()
 
     # ---- e2e: the host-buffer entry point (device -> host images per step) --
@@ -555,6 +580,13 @@ def main_ours(args):
                       "ms_per_step": t_plain / args.steps * 1e3,
                       "path": "one fused hy_render_device launch per view"},
             "batched_over_plain": t_plain / t,
+            "passes": None if t_passes is None else {
+                "value": aggregate_gsamples(samples, ws, args.steps, t_passes),
+                "unit": "Gsamples/s", "views_per_s": len(views) * ws * args.steps / t_passes,
+                "ms_per_step": t_passes / args.steps * 1e3,
+                "path": "per view: emit pass (march into a 64 B/px film) + pixel pass, "
+                        "the reference's pass structure through hy_shade_pass"},
+            "batched_over_passes": None if t_passes is None else t_passes / t,
             "batch_matches_plain": same and samples_b == samples,
             "e2e": {"value": e2e, "unit": "Gsamples/s",
                     "h2d_bytes_per_step": 0,
