@@ -3,8 +3,9 @@
 // Mirrors the reference's renderer-level plugin interface so that a host
 // application written against it switches by changing includes and names:
 //   * IRenderer {init(dataset, RendererConfig), update(json params),
-//     offline_render(Camera) -> image, realtime_render}
-//     (include/hydrant/core/renderer.hpp:30-49);
+//     offline_render(Camera) -> image, realtime_render(IRenderLoop &,
+//     RealtimeRenderOptions)} with IRenderLoop's callbacks
+//     (include/hydrant/core/renderer.hpp:17-49, render_loop.hpp:12-34);
 //   * RendererRegistry + HYGB_REGISTER_RENDERER(T, "name") and
 //     RendererFactory(dataset_path).create(cfg) / list_candidates()
 //     (renderer.hpp:51-89);
@@ -227,6 +228,34 @@ struct Image {
 
 // ---- renderer interface ----------------------------------------------------------
 
+// The realtime session's callbacks (include/hydrant/core/render_loop.hpp:12-34):
+// realtime_render(loop, opts) calls post_loop once, then per frame post_frame,
+// one frame at `camera` (which the loop may change between frames), on_frame
+// and after_frame until should_stop, then after_loop.
+struct IRenderLoop {
+    explicit IRenderLoop(CameraConfig const &cam) : camera(cam) {}
+    virtual ~IRenderLoop() = default;
+    IRenderLoop(IRenderLoop const &) = delete;
+    IRenderLoop &operator=(IRenderLoop const &) = delete;
+
+    virtual void post_loop() {}
+    virtual bool should_stop() = 0;
+    virtual void post_frame() {}
+    virtual void on_frame(Image &frame) = 0;
+    virtual void after_frame() {}
+    virtual void after_loop() {}
+
+    CameraConfig camera;
+};
+
+// renderer.hpp:17-27: Lossless frames page every visible brick through the
+// lossless pager (offline_render), Dynamic frames come from the realtime
+// pager (realtime_render(camera)).  There is one rank, so no communicator.
+enum class RealtimeRenderQuality { Lossless, Dynamic };
+struct RealtimeRenderOptions {
+    RealtimeRenderQuality quality = RealtimeRenderQuality::Dynamic;
+};
+
 class IRenderer {
 public:
     virtual ~IRenderer() = default;
@@ -239,9 +268,23 @@ public:
     }
     virtual void update(json::Value const &params) { (void)params; }
     virtual Image offline_render(CameraConfig const &camera) = 0;
-    // one frame of the realtime path (the render loop and its MPI / network
-    // plumbing are the caller's)
+    // one frame of the realtime path
     virtual Image realtime_render(CameraConfig const &camera) = 0;
+
+    // the realtime session (basic_renderer.hpp:106-133): frames until the
+    // loop says stop
+    void realtime_render(IRenderLoop &loop, RealtimeRenderOptions const &opts = {}) {
+        loop.post_loop();
+        while (!loop.should_stop()) {
+            loop.post_frame();
+            Image frame = opts.quality == RealtimeRenderQuality::Lossless
+                              ? offline_render(loop.camera)
+                              : realtime_render(loop.camera);
+            loop.on_frame(frame);
+            loop.after_frame();
+        }
+        loop.after_loop();
+    }
 
 protected:
     std::shared_ptr<Dataset> dataset;
@@ -388,6 +431,7 @@ public:
     Image offline_render(CameraConfig const &camera) override {
         return frame(offline(mem_limit_mb), params(), camera);
     }
+    using IRenderer::realtime_render;  // keep the loop overload visible
     Image realtime_render(CameraConfig const &camera) override {
         return frame(realtime(mem_limit_mb), params(), camera);
     }
@@ -420,6 +464,7 @@ public:
         density = float(p.number_or("density", density));
     }
     Image offline_render(CameraConfig const &camera) override { return render(camera); }
+    using IRenderer::realtime_render;  // keep the loop overload visible
     Image realtime_render(CameraConfig const &camera) override { return render(camera); }
 
 private:
@@ -460,6 +505,7 @@ public:
     Image offline_render(CameraConfig const &camera) override {
         return frame(offline(mem_limit_mb), params(), camera);
     }
+    using IRenderer::realtime_render;  // keep the loop overload visible
     Image realtime_render(CameraConfig const &camera) override {
         return frame(realtime(mem_limit_mb), params(), camera);
     }
@@ -497,6 +543,7 @@ public:
         img.rgba.assign(size_t(img.width) * img.height * 4, 0);
         return img;
     }
+    using IRenderer::realtime_render;  // keep the loop overload visible
     Image realtime_render(CameraConfig const &camera) override {
         return frame(realtime(mem_limit_mb), base_params(HY_SHADER_PAGING), camera);
     }

@@ -73,7 +73,14 @@ def test_renderer_factory_renders_like_the_c_abi(ctx, tmp_path, renderer, params
                        capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr
     got = {k: np.fromfile(tmp_path / f"out.{k}.rgba", np.uint8).reshape(H, W, 4)
-           for k in ("offline", "realtime", "updated")}
+           for k in ("offline", "realtime", "updated", "loop_dynamic", "loop_lossless")}
+    # the realtime session through IRenderLoop: every callback in order, and
+    # the last frame (back at the configured camera) as the single frames
+    for q in ("dynamic", "lossless"):
+        assert (f"loop {q} post_loop=1 post_frame=3 frames=3 after_frame=3 after_loop=1"
+                in r.stdout), r.stdout
+    assert np.array_equal(got["loop_dynamic"], got["realtime"])
+    assert np.array_equal(got["loop_lossless"], got["offline"])
 
     # the same frames through the Python binding
     cam = hy.camera_orbit((30, 40, 2.2))
