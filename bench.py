@@ -190,10 +190,11 @@ def profile_per_sample(block_queue: int, what: str = "dram_bytes_per_sample"):
 
 
 def issue_roofline(inst_per_sample, samples, launch_s, clocks, device):
-    """The march is instruction-issue bound: warp instructions per second
-    (the profiled instructions per sample x samples / launch time) against
-    the peak of one instruction per cycle on each of the SMs' 4 schedulers at
-    the median SM clock sampled during the timed region."""
+    """The bound the march works against besides L1 latency: warp
+    instructions per second (the profiled instructions per sample x samples
+    / launch time) against the peak of one instruction per cycle on each of
+    the SMs' 4 schedulers at the median SM clock sampled during the timed
+    region."""
     if not inst_per_sample or not clocks or not clocks.get("sm_mhz"):
         return None
     import torch
@@ -596,7 +597,7 @@ def main_ours(args):
                 "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": achieved / hbm, "peak_kind": peak_kind,
                 "traffic": (tps * samples) if tps else None,
-                "note": "8 B/sample algorithmic footprint; the kernel is issue bound",
+                "note": "8 B/sample algorithmic footprint; the march is bound by L1 latency and instruction issue, not HBM",
             },
             "issue_roofline": issue_roofline(ipsm, samples, mean_launch_s, ck, local),
             "cpu_baseline": cpu,
