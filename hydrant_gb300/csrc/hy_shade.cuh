@@ -397,10 +397,9 @@ struct BrickCursor {
     }
 };
 
-// VolumeShaderKernel::main (volume_shader.cu:32-81), split into the per-ray
-// state and one loop iteration so that a caller can interleave rays (the
-// batched kernel refills finished lanes).  volume_main is the plain loop.
-// PADDED: the volume has an apron of >= 1 voxel, so the interior sampler applies.
+// VolumeShaderKernel::main (volume_shader.cu:32-81) as the per-ray state and
+// one loop iteration; volume_main is the loop.  PADDED: the volume has an
+// apron of >= 1 voxel, so the interior sampler applies.
 struct VolumeMarch {
     BrickCursor c;
     float cdu, rx, ry, rz;
