@@ -262,6 +262,31 @@ def build_all():
     __graft_entry__.build()
 
 
+def cpu_model() -> str:
+    """The host CPU as /proc/cpuinfo or lscpu name it (architecture first)."""
+    import platform
+    import subprocess
+
+    name = ""
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "hardware")):
+                name = line.split(":", 1)[1].strip()
+                break
+    except OSError:
+        pass
+    if not name:
+        try:
+            out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+            for line in out.splitlines():
+                if line.startswith("Model name:"):
+                    name = line.split(":", 1)[1].strip()
+                    break
+        except (OSError, subprocess.SubprocessError):
+            pass
+    return f"{platform.machine()} {name}".strip()
+
+
 def cpu_sample(args, w, vox, nthreads, budget_rows=None):
     """Time the oracle (the reference's CPU backend, restated) on a bounded sample."""
     import numpy as np
@@ -356,7 +381,7 @@ def main_reference(args):
         "data": "synthetic",
         "config": {"workload": w.name, "inputs": "host memory (CPU backend)"},
         "cpu_baseline": {"value": value, "unit": "Gsamples/s", "cores": nthreads, "kind": "port",
-                         "sample": sample},
+                         "sample": sample, "cpu": cpu_model()},
         "e2e": {"value": value, "unit": "Gsamples/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -549,7 +574,7 @@ def main_ours(args):
             oview, op, view, y0, y1 = spec
             cpu = {"value": s / dt / 1e9, "unit": "Gsamples/s", "cores": nth, "kind": "port",
                    "sample": f"rows {y0}..{y1} of the {view.width}x{view.height} view, {s} samples, "
-                             f"{dt:.2f} s"}
+                             f"{dt:.2f} s", "cpu": cpu_model()}
             parity = rows_parity(ctx, vol, w, ov, spec, w.tf, nth)
         out_json = {
             "metric": "Gsamples/s",
