@@ -176,7 +176,10 @@ typedef struct hy_render_stats {
     float ms;               /* device time of the last render's kernels */
 } hy_render_stats;
 
-/* ---- context ---------------------------------------------------------------- */
+/* ---- context ----------------------------------------------------------------
+ * One CUDA device and its stream: the cufx::Device a BasicRenderer selects by
+ * comm_rank and holds a lock on while it renders (basic_renderer.hpp:43-52,
+ * 87-92, 170-176).  Errors are status codes; hy_last_error has the message. */
 int hy_ctx_create(int device, hy_ctx **out);
 int hy_ctx_destroy(hy_ctx *ctx);
 const char *hy_last_error(const hy_ctx *ctx);
@@ -189,7 +192,10 @@ int hy_render_stats_get(hy_ctx *ctx, hy_render_stats *out);
  * transfer_fn.hpp:16-23: Border, Linear, normalised coordinates). */
 int hy_tf_set(hy_ctx *ctx, const float *rgba, int32_t n);
 
-/* ---- volume (brick pool, page table, thumbnails) ---------------------------- */
+/* ---- volume (brick pool, page table, thumbnails) ----------------------------
+ * The bricks, the vaddr page table and the chebyshev / mean thumbnails a
+ * renderer builds from its dataset (basic_renderer.hpp:140-168,
+ * block_paging.hpp:38-44). */
 int hy_volume_create(hy_ctx *ctx, const hy_volume_desc *desc, hy_volume **out);
 int hy_volume_destroy(hy_volume *vol);
 /* Upload a whole raw volume (x fastest) from host memory; bricks it on the
@@ -212,7 +218,10 @@ int hy_camera_view(const hy_volume *vol, const hy_camera *cam, hy_view *out);
 /* Fill to_world / eye_pos / light_pos as IsosurfaceRenderer does (isosurface.cc:108-113). */
 int hy_iso_lighting(const hy_volume *vol, const hy_camera *cam, hy_shader_params *inout);
 
-/* ---- rendering -------------------------------------------------------------- */
+/* ---- rendering --------------------------------------------------------------
+ * A renderer's offline_render_ctxed for one view (basic_renderer.hpp:87-98;
+ * volume.cc:95-134): Raycaster's emit and pixel passes (raycaster.hpp:32-123)
+ * fused into one launch with no film in memory. */
 /* Fused emit + march + pixel for one view: rgba8 out (RGB by the reference's
  * write_to rule, A = trunc(clamp(v.a,0,1)*255)); optional float outputs:
  * v_out (W*H*4, pre-quantisation v), aux_out (W*H*4: Volume theta.xyz,phi;
