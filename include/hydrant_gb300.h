@@ -423,7 +423,9 @@ int hy_batch_get_config(const hy_batch *batch, hy_batch_config *out);
 int hy_batch_set_counting(hy_batch *batch, int32_t count_samples);
 /* Device output, asynchronous on the context's stream. */
 int hy_batch_render_device(hy_batch *batch, uint8_t *rgba_dev);
-/* Host output; returns when the images are on the host.  A pinned host
+/* Host output; returns when the images are on the host.  rgba_host must
+ * hold hy_batch_output_bytes bytes (as a cudaMemcpy destination must: a
+ * short pinned buffer would be overrun by the device).  A pinned host
  * buffer mapped into the device's address space (cudaHostAlloc, or
  * cudaHostRegister with mapping) is written by the kernel itself, with no
  * staging copy; any other buffer receives one copy from device memory. */
