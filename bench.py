@@ -74,8 +74,8 @@ def parse_args():
                          "block_queue (implies --no-autotune)")
     ap.add_argument("--no-autotune", action="store_true",
                     help="use the default batch launch shape (profiling)")
-    ap.add_argument("--cpu-sample-rows", type=int, default=0,
-                    help="rows of the CPU-baseline sample (0 = auto)")
+    ap.add_argument("--cpu-row-step", type=int, default=128,
+                    help="CPU sample: every this many-th pixel row of every view")
     ap.add_argument("--shader", choices=["Volume", "Blocks", "Isosurface"], default="",
                     help="tubes / volume / multiview: render with this shader instead")
     ap.add_argument("--mode", default="",
@@ -94,8 +94,23 @@ def workload(args):
     return with_overrides(args, base_workload(args))
 
 
+def workloads_module():
+    """hydrant_gb300/workloads.py (seeds, shapes, cameras, parameters) loaded
+    on its own: the CPU side of the measurement reads the workload
+    descriptions without importing the product package or its library."""
+    import importlib.util
+
+    name = "_hy_workload_defs"
+    if name not in sys.modules:
+        spec = importlib.util.spec_from_file_location(name, ROOT / "hydrant_gb300" / "workloads.py")
+        mod = importlib.util.module_from_spec(spec)
+        sys.modules[name] = mod
+        spec.loader.exec_module(mod)
+    return sys.modules[name]
+
+
 def base_workload(args):
-    from hydrant_gb300 import workloads as wl
+    wl = workloads_module()
 
     if args.workload == "volume":
         return wl.volume_c0()
@@ -287,84 +302,103 @@ def cpu_model() -> str:
     return f"{platform.machine()} {name}".strip()
 
 
-def cpu_sample(args, w, vox, nthreads, budget_rows=None):
-    """Time the oracle (the reference's CPU backend, restated) on a bounded sample."""
-    import numpy as np
+def workload_config(w, ov):
+    """The workload as both arms name it: the volume, bricking, views and
+    shader parameters, and the input size against L2 (the brick pool of the
+    non-empty bricks, 256-byte aligned slots)."""
+    P = w.block_size + 2 * w.padding
+    slot = (P ** 3 * (1 if w.generator.endswith("u8") else 4) + 255) // 256 * 256
+    pool = ov.nonempty * slot
+    return {
+        "workload": w.name, "volume": list(w.dim), "block_size": w.block_size,
+        "padding": w.padding, "views": len(w.views),
+        "pixels_per_step": sum(v.width * v.height for v in w.views),
+        "params": {k: v for k, v in w.params.items()},
+        "l2": ("inputs larger than L2 (brick pool %.2f GB)" % (pool / 1e9)) if pool >= 256 * 2**20
+              else ("L2 flushed between timed steps (brick pool %.1f MB)" % (pool / 1e6)),
+    }
 
-    import hydrant_gb300 as hy
+
+def cpu_views(w, ov, views=None):
+    """Per view of the workload: (oracle view array, oracle parameters, W, H).
+    `views`: the product's view arrays, so the oracle renders exactly the
+    rays the GPU rendered (parity); without them the oracle computes the
+    cameras itself (the reference arm loads nothing else)."""
     from oracle import oracle as orc
 
-    ov = orc.OracleVolume(vox, w.block_size, w.padding)
-    # the largest view; a band of rows through its middle
-    view = max(w.views, key=lambda v: v.width * v.height)
-    cam = __import__("hydrant_gb300.workloads", fromlist=["x"]).make_camera(view.camera)
-    ocam = np.array(list(cam.position) + list(cam.target) + list(cam.up) + [cam.ctg_fovy_2],
-                    np.float32)
-    oview = orc.camera_view(ov, ocam)
-    p = hy.shader_params(**w.params)
-    op = orc.params_from(p)
-    if p.shader == hy._abi.SHADER_ISOSURFACE:
-        orc.iso_lighting(ov, ocam, op)
-    rows = budget_rows or args.cpu_sample_rows or max(8, view.height // 32)
-    y0 = view.height // 2 - rows // 2
-    return ov, (oview, op, view, y0, y0 + rows)
+    out = []
+    for i, v in enumerate(w.views):
+        c = v.camera
+        cam = (orc.camera_orbit(c.a, c.target, c.fovy) if c.kind == "orbit"
+               else orc.camera_ptu(c.a, c.target, c.up, c.fovy))
+        p = orc.shader_params(**w.params)
+        if p.shader == 2:
+            orc.iso_lighting(ov, cam, p)
+        va = views[i] if views is not None else orc.camera_view(ov, cam)
+        out.append((va, p, v.width, v.height))
+    return out
 
 
-def rows_parity(ctx, vol, w, ov, spec, tf, nthreads):
-    """The GPU's image of the CPU-baseline view against the oracle on the
-    baseline's rows: max LSB difference of RGBA8 and max abs difference of
-    the pre-quantisation floats (the bar is <= 1 LSB and <= 1e-4)."""
-    import numpy as np
+def sample_rows(H, row_step):
+    y0 = min(row_step // 2, H // 2)
+    return y0, len(range(y0, H, row_step))
 
-    import hydrant_gb300 as hy
-    from hydrant_gb300 import workloads as wl
+
+def cpu_step(w, ov, cviews, row_step, nthreads, want_v=False, only=None):
+    """One step of the CPU sample: pixel rows row_step/2, row_step/2 +
+    row_step, ... of every view (1/row_step of the workload's rays, spread
+    over all views and over each image)."""
     from oracle import oracle as orc
 
-    oview, op, view, y0, y1 = spec
-    ref = orc.render(ov, tf, op, oview, view.width, view.height, nthreads=nthreads, want_v=True,
-                     want_aux=False, rows=(y0, y1))
-    cam = wl.make_camera(view.camera)
-    p = hy.shader_params(**w.params)
-    if p.shader == hy._abi.SHADER_ISOSURFACE:
-        hy.iso_lighting(vol, cam, p)
-    g = hy.render(ctx, vol, p, hy.camera_view(vol, cam), view.width, view.height, want_v=True)
-    lsb = int(np.abs(g.rgba[y0:y1].astype(int) - ref["rgba"][y0:y1].astype(int)).max())
-    fab = float(np.abs(g.v[y0:y1].astype(np.float64) - ref["v"][y0:y1]).max())
-    return {"rows": f"{y0}..{y1} of the {view.width}x{view.height} view", "max_lsb": lsb,
-            "max_abs": fab, "bar": "<= 1 LSB, <= 1e-4"}
+    samples, imgs = 0, []
+    for i, (va, p, W, H) in enumerate(cviews):
+        if only is not None and i not in only:
+            imgs.append(None)
+            continue
+        y0, _ = sample_rows(H, row_step)
+        r = orc.render_row_step(ov, w.tf, p, va, W, H, y0, row_step, nthreads, want_v=want_v)
+        samples += r["samples"]
+        imgs.append(r)
+    return samples, imgs
 
 
-def run_cpu_sample(ov, spec, tf, nthreads):
-    from oracle import oracle as orc
-
-    oview, op, view, y0, y1 = spec
-    t = time.perf_counter()
-    r = orc.render(ov, tf, op, oview, view.width, view.height, nthreads=nthreads, want_v=False,
-                   want_aux=False, rows=(y0, y1))
-    dt = time.perf_counter() - t
-    return r["samples"], dt
+def sample_desc(w, row_step, samples):
+    rays = 0
+    for v in w.views:
+        rays += v.width * sample_rows(v.height, row_step)[1]
+    return (f"every {row_step}th pixel row of all {len(w.views)} views ({rays} rays, "
+            f"1/{row_step} of the step's rays), {samples} samples per step")
 
 
 def main_reference(args):
+    """The reference's CPU multi-thread backend (cpu_shading.cc:9-90 over the
+    shared shaders, restated in oracle/) on every host thread, on a bounded
+    sample of the same workload: 1/row_step of every view's pixel rows.
+    Loads the oracle only: voxels, cameras and parameters come from the
+    oracle's own host code."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return 0
-    build_all()
+    from oracle import build as ob
+    from oracle import oracle as orc
+
+    ob.build()
     w = workload(args)
-    vox = w.voxels()
     nthreads = os.cpu_count() or 1
-    ov, spec = cpu_sample(args, w, vox, nthreads)
+    vox = orc.workload_voxels(w, nthreads)
+    ov = orc.OracleVolume(vox, w.block_size, w.padding)
+    cviews = cpu_views(w, ov)
+    step = max(1, args.cpu_row_step)
     for _ in range(args.warmup):
-        run_cpu_sample(ov, spec, w.tf, nthreads)
+        cpu_step(w, ov, cviews, step, nthreads)
     tot_s, tot_t = 0, 0.0
     for _ in range(args.steps):
-        s, dt = run_cpu_sample(ov, spec, w.tf, nthreads)
+        t = time.perf_counter()
+        s, _ = cpu_step(w, ov, cviews, step, nthreads)
+        tot_t += time.perf_counter() - t
         tot_s += s
-        tot_t += dt
     value = tot_s / tot_t / 1e9
-    oview, op, view, y0, y1 = spec
-    sample = (f"rows {y0}..{y1} of the {view.width}x{view.height} view "
-              f"({(y1 - y0) * view.width} rays), {tot_s // max(1, args.steps)} samples per step")
+    sample = sample_desc(w, step, tot_s // max(1, args.steps))
     out = {
         "impl": "reference",
         "metric": "Gsamples/s",
@@ -379,7 +413,7 @@ def main_reference(args):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": w.name, "inputs": "host memory (CPU backend)"},
+        "config": workload_config(w, ov),
         "cpu_baseline": {"value": value, "unit": "Gsamples/s", "cores": nthreads, "kind": "port",
                          "sample": sample, "cpu": cpu_model()},
         "e2e": {"value": value, "unit": "Gsamples/s", "h2d_bytes_per_step": 0,
@@ -387,6 +421,39 @@ def main_reference(args):
     }
     print(json.dumps(out), flush=True)
     return 0
+
+
+def view_array(view):
+    """A product view (hy_view) as the oracle's 20 floats."""
+    import numpy as np
+
+    return np.array(list(view.trans) + [view.ctg_fovy_2] + list(view.ray_o), np.float32)
+
+
+def sampled_parity(hy, ctx, vol, w, ov, views, params, cviews, imgs, batch, flat, step, nth):
+    """The timed batch kernel's images against the oracle on the CPU
+    sample's rows of every view (max LSB of RGBA8), and the pre-quantisation
+    floats of the largest view (the per-view lean kernel with a float
+    output, same march) against the oracle's on those rows."""
+    import numpy as np
+
+    lsb = 0
+    rows = 0
+    for i, (img, r) in enumerate(zip(batch.split(flat), imgs)):
+        H = img.shape[0]
+        y0, _ = sample_rows(H, step)
+        d = np.abs(img[y0::step].astype(np.int32) - r["rgba"][y0::step].astype(np.int32))
+        lsb = max(lsb, int(d.max()))
+        rows += d.shape[0]
+    big = max(range(len(views)), key=lambda i: views[i][1] * views[i][2])
+    v, W, H = views[big]
+    _, fl = cpu_step(w, ov, cviews, step, nth, want_v=True, only={big})
+    g = hy.render(ctx, vol, params[big], v, W, H, want_v=True)
+    y0, _ = sample_rows(H, step)
+    fab = float(np.abs(g.v[y0::step].astype(np.float64) - fl[big]["v"][y0::step]).max())
+    return {"rows": f"{rows} sampled rows over all {len(views)} views (batch kernel, RGBA8); "
+                    f"floats on the {W}x{H} view", "max_lsb": lsb, "max_abs": fab,
+            "bar": "<= 1 LSB, <= 1e-4"}
 
 
 def _timed_steps(torch, stream, steps, fn, flush=None):
@@ -422,7 +489,8 @@ def main_ours(args):
     dev = f"cuda:{local}"
     w = workload(args)
     t0 = time.perf_counter()
-    vox = w.voxels()
+    vox = {"blobs_u8": hy.synth_blobs_u8, "tubes_u8": hy.synth_tubes_u8,
+           "blobs_f32": hy.synth_blobs_f32}[w.generator](w.seed, w.dim, w.count)
     t_gen = time.perf_counter() - t0
     ctx = hy.Context(local)
     t0 = time.perf_counter()
@@ -565,17 +633,22 @@ def main_ours(args):
         ipsm = profile_per_sample(int(tuned.get("block_queue", 1)),
                                   "warp_instructions_per_sample")
     if rank == 0:
+        from oracle import oracle as orc
+
         cpu = None
         parity = None
+        nth = os.cpu_count() or 1
+        ov = orc.OracleVolume(vox, w.block_size, w.padding)
         if not args.no_cpu_baseline:
-            nth = os.cpu_count() or 1
-            ov, spec = cpu_sample(args, w, vox, nth)
-            s, dt = run_cpu_sample(ov, spec, w.tf, nth)
-            oview, op, view, y0, y1 = spec
+            step = max(1, args.cpu_row_step)
+            cviews = cpu_views(w, ov, [view_array(v) for v, _, _ in views])
+            t0 = time.perf_counter()
+            s, imgs = cpu_step(w, ov, cviews, step, nth)
+            dt = time.perf_counter() - t0
             cpu = {"value": s / dt / 1e9, "unit": "Gsamples/s", "cores": nth, "kind": "port",
-                   "sample": f"rows {y0}..{y1} of the {view.width}x{view.height} view, {s} samples, "
-                             f"{dt:.2f} s", "cpu": cpu_model()}
-            parity = rows_parity(ctx, vol, w, ov, spec, w.tf, nth)
+                   "sample": sample_desc(w, step, s) + f", {dt:.2f} s", "cpu": cpu_model()}
+            parity = sampled_parity(hy, ctx, vol, w, ov, views, params, cviews, imgs, batch,
+                                    out.cpu().numpy(), step, nth)
         out_json = {
             "metric": "Gsamples/s",
             "value": value,
@@ -589,17 +662,10 @@ def main_ours(args):
             "vs_baseline": None,
             "dtype": "f32",
             "data": "synthetic",
-            "config": {
-                "workload": w.name,
-                "volume": list(w.dim), "block_size": w.block_size, "padding": w.padding,
-                "views": len(views), "pixels_per_step": npix,
-                "samples_per_step": samples,
-                "path": "batched: one persistent launch per step from a CUDA graph",
-                "launch_shape": tuned,
-                "l2": ("inputs larger than L2 (brick pool %.2f GB)" % (info.pool_bytes / 1e9))
-                      if flush is None else
-                      ("L2 flushed between timed steps (brick pool %.1f MB)" % (info.pool_bytes / 1e6)),
-            },
+            "config": workload_config(w, ov),
+            "samples_per_step": samples,
+            "path": "batched: one persistent launch per step from a CUDA graph",
+            "launch_shape": tuned,
             "views_per_s": len(views) * ws * args.steps / t,
             "plain": {"value": plain_value, "unit": "Gsamples/s",
                       "views_per_s": len(views) * ws * args.steps / t_plain,

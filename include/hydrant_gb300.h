@@ -446,6 +446,8 @@ int hy_batch_autotune(hy_batch *batch, uint8_t *rgba_dev, int32_t reps, hy_batch
  * until exit; the first call on a device looks up its address and should
  * come before any stream capture.  Calls share that array: calls that overlap
  * on the GPU race.  More than 256 views is rejected with HY_ERR_INVALID.
+ * rgba_dev must hold at least max over views of rgba_offset + width*height*4
+ * bytes (there is no size argument to check it against).
  * Asynchronous on the context's stream; count_samples is ignored. */
 int hy_render_views_noalloc(hy_ctx *ctx, const hy_volume *vol, const hy_shader_params *params,
                             const hy_batch_view *views, int32_t nviews, uint8_t *rgba_dev);

@@ -17,7 +17,7 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 OUT = HERE / "_build"
 LIB = OUT / "libhy_oracle.so"
-SRC = [HERE / "hy_oracle.cc"]
+SRC = [HERE / "hy_oracle.cc", HERE / "synth.cc"]
 
 
 def build(force: bool = False) -> Path:

@@ -1169,6 +1169,35 @@ extern "C" int64_t orc_render_rows(const orc_volume *v, const float *tf, int32_t
     return total;
 }
 
+// A bounded sample for the CPU baseline: rows y0, y0 + ystep, ... below y1,
+// the m-th of them on thread m mod N (cpu_shading.cc's interleave over the
+// sampled rows).
+extern "C" int64_t orc_render_row_step(const orc_volume *v, const float *tf, int32_t ntf,
+                                       const orc_params *p, const float view[20], int32_t W,
+                                       int32_t H, int32_t y0, int32_t y1, int32_t ystep,
+                                       int32_t nthreads, float *v_out, uint8_t *rgba_out) {
+    if (!v || !p || !view || W <= 0 || H <= 0 || ystep <= 0) return -1;
+    if ((p->shader == 0) && (!tf || ntf <= 0)) return -1;
+    Ctx c = make_ctx(v, tf, ntf, p);
+    Out o{v_out, rgba_out, nullptr, nullptr};
+    if (nthreads <= 0) nthreads = int(std::thread::hardware_concurrency());
+    if (nthreads <= 0) nthreads = 1;
+    std::vector<int64_t> counts(nthreads, 0);
+    std::vector<std::thread> threads;
+    for (int i = 0; i < nthreads; ++i) {
+        threads.emplace_back([&, i] {
+            int64_t n = 0;
+            for (long long y = y0 + (long long)i * ystep; y < y1; y += (long long)nthreads * ystep)
+                for (int x = 0; x < W; ++x) n += shade_pixel(c, view, x, int(y), W, H, o);
+            counts[i] = n;
+        });
+    }
+    for (auto &t : threads) t.join();
+    int64_t total = 0;
+    for (auto n : counts) total += n;
+    return total;
+}
+
 extern "C" int64_t orc_render(const orc_volume *v, const float *tf, int32_t ntf,
                               const orc_params *p, const float view[20], int32_t W, int32_t H,
                               int32_t nthreads, float *v_out, uint8_t *rgba_out, float *aux_out,

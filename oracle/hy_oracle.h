@@ -90,6 +90,22 @@ int64_t orc_render_rows(const orc_volume *v, const float *tf_rgba, int32_t ntf,
                         int32_t height, int32_t y0, int32_t y1, int32_t nthreads,
                         float *v_out, uint8_t *rgba_out, float *aux_out, void *film_out);
 
+/* Rows y0, y0 + ystep, ... below y1 only (v_out / rgba_out are full-image
+ * buffers, written at those rows). */
+int64_t orc_render_row_step(const orc_volume *v, const float *tf_rgba, int32_t ntf,
+                            const orc_params *p, const float view[20], int32_t width,
+                            int32_t height, int32_t y0, int32_t y1, int32_t ystep,
+                            int32_t nthreads, float *v_out, uint8_t *rgba_out);
+
+/* Seeded synthetic volumes (oracle/synth.cc): the benchmark's generators,
+ * byte for byte, for the CPU side of the measurement. */
+int orc_synth_blobs_u8(uint64_t seed, const int32_t dim[3], int32_t nblobs, uint8_t *out,
+                       int32_t nthreads);
+int orc_synth_blobs_f32(uint64_t seed, const int32_t dim[3], int32_t nblobs, float *out,
+                        int32_t nthreads);
+int orc_synth_tubes_u8(uint64_t seed, const int32_t dim[3], int32_t ntubes, uint8_t *out,
+                       int32_t nthreads);
+
 /* Visible non-empty bricks (OctreeCuller::cull): the nearest `limit` (< 0:
  * all) by squared distance of the brick centre to the frustum origin, ties by
  * index, returned in index order.  rect = {min.x, min.y, max.x, max.y} or NULL

@@ -73,6 +73,12 @@ def lib() -> C.CDLL:
                                            C.c_int32, C.c_int32, P]),
             "orc_cull": (C.c_int32, [P, P, P, C.c_int32, P, P]),
             "orc_lossless_order": (None, [P, P, P, C.c_int32, P]),
+            "orc_render_row_step": (C.c_int64, [P, P, C.c_int32, C.POINTER(OrcParams), P,
+                                                C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                                C.c_int32, C.c_int32, P, P]),
+            "orc_synth_blobs_u8": (C.c_int, [C.c_uint64, P, C.c_int32, P, C.c_int32]),
+            "orc_synth_blobs_f32": (C.c_int, [C.c_uint64, P, C.c_int32, P, C.c_int32]),
+            "orc_synth_tubes_u8": (C.c_int, [C.c_uint64, P, C.c_int32, P, C.c_int32]),
         }
         for name, (res, args) in protos.items():
             fn = getattr(l, name)
@@ -84,6 +90,63 @@ def lib() -> C.CDLL:
 
 def _p(a: Optional[np.ndarray]):
     return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+SHADERS = {"Volume": 0, "Blocks": 1, "Isosurface": 2, "Paging": 3}
+MODES = {0: {"Default": 0, "Partition": 1, "Paging": 2}, 1: {"Volume": 0, "Solid": 1},
+         2: {"Color": 0, "Normal": 1, "Position": 2}, 3: {"Default": 0}}
+
+
+def shader_params(shader="Volume", mode=0, sample_rate=1.0, max_steps=4000000, density=1.0,
+                  isovalue=0.5, surface_color=(1.0, 1.0, 1.0), clear_color=(0.0, 0.0, 0.0),
+                  rank=0.0, lowest_blkcnt=0, composite=False, srgb=False,
+                  count_samples=False) -> OrcParams:
+    """Shader parameters by name, with the product's defaults (the CPU side
+    of the measurement builds them without loading the product library;
+    tests/test_oracle_synth.py holds the bytes equal)."""
+    p = OrcParams()
+    p.shader = SHADERS[shader] if isinstance(shader, str) else int(shader)
+    p.mode = MODES[p.shader][mode] if isinstance(mode, str) else int(mode)
+    p.sample_rate = sample_rate
+    p.max_steps = max_steps
+    p.density = density
+    p.isovalue = isovalue
+    p.surface_color = f3(*surface_color)
+    p.clear_color = f3(*clear_color)
+    p.rank = rank
+    p.lowest_blkcnt = lowest_blkcnt
+    p.composite = int(bool(composite))
+    p.srgb = int(bool(srgb))
+    p.count_samples = int(bool(count_samples))
+    return p
+
+
+def _synth(fn, dtype, seed, dim, count, nthreads):
+    nx, ny, nz = dim
+    out = np.empty((nz, ny, nx), dtype)
+    d = (C.c_int32 * 3)(nx, ny, nz)
+    if fn(seed, C.cast(d, P), count, _p(out), nthreads) != 0:
+        raise ValueError("bad synthetic volume arguments")
+    return out
+
+
+def synth_blobs_u8(seed, dim, count, nthreads=0):
+    return _synth(lib().orc_synth_blobs_u8, np.uint8, seed, dim, count, nthreads)
+
+
+def synth_blobs_f32(seed, dim, count, nthreads=0):
+    return _synth(lib().orc_synth_blobs_f32, np.float32, seed, dim, count, nthreads)
+
+
+def synth_tubes_u8(seed, dim, count, nthreads=0):
+    return _synth(lib().orc_synth_tubes_u8, np.uint8, seed, dim, count, nthreads)
+
+
+def workload_voxels(w, nthreads=0):
+    """Voxels of a workload description (generator, seed, dims, count)."""
+    fn = {"blobs_u8": synth_blobs_u8, "tubes_u8": synth_tubes_u8,
+          "blobs_f32": synth_blobs_f32}[w.generator]
+    return fn(w.seed, w.dim, w.count, nthreads)
 
 
 def params_from(struct) -> OrcParams:
@@ -195,6 +258,21 @@ def render(vol: OracleVolume, tf, params: OrcParams, view: np.ndarray, width: in
                                   height, rows[0], rows[1], nthreads, _p(v), _p(rgba), _p(aux),
                                   _p(film))
     return dict(v=v, rgba=rgba, aux=aux, film=film, samples=int(n))
+
+
+def render_row_step(vol: OracleVolume, tf, params: OrcParams, view: np.ndarray, width: int,
+                    height: int, y0: int, ystep: int, nthreads: int = 0, want_v=False):
+    """Rows y0, y0 + ystep, ... of one view (a bounded sample spread over
+    the image); the full-size outputs hold those rows."""
+    tfa = np.ascontiguousarray(np.asarray(tf, np.float32).reshape(-1, 4))
+    v = np.zeros((height, width, 4), np.float32) if want_v else None
+    rgba = np.zeros((height, width, 4), np.uint8)
+    view = np.ascontiguousarray(view, np.float32)
+    n = lib().orc_render_row_step(vol.h, _p(tfa), tfa.shape[0], C.byref(params), _p(view), width,
+                                  height, y0, height, ystep, nthreads, _p(v), _p(rgba))
+    if n < 0:
+        raise ValueError("orc_render_row_step: bad arguments")
+    return dict(v=v, rgba=rgba, samples=int(n))
 
 
 def march_film(vol: OracleVolume, tf, params: OrcParams, film: np.ndarray, width: int, height: int,

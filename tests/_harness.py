@@ -35,13 +35,23 @@ class Case:
         self.vol.close()
 
     def render_both(self, cam, W, H, nthreads=0, **kw):
+        """GPU and oracle images of one view.  The GPU renders twice: with the
+        aux output (theta / phi or depth) and without it.  Without aux the
+        Volume shader in Default mode takes the lean march (the instantiation
+        the benchmark times), so both kernel instantiations face the oracle;
+        the lean one is checked here (images, floats, sample count) and the
+        full one is returned for the caller's own checks."""
         p = hy.shader_params(count_samples=True, **kw)
         if p.shader == hy._abi.SHADER_ISOSURFACE:
             hy.iso_lighting(self.vol, cam, p)
         view = hy.camera_view(self.vol, cam)
         self.ctx.set_transfer_fn(self.tf)
         g = hy.render(self.ctx, self.vol, p, view, W, H, want_v=True, want_aux=True)
+        lean = hy.render(self.ctx, self.vol, p, view, W, H, want_v=True, want_aux=False)
         r = orc.render(self.ov, self.tf, orc.params_from(p), view_array(view), W, H, nthreads=nthreads)
+        assert_parity(lean, r, check_aux=False, what=f"no-aux render {kw}")
+        assert np.array_equal(lean.rgba, g.rgba) and np.array_equal(lean.v, g.v), \
+            f"no-aux render differs from the aux render {kw}"
         return g, r, p, view
 
 

@@ -42,11 +42,13 @@ def test_gpu_matches_golden(ctx, case):
         p = hy.shader_params(count_samples=True, **{k: val for k, val in params.items()})
         if p.shader == hy._abi.SHADER_ISOSURFACE:
             hy.iso_lighting(vol, hy.camera_orbit(arm), p)
-        r = hy.render(ctx, vol, p, view, W, H, want_v=True, want_aux=True)
-        d8 = np.abs(r.rgba.astype(int) - GOLDEN[f"{name}/rgba"].astype(int)).max()
-        assert d8 <= 1
-        gv = GOLDEN[f"{name}/v"]
-        assert np.abs(r.v - gv).max() <= 1e-4
-        assert r.samples == int(GOLDEN[f"{name}/samples"][0])
+        # with aux output, and without it (the Volume shader's lean march)
+        for want_aux in (True, False):
+            r = hy.render(ctx, vol, p, view, W, H, want_v=True, want_aux=want_aux)
+            d8 = np.abs(r.rgba.astype(int) - GOLDEN[f"{name}/rgba"].astype(int)).max()
+            assert d8 <= 1, f"aux={want_aux}: {d8} LSB"
+            gv = GOLDEN[f"{name}/v"]
+            assert np.abs(r.v - gv).max() <= 1e-4, f"aux={want_aux}"
+            assert r.samples == int(GOLDEN[f"{name}/samples"][0]), f"aux={want_aux}"
     finally:
         vol.close()

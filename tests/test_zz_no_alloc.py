@@ -87,3 +87,81 @@ def test_noalloc_rejects_more_views_than_the_scratch_holds(ctx):
         assert b"256" in hy.lib().hy_last_error(ctx.handle)
     finally:
         vol.close()
+
+
+def _batch_views(views, offsets):
+    arr = (_abi.HyBatchView * len(views))()
+    for i, ((v, W, H), off) in enumerate(zip(views, offsets)):
+        arr[i].view = v
+        arr[i].width = W
+        arr[i].height = H
+        arr[i].rgba_offset = off
+    return arr
+
+
+def test_noalloc_matches_oracle(ctx):
+    """The entry point runs the lean batch march the benchmark times: its
+    images face the oracle directly (a 128^3 blob volume in 64^3 bricks with
+    an apron, four cameras on a seeded sphere), twice in a row."""
+    torch = pytest.importorskip("torch")
+    from oracle import oracle as orc
+    from tests._harness import view_array
+
+    w = wl.multiview_c3(n=128, nviews=4, resolutions=(48, 96, 160))
+    vox = w.voxels()
+    vol = hy.Volume(ctx, vox, w.block_size, w.padding)
+    ov = orc.OracleVolume(vox, w.block_size, w.padding)
+    try:
+        ctx.set_transfer_fn(w.tf)
+        p = hy.shader_params(**w.params)
+        views = [(hy.camera_view(vol, wl.make_camera(v.camera)), v.width, v.height)
+                 for v in w.views]
+        offsets = np.cumsum([0] + [W * H * 4 for _, W, H in views]).tolist()
+        arr = _batch_views(views, offsets[:-1])
+        refs = [orc.render(ov, w.tf, orc.params_from(p), view_array(v), W, H, want_v=False,
+                           want_aux=False)["rgba"] for v, W, H in views]
+        for attempt in range(2):
+            out = torch.full((offsets[-1],), 3, dtype=torch.uint8, device="cuda")
+            ctx.check(hy.lib().hy_render_views_noalloc(ctx.handle, vol.handle, C.byref(p), arr,
+                                                       len(views), C.c_void_p(out.data_ptr())))
+            ctx.synchronize()
+            flat = out.cpu().numpy()
+            for i, ((_, W, H), ref) in enumerate(zip(views, refs)):
+                got = flat[offsets[i]:offsets[i] + W * H * 4].reshape(H, W, 4)
+                d = np.abs(got.astype(np.int32) - ref.astype(np.int32)).max()
+                assert d <= 1, f"call {attempt}, view {i}: {d} LSB"
+    finally:
+        vol.close()
+
+
+def test_noalloc_at_the_view_limit(ctx):
+    """256 views -- the most the static scratch holds, filling every
+    descriptor slot and the largest shared-memory table of view starts --
+    render as the batched entry point renders them."""
+    torch = pytest.importorskip("torch")
+    vol = hy.Volume(ctx, hy.synth_blobs_u8(6, (64, 64, 64), 8), 32, 1)
+    try:
+        ctx.set_transfer_fn(wl.TF9)
+        rng = wl.SplitMix64(29)
+        p = hy.shader_params(shader="Volume", density=0.5, sample_rate=0.5)
+        views = []
+        for i in range(256):
+            arm = (rng.uniform(-180, 180), rng.uniform(-60, 60), rng.uniform(1.8, 2.6))
+            views.append((hy.camera_view(vol, hy.camera_orbit(arm)), 8 + i % 5, 8 + i % 3))
+        offsets = np.cumsum([0] + [W * H * 4 for _, W, H in views]).tolist()
+        b = hy.Batch(ctx, vol, p, views)
+        ref = torch.zeros(b.nbytes, dtype=torch.uint8, device="cuda")
+        b.render_device(ref.data_ptr())
+        ctx.synchronize()
+        expect = ref.cpu().numpy()
+        b.close()
+        arr = _batch_views(views, offsets[:-1])
+        for attempt in range(2):
+            out = torch.full((offsets[-1],), 5, dtype=torch.uint8, device="cuda")
+            ctx.check(hy.lib().hy_render_views_noalloc(ctx.handle, vol.handle, C.byref(p), arr,
+                                                       256, C.c_void_p(out.data_ptr())))
+            ctx.synchronize()
+            assert np.array_equal(out.cpu().numpy(), expect), f"call {attempt}"
+        assert expect.any()
+    finally:
+        vol.close()
