@@ -59,6 +59,10 @@ def parse_args():
     ap.add_argument("--res", type=int, default=0,
                     help="keep only the views of this resolution (profiling a small case)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ckpt-k", type=int, default=32,
+                    help="diff workload: checkpoint interval of the differentiable march")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="leave out the compositing and differentiable legs (profiling)")
     ap.add_argument("--coarse-level", type=int, default=3,
                     help="paging: coarse fallback level (box filter 2**L; 0 = none)")
     ap.add_argument("--pager", choices=["realtime", "lossless"], default="realtime",
@@ -423,6 +427,51 @@ def main_reference(args):
     return 0
 
 
+def composite_leg(hy, ctx, vol, w, views, lighting, stream, flush, args):
+    """All views of the step with per-brick sort-last compositing (every
+    non-empty brick a ray crosses is its own segment, composited front to
+    back with volume.cc:267-280): batched (one persistent launch from a CUDA
+    graph) and plain (one launch per view), CUDA events on the library's
+    stream."""
+    import torch
+
+    kw = dict(w.params)
+    kw["composite"] = True
+    p = hy.shader_params(**kw)
+    batch = hy.Batch(ctx, vol, p, views, lighting)
+    try:
+        out = torch.empty(batch.nbytes, dtype=torch.uint8, device=f"cuda:{ctx.device}")
+        batch.set_counting(True)
+        batch.render_device(out.data_ptr())
+        samples = ctx.stats().samples
+        batch.set_counting(False)
+        for _ in range(args.warmup):
+            batch.render_device(out.data_ptr())
+        evs = _timed_steps(torch, stream, args.steps, lambda: batch.render_device(out.data_ptr()),
+                           flush)
+        ctx.synchronize()
+        tb = sum(a.elapsed_time(b) for a, b in evs) / 1e3 / args.steps
+
+        def plain_step():
+            for (view, W, H), off in zip(views, batch.offsets):
+                hy.render_device(ctx, vol, p, view, W, H, out.data_ptr() + off)
+
+        for _ in range(args.warmup):
+            plain_step()
+        evs = _timed_steps(torch, stream, args.steps, plain_step, flush)
+        ctx.synchronize()
+        tp = sum(a.elapsed_time(b) for a, b in evs) / 1e3 / args.steps
+    finally:
+        batch.close()
+    return {"value": samples / tb / 1e9, "unit": "Gsamples/s", "samples_per_step": samples,
+            "ms_per_step": tb * 1e3, "views_per_s": len(views) / tb,
+            "plain": {"value": samples / tp / 1e9, "unit": "Gsamples/s", "ms_per_step": tp * 1e3,
+                      "views_per_s": len(views) / tp},
+            "batched_over_plain": tp / tb,
+            "path": "per-brick segments composited front to back; batched = one persistent "
+                    "launch per step from a CUDA graph, plain = one launch per view"}
+
+
 def view_array(view):
     """A product view (hy_view) as the oracle's 20 floats."""
     import numpy as np
@@ -617,6 +666,14 @@ def main_ours(args):
     if ws > 1:
         (t_e2e,) = max_over_ranks([t_e2e], dev)
 
+    # ---- the configuration's compositing variant and the differentiable
+    # configuration, each at its stated size (rank 0 of a 1-GPU run) -------
+    composite = diff = None
+    if ws == 1 and not args.no_extra:
+        if not args.composite:
+            composite = composite_leg(hy, ctx, vol, w, views, lighting, stream, flush, args)
+        diff = diff_leg(hy, ctx, dev)
+
     value = aggregate_gsamples(samples, ws, args.steps, t)
     plain_value = aggregate_gsamples(samples, ws, args.steps, t_plain)
     e2e = aggregate_gsamples(samples, ws, args.steps, t_e2e)
@@ -696,6 +753,8 @@ def main_ours(args):
             "gpu_launches": args.steps,
             "clocks": ck,
             "setup_s": {"generate": t_gen, "upload_and_brick": t_up},
+            "composite": composite,
+            "diff": diff,
         }
         print(json.dumps(out_json), flush=True)
     batch.close()
@@ -811,11 +870,112 @@ def main_paging(args):
     return 0
 
 
+DIFF_CONFIG = dict(n=256, res=512, views=16, knots=32, ckpt_k=32, blobs=24)
+
+
+def diff_leg(hy, ctx, dev, reps=5, fd_params=4, ckpt_k=None):
+    """The differentiable configuration at its stated size: 256^3 f32 blob
+    density (seed 4 truth, seed 5 estimate), 32-knot TF, 16 views of 512^2
+    on a seeded orbit, checkpoints every 32 steps.  Times (CUDA events on the
+    library's stream, every launch on that stream) the forward without and
+    with checkpoints and the adjoint, per view; and checks the adjoint's
+    gradient of the L2 image loss against central finite differences
+    (eps 1e-3, loss in float64) on the largest knot and voxel gradients and
+    along a random direction over all knots."""
+    import numpy as np
+    import torch
+
+    from hydrant_gb300 import fit
+
+    c = DIFF_CONFIG
+    n, res, nv, ntf = c["n"], c["res"], c["views"], c["knots"]
+    K = ckpt_k or c["ckpt_k"]
+    vt = hy.synth_blobs_f32(4, (n, n, n), c["blobs"])
+    vi = hy.synth_blobs_f32(5, (n, n, n), c["blobs"])
+    holder = hy.Volume(ctx, vt, n, 1)
+    views = fit.orbit_views(holder, 4, nv)
+    holder.close()
+    tft = fit.seeded_tf(4, ntf)
+    r = fit.DiffRenderer(ctx, n, views, res, res, ntf, ckpt_k=K)
+    out = {}
+    with torch.cuda.stream(r.stream):
+        target = r.forward(torch.from_numpy(vt).to(dev), torch.from_numpy(tft).to(dev),
+                           keep=False).clone()
+        vol = torch.from_numpy(vi).to(dev)
+        # a non-uniform TF (the fit starts from uniform grey, where the image
+        # does not depend on the voxels at all)
+        tf = torch.from_numpy(np.clip(tft * 0.8 + 0.1, 0, 1).astype(np.float32)).to(dev)
+
+        def timed(fn):
+            for _ in range(2):
+                fn()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(r.stream)
+            for _ in range(reps):
+                fn()
+            e1.record(r.stream)
+            e1.synchronize()
+            return e0.elapsed_time(e1) / reps / nv
+
+        img = r.forward(vol, tf, keep=True)
+        g = (2.0 / img.numel()) * (img - target)
+        fwd = timed(lambda: r.forward(vol, tf, keep=False))
+        fwd_k = timed(lambda: r.forward(vol, tf, keep=True))
+        bwd = timed(lambda: r.backward(vol, tf, g))
+        r.forward(vol, tf, keep=True)
+        dvol, dtf = r.backward(vol, tf, g)
+
+        def loss64(v, t):
+            im = r.forward(v, t, keep=False)
+            return float(((im.double() - target.double()) ** 2).mean())
+
+        eps = 1e-3
+        checks = []
+        gt = dtf.reshape(-1)
+        for idx in torch.topk(gt.abs(), fd_params).indices.tolist():
+            tp, tm = tf.clone(), tf.clone()
+            tp.view(-1)[idx] += eps
+            tm.view(-1)[idx] -= eps
+            fd = (loss64(vol, tp) - loss64(vol, tm)) / (2 * eps)
+            checks.append(("knot", idx, float(gt[idx]), fd))
+        gv = dvol.reshape(-1)
+        for idx in torch.topk(gv.abs(), fd_params).indices.tolist():
+            vp, vm = vol.clone(), vol.clone()
+            vp.view(-1)[idx] += eps
+            vm.view(-1)[idx] -= eps
+            fd = (loss64(vp, tf) - loss64(vm, tf)) / (2 * eps)
+            checks.append(("voxel", idx, float(gv[idx]), fd))
+        gen = torch.Generator(device="cpu").manual_seed(7)
+        d = torch.randn(tf.shape, generator=gen).to(dev)
+        fd = (loss64(vol, tf + eps * d) - loss64(vol, tf - eps * d)) / (2 * eps)
+        checks.append(("knot direction", -1, float((dtf * d).sum()), fd))
+    torch.cuda.synchronize()
+    rel = [abs(a - f) / max(abs(f), 1e-30) for _, _, a, f in checks]
+    out.update({
+        "config": {"workload": f"diff_{n}cube_{nv}x{res}px_{ntf}knots_K{K}", "volume": [n, n, n],
+                   "dtype": "f32", "views": nv, "resolution": res, "knots": ntf, "ckpt_k": K},
+        "forward_ms_per_view": fwd,
+        "forward_ckpt_ms_per_view": fwd_k,
+        "adjoint_ms_per_view": bwd,
+        "fwd_adjoint_ms_per_view": fwd_k + bwd,
+        "fwd_adjoint_over_forward": (fwd_k + bwd) / fwd,
+        "fwd_adjoint_over_forward_ckpt": (fwd_k + bwd) / fwd_k,
+        "fd_check": {"eps": eps, "loss": "mean squared image error (float64)",
+                     "max_rel_err": max(rel),
+                     "cases": [{"param": k, "index": i, "adjoint": a, "fd": f,
+                                "rel_err": e} for (k, i, a, f), e in zip(checks, rel)]},
+        "timing": "CUDA events on the library stream, mean of %d launches after 2 warm-up" % reps,
+    })
+    r.ckpt = None
+    return out
+
+
 def main_diff(args):
     """Differentiable fit: 256^3 f32 blob density (seed 4 truth, seed 5 init),
     32-knot RGBA TF (seeded truth, uniform grey init), 16 views of 512^2 on a
-    seeded orbit, L2 image loss, checkpoints every 16 steps, Adam for
-    --steps iterations (default 200 here)."""
+    seeded orbit, L2 image loss, checkpoints every --ckpt-k (32) steps, Adam
+    for --frames iterations (default 200 here); the kernel timings and the
+    finite-difference check of diff_leg beside it."""
     import numpy as np
     import torch
 
@@ -837,19 +997,22 @@ def main_diff(args):
     tfi = np.full((ntf, 4), 0.5, np.float32)
     t0 = time.perf_counter()
     warm = max(3, args.warmup)
-    res_fit = fit.fit(ctx, vt, vi, views, res, res, tft, tfi, steps=steps, ckpt_k=16, warmup=warm)
+    K = args.ckpt_k
+    res_fit = fit.fit(ctx, vt, vi, views, res, res, tft, tfi, steps=steps, ckpt_k=K, warmup=warm)
     wall = time.perf_counter() - t0
+    kernels = diff_leg(hy, ctx, f"cuda:{local}", ckpt_k=K)
     out = {
         "metric": "fwd+adjoint ms/view", "value": res_fit.fwd_adj_ms_per_view, "unit": "ms/view",
         "n_gpus": 1, "steps": steps, "warmup": warm, "higher_is_better": False, "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": f"diff_fit_{n}cube_{nviews}x{res}px_{ntf}knots", "ckpt_k": 16},
+        "config": {"workload": f"diff_fit_{n}cube_{nviews}x{res}px_{ntf}knots", "ckpt_k": K},
         "forward_ms_per_view": res_fit.fwd_ms_per_view,
         "adjoint_over_forward": res_fit.fwd_adj_ms_per_view / res_fit.fwd_ms_per_view,
         "iteration_ms_median": float(np.median(res_fit.iter_ms)),
         "loss_first": res_fit.losses[0], "loss_last": res_fit.losses[-1],
         "loss_curve": res_fit.losses[:: max(1, steps // 20)],
         "wall_s": wall,
+        "kernels": kernels,
     }
     print(json.dumps(out), flush=True)
     ctx.close()

@@ -44,9 +44,15 @@ def nvcc() -> str:
     raise RuntimeError("nvcc not found")
 
 
+def extra_flags() -> list[str]:
+    """Macro settings for tuning builds (e.g. "-DHY_DIFF_MIN_BLOCKS=6"), from
+    HYDRANT_GB300_NVCC_DEFINES; only -D options are taken."""
+    return [f for f in os.environ.get("HYDRANT_GB300_NVCC_DEFINES", "").split() if f.startswith("-D")]
+
+
 def _compile(src: str, verbose: bool) -> Path:
     obj = BUILD / (Path(src).stem + ".o")
-    cmd = [nvcc(), *ARCH, *NVCC_COMMON, "-c", str(CSRC / src), "-o", str(obj)]
+    cmd = [nvcc(), *ARCH, *NVCC_COMMON, *extra_flags(), "-c", str(CSRC / src), "-o", str(obj)]
     if verbose:
         cmd.insert(1, "-Xptxas=-v")
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -68,7 +74,10 @@ def _stale(sources: list[Path], target: Path) -> bool:
 
 def build(force: bool = False, verbose: bool = False) -> Path:
     srcs = [CSRC / s for s in SOURCES]
-    if not force and not _stale(srcs, LIB):
+    stamp = BUILD / "defines.txt"
+    defines = " ".join(extra_flags())
+    same_defines = (stamp.read_text() if stamp.exists() else "") == defines
+    if not force and same_defines and not _stale(srcs, LIB):
         return LIB
     BUILD.mkdir(exist_ok=True)
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
@@ -79,6 +88,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    stamp.write_text(defines)
     return LIB
 
 
