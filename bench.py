@@ -59,6 +59,8 @@ def parse_args():
     ap.add_argument("--res", type=int, default=0,
                     help="keep only the views of this resolution (profiling a small case)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--sampler", choices=["gather", "loads"], default="gather",
+                    help="Volume march over u8 bricks: texture gathers or loads")
     ap.add_argument("--ckpt-k", type=int, default=32,
                     help="diff workload: checkpoint interval of the differentiable march")
     ap.add_argument("--no-extra", action="store_true",
@@ -546,6 +548,7 @@ def main_ours(args):
     vol = hy.Volume(ctx, vox, w.block_size, w.padding)
     t_up = time.perf_counter() - t0
     ctx.set_transfer_fn(w.tf)
+    vol.set_gather_sampling(args.sampler == "gather")
     info = vol.info
 
     views, params, lighting, bufs = [], [], [], []
@@ -722,6 +725,8 @@ def main_ours(args):
             "config": workload_config(w, ov),
             "samples_per_step": samples,
             "path": "batched: one persistent launch per step from a CUDA graph",
+            "sampler": ("two texture gathers per sample (u8 bricks in gather textures)"
+                        if vol.gather_sampling else "eight loads per sample from the brick pool"),
             "launch_shape": tuned,
             "views_per_s": len(views) * ws * args.steps / t,
             "plain": {"value": plain_value, "unit": "Gsamples/s",

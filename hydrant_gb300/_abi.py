@@ -140,6 +140,8 @@ _PROTOS = {
     "hy_volume_upload": (C.c_int, [P, P]),
     "hy_volume_get_info": (C.c_int, [P, C.POINTER(HyVolumeInfo)]),
     "hy_volume_thumbnails": (C.c_int, [P, P, P]),
+    "hy_volume_set_gather_sampling": (C.c_int, [P, C.c_int32]),
+    "hy_volume_gather_sampling": (C.c_int, [P, C.POINTER(C.c_int32)]),
     "hy_camera_orbit": (C.c_int, [P, P, C.c_float, C.POINTER(HyCamera)]),
     "hy_camera_ptu": (C.c_int, [P, P, P, C.c_float, C.POINTER(HyCamera)]),
     "hy_camera_view": (C.c_int, [P, C.POINTER(HyCamera), C.POINTER(HyView)]),

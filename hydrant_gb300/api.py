@@ -109,6 +109,18 @@ class Volume:
         self.ctx.check(lib().hy_volume_get_info(self.handle, C.byref(i)))
         return i
 
+    def set_gather_sampling(self, on: bool) -> None:
+        """Volume march over u8 bricks with an apron: two texture gathers per
+        sample (on, the default) or eight loads (off); same images."""
+        self.ctx.check(lib().hy_volume_set_gather_sampling(self.handle, int(bool(on))))
+
+    @property
+    def gather_sampling(self) -> bool:
+        """Whether renders of this volume use the gathers."""
+        v = C.c_int32()
+        self.ctx.check(lib().hy_volume_gather_sampling(self.handle, C.byref(v)))
+        return bool(v.value)
+
     def thumbnails(self):
         i = self.info
         n = i.nbricks

@@ -20,9 +20,28 @@ struct __align__(16) RegEntry {
 };
 static_assert(sizeof(RegEntry) == 32, "RegEntry is two 16-byte loads");
 
+// Where a resident u8 brick also sits in a 2-D gather texture: its P
+// slices stacked as P x P tiles in one column of texels, slice z at rows
+// y0 + z * P, columns x0 .. x0 + P - 1, in texture `which` (0 or 1) of the
+// volume.  The texture returns a u8 texel u as the float u / 255
+// (normalised read), so one gather fetches four normalised taps of the
+// trilinear footprint.
+struct __align__(16) TexEntry {
+    float x0, y0;
+    int which;
+    int pad_;
+};
+static_assert(sizeof(TexEntry) == 16, "TexEntry is one 16-byte load");
+// A volume's bricks go in at most this many gather textures; the handles
+// travel in the kernel parameters, so every gather names a warp-uniform
+// texture (a per-brick handle in a register would make the compiler
+// serialise the gather over the distinct handles of a warp).
+constexpr int kMaxGatherTextures = 2;
+
 // Device view of a volume: the brick pool, the page table + chebyshev
 // thumbnail packed per brick as int2 {chebyshev, registry id or -1}, the
-// registry, and the mean thumbnail.
+// registry, and the mean thumbnail; `tex` (per registry id, or null) places
+// each brick in a gather texture.
 struct DevVolume {
     const unsigned char *pool;
     const int2 *info;
@@ -32,6 +51,9 @@ struct DevVolume {
     int P;      // padded brick edge
     int dtype;  // HY_DTYPE_*
     int pad;    // apron width
+    const TexEntry *tex;
+    unsigned long long gtex[kMaxGatherTextures];  // cudaTextureObject_t
+    float map_k, map_b;  // BlockSamplerMapping of every resident brick (with `tex`)
 };
 
 // Per-view inputs: ViewArgs (shader.hpp:63-68) plus the image size and the
@@ -118,6 +140,11 @@ struct hy_volume {
     float du = 0.f;
     bool uploaded = false;
     bool paged = false;       // pool is a brick cache owned by a hy_pager
+    // gather textures of the resident bricks (u8 with an apron; see TexEntry)
+    std::vector<cudaArray_t> atlas;
+    std::vector<unsigned long long> atlas_tex;
+    hy::TexEntry *tex_dev = nullptr;
+    bool tex_sampling = true;  // hy_volume_set_gather_sampling
 };
 
 // Brick store: every non-empty padded brick in pinned host memory, laid out
@@ -144,6 +171,12 @@ struct hy_store {
 };
 
 int hy_volume_init(hy_ctx *ctx, const hy_volume_desc *desc, hy_volume *v);
+// The gather-texture table of a volume's bricks when they have one and
+// sampling through it is on, else null (hy_volume.cu).
+const hy::TexEntry *hy_volume_gather_table(const hy_volume *v);
+// Fills the gather fields of a device view of the volume (table and handles,
+// or null and zeros).
+void hy_volume_gather_view(const hy_volume *v, hy::DevVolume *dv);
 // store helpers (hy_page.cu): grid / padded edge / slot stride from a
 // descriptor, and the pinned allocation for `nonempty` bricks
 void hy_store_geometry(hy_store *s, const hy_volume_desc &d);

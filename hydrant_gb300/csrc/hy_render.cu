@@ -50,7 +50,7 @@ __device__ __forceinline__ uchar4 quantise(const ShadeArgs &A, float4 v) {
 
 // LEAN: Volume shader, Default mode, no compositing and no aux output
 // (theta / phi are not computed; see VolumeMarch::step).
-template <int SHADER, int PC, int DT, bool PADDED, int COMPOSITE, bool LEAN>
+template <int SHADER, int PC, int DT, bool PADDED, int COMPOSITE, bool LEAN, bool GATHER = false>
 __device__ __forceinline__ void render_body(const ShadeArgs &A) {
     extern __shared__ float4 smem[];
     float4 *tf = smem;
@@ -68,9 +68,9 @@ __device__ __forceinline__ void render_body(const ShadeArgs &A) {
             samples = composite_ray<SHADER, PC, DT, PADDED>(A, A.view, S, ox, oy, oz, dx, dy, dz, v, aux);
         } else {
             Px p;
-            samples = emit<SHADER, PC, DT, PADDED, LEAN>(p, A, A.view, S, ox, oy, oz, dx, dy, dz,
-                                                         0.f, 0.f, 0.f, A.bbox_max[0],
-                                                         A.bbox_max[1], A.bbox_max[2]);
+            samples = emit<SHADER, PC, DT, PADDED, LEAN, GATHER>(
+                p, A, A.view, S, ox, oy, oz, dx, dy, dz, 0.f, 0.f, 0.f, A.bbox_max[0],
+                A.bbox_max[1], A.bbox_max[2]);
             v = make_float4(p.vx, p.vy, p.vz, p.vw);
             if (SHADER == HY_SHADER_VOLUME)
                 aux = make_float4(p.e0, p.e1, p.e2, p.e3);
@@ -87,9 +87,20 @@ __device__ __forceinline__ void render_body(const ShadeArgs &A) {
     count_samples(A, samples);
 }
 
-template <int SHADER, int PC, int DT, bool PADDED, int COMPOSITE, bool LEAN>
+template <int SHADER, int PC, int DT, bool PADDED, int COMPOSITE, bool LEAN, bool GATHER = false>
 __global__ void __launch_bounds__(kThreads) render_kernel(const __grid_constant__ ShadeArgs A) {
-    render_body<SHADER, PC, DT, PADDED, COMPOSITE, LEAN>(A);
+    render_body<SHADER, PC, DT, PADDED, COMPOSITE, LEAN, GATHER>(A);
+}
+
+// The lean march sampling by texture gathers, held to HY_RENDER_GATHER_REGS
+// registers (the gathers' latency wants resident warps).
+#ifndef HY_RENDER_GATHER_REGS
+#define HY_RENDER_GATHER_REGS 56
+#endif
+template <int SHADER, int PC, int DT, bool PADDED>
+__global__ void __maxnreg__(HY_RENDER_GATHER_REGS)
+    render_gather_kernel(const __grid_constant__ ShadeArgs A) {
+    render_body<SHADER, PC, DT, PADDED, 0, true, true>(A);
 }
 
 // The per-brick compositing variants of the Volume and Isosurface shaders,
@@ -261,6 +272,13 @@ void launch_fused(const ShadeArgs &a, cudaStream_t s) {
     }
     if constexpr (SHADER == HY_SHADER_VOLUME) {
         if (a.mode == HY_VOLUME_DEFAULT && !a.aux) {
+            if constexpr (DT == HY_DTYPE_U8 && PADDED) {
+                if (a.vol.tex) {  // bricks in gather textures
+                    render_gather_kernel<SHADER, PC, DT, PADDED>
+                        <<<grid_of(a), kThreads, smem_bytes(a), s>>>(a);
+                    return;
+                }
+            }
             render_kernel<SHADER, PC, DT, PADDED, 0, true><<<grid_of(a), kThreads, smem_bytes(a), s>>>(a);
             return;
         }
@@ -347,7 +365,9 @@ int hy_fill_args(hy_ctx *ctx, const hy_volume *vol, const hy_shader_params *p, c
         return hy_fail(ctx, HY_ERR_STATE, "render: Volume shader needs a transfer function");
     std::memset(a, 0, sizeof(*a));
     a->vol = DevVolume{vol->pool, vol->info_dev, vol->reg_dev, vol->mean_dev, vol->grid[0],
-                       vol->grid[1], vol->grid[2], vol->P, vol->desc.dtype, vol->desc.padding};
+                       vol->grid[1], vol->grid[2], vol->P, vol->desc.dtype, vol->desc.padding,
+                       nullptr, {0ull, 0ull}, vol->k, vol->b};
+    hy_volume_gather_view(vol, &a->vol);
     for (int i = 0; i < 3; ++i) a->bbox_max[i] = vol->bbox_max[i];
     a->du = vol->du;
     a->step = vol->du / 4.f / p->sample_rate;  // basic_renderer.hpp:129

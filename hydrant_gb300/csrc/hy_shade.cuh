@@ -110,18 +110,27 @@ __device__ __forceinline__ int skip_nblock_steps(Px &p, float rx, float ry, floa
     return skip_count(di);
 }
 
-// A resident brick: BlockSampler {storage, mapping} (block_paging.hpp:24-36).
+// A resident brick: BlockSampler {storage, mapping} (block_paging.hpp:24-36);
+// with GATHER its gather texture (which) and texel origin (TexEntry) instead
+// of the pool address.
 struct BrickRef {
     const unsigned char *base;
     float k, bx, by, bz;
+    float tx, ty;
+    int which;
 };
 
+template <bool GATHER = false>
 __device__ __forceinline__ BrickRef load_brick(const DevVolume &V, int reg) {
     const float4 *e = reinterpret_cast<const float4 *>(V.reg + reg);
+    if (GATHER) {  // resident bricks: the mapping is the volume's (V.map_k, V.map_b)
+        const float4 t = __ldg(reinterpret_cast<const float4 *>(V.tex + reg));
+        return BrickRef{nullptr, 0.f, 0.f, 0.f, 0.f, t.x, t.y, __float_as_int(t.z)};
+    }
     float4 m = __ldg(e);
     float4 o = __ldg(e + 1);
     long long off = (long long)__float_as_uint(o.x) | ((long long)__float_as_uint(o.y) << 32);
-    return BrickRef{V.pool + off, m.x, m.y, m.z, m.w};
+    return BrickRef{V.pool + off, m.x, m.y, m.z, m.w, 0.f, 0.f, 0};
 }
 
 // Brick sample: BlockSampler::sample_3d -> CpuSampler with normalised
@@ -174,6 +183,35 @@ __device__ __forceinline__ float lut_at(const float *__restrict__ lut, unsigned 
 template <int TAP>
 __device__ __forceinline__ float u8_value(unsigned char u, const float *__restrict__ lut) {
     return TAP < HY_U8_ARITH_TAPS ? u8_norm(u) : lut_at(lut, u);
+}
+
+// The lerps of a trilinear sample (cpu_sampler.hpp:88-104, do_lerp
+// x*(1-a) + y*a): the taps in z pairs, c<y><x> = (tap at layer z, tap at
+// layer z + 1), fractions axy = (ax, ay) and az.
+__device__ __forceinline__ float trilerp(float2 c00, float2 c01, float2 c10, float2 c11,
+                                         float2 axy, float az) {
+#if HY_F32X2
+    // lerp along x of both z layers at once, then along y, then z:
+    // X0 = (x0_0, x0_1), X1 = (x1_0, x1_1), Y = (y0, y1)
+    const float2 bxy = sub2(f2(1.f, 1.f), axy);
+    const float bz = 1.f - az;
+    const float2 bx2 = f2(bxy.x, bxy.x), ax2 = f2(axy.x, axy.x);
+    const float2 X0 = lerp2(c00, bx2, c01, ax2);
+    const float2 X1 = lerp2(c10, bx2, c11, ax2);
+    const float2 Y = lerp2(X0, f2(bxy.y, bxy.y), X1, f2(axy.y, axy.y));
+    const float2 Z = mul2(Y, f2(bz, az));
+    return __fadd_rn(Z.x, Z.y);
+#else
+    const float ax = axy.x, ay = axy.y;
+    const float bx = 1.f - ax, by = 1.f - ay, bz = 1.f - az;
+    float x0_0 = c00.x * bx + c01.x * ax;
+    float x1_0 = c10.x * bx + c11.x * ax;
+    float x0_1 = c00.y * bx + c01.y * ax;
+    float x1_1 = c10.y * bx + c11.y * ax;
+    float y0 = x0_0 * by + x1_0 * ay;
+    float y1 = x0_1 * by + x1_1 * ay;
+    return y0 * bz + y1 * az;
+#endif
 }
 
 template <int PC, int DT, bool INTERIOR = false>
@@ -260,25 +298,82 @@ __device__ __forceinline__ float sample_brick(const BrickRef &b, int Prt, float 
         }
     }
 #if HY_F32X2
-    // lerp along x of both z layers at once, then along y, then z:
-    // X0 = (x0_0, x0_1), X1 = (x1_0, x1_1), Y = (y0, y1)
-    const float2 bxy = sub2(f2(1.f, 1.f), axy);
-    const float bz = 1.f - az;
-    const float2 bx2 = f2(bxy.x, bxy.x), ax2 = f2(axy.x, axy.x);
-    const float2 X0 = lerp2(c00, bx2, c01, ax2);
-    const float2 X1 = lerp2(c10, bx2, c11, ax2);
-    const float2 Y = lerp2(X0, f2(bxy.y, bxy.y), X1, f2(axy.y, axy.y));
-    const float2 Z = mul2(Y, f2(bz, az));
+    return trilerp(c00, c01, c10, c11, axy, az);
+#else
+    return trilerp(c00, c01, c10, c11, f2(ax, ay), az);
+#endif
+}
+
+#ifndef HY_GATHER_ROWS
+#define HY_GATHER_ROWS 1
+#endif
+// Brick sample through the brick's gather texture (interior case only, the
+// same arithmetic as sample_brick<PC, HY_DTYPE_U8, true>): the texel
+// coordinates of the footprint are whole numbers, so the two gathers fetch
+// exactly the taps the loads would, already normalised (u / 255, checked
+// per device when the textures are built).
+// The two gathers of a footprint from the volume's texture `which`: each
+// branch names a handle from the kernel parameters, so the texture is
+// warp-uniform in each (lanes in bricks of different textures take both).
+__device__ __forceinline__ void gather2(const DevVolume &V, int which, float X, float Y, float fd,
+                                        float4 &g0, float4 &g1) {
+    if (which == 0) {
+        g0 = tex2Dgather<float4>(V.gtex[0], X, Y, 0);
+        g1 = tex2Dgather<float4>(V.gtex[0], X, Y + fd, 0);
+    } else {
+        g0 = tex2Dgather<float4>(V.gtex[1], X, Y, 0);
+        g1 = tex2Dgather<float4>(V.gtex[1], X, Y + fd, 0);
+    }
+}
+
+template <int PC>
+__device__ __forceinline__ float sample_brick_gather(const DevVolume &V, const BrickRef &b,
+                                                     int Prt, float lx, float ly, float lz) {
+    const int P = PC ? PC : Prt;
+    const float fd = float(P);
+    const float k = V.map_k, bm = V.map_b;  // every resident brick's mapping
+#if HY_F32X2
+    const float2 kl = mul2(f2(k, k), f2(lx, ly));
+    const float2 fxy0 = mul2(f2(fd, fd), f2(__fadd_rn(kl.x, bm), __fadd_rn(kl.y, bm)));
+    const float fx = fxy0.x, fy = fxy0.y, fz = fd * (k * lz + bm);
+    const float ux = fx - .5f, uy = fy - .5f, uz = fz - .5f;
+    const float flx = floorf(ux), fly = floorf(uy), flz = floorf(uz);
+    const float2 axy = sub2(f2(ux, uy), f2(flx, fly));
+    const float az = uz - flz;
+#else
+    const float mx = k * lx + bm, my = k * ly + bm, mz = k * lz + bm;
+    const float fx = fd * mx, fy = fd * my, fz = fd * mz;
+    const float ux = fx - .5f, uy = fy - .5f, uz = fz - .5f;
+    const float flx = floorf(ux), fly = floorf(uy), flz = floorf(uz);
+    const float2 axy = f2(ux - flx, uy - fly);
+    const float az = uz - flz;
+#endif
+    // column of tap x + 1 and row of tap (y + 1, z): whole numbers below
+    // 2^24, so the sums are exact and the gather's footprint is (x, y) ..
+    // (x + 1, y + 1) of slice z (and, P rows further down, of slice z + 1)
+    const float X = (b.tx + flx) + 1.f;
+    const float Y = (b.ty + (flz * fd + fly)) + 1.f;
+    float4 g0, g1;
+    gather2(V, b.which, X, Y, fd, g0, g1);
+    // gather order: w = (x, y), z = (x + 1, y), x = (x, y + 1), y = (x + 1, y + 1)
+#if HY_F32X2 && HY_GATHER_ROWS
+    // The x lerps row by row, each row's two taps as the gather returns them
+    // (adjacent registers): (x, y+1), (x+1, y+1) times (1-ax, ax) and
+    // (x+1, y), (x, y) times (ax, 1-ax), then one scalar add per row (IEEE
+    // addition commutes, so each row is fl(fl(c_x (1-ax)) + fl(c_x1 ax)) as
+    // in trilerp); then y per slice and z as there.
+    const float bx = 1.f - axy.x;
+    const float2 w10 = f2(bx, axy.x), w01 = f2(axy.x, bx);
+    const float2 r1z0 = mul2(f2(g0.x, g0.y), w10), r0z0 = mul2(f2(g0.z, g0.w), w01);
+    const float2 r1z1 = mul2(f2(g1.x, g1.y), w10), r0z1 = mul2(f2(g1.z, g1.w), w01);
+    const float2 X0 = f2(__fadd_rn(r0z0.x, r0z0.y), __fadd_rn(r0z1.x, r0z1.y));  // row y
+    const float2 X1 = f2(__fadd_rn(r1z0.x, r1z0.y), __fadd_rn(r1z1.x, r1z1.y));  // row y + 1
+    const float by = 1.f - axy.y, bz = 1.f - az;
+    const float2 Yv = lerp2(X0, f2(by, by), X1, f2(axy.y, axy.y));
+    const float2 Z = mul2(Yv, f2(bz, az));
     return __fadd_rn(Z.x, Z.y);
 #else
-    const float bx = 1.f - ax, by = 1.f - ay, bz = 1.f - az;
-    float x0_0 = c00.x * bx + c01.x * ax;
-    float x1_0 = c10.x * bx + c11.x * ax;
-    float x0_1 = c00.y * bx + c01.y * ax;
-    float x1_1 = c10.y * bx + c11.y * ax;
-    float y0 = x0_0 * by + x1_0 * ay;
-    float y1 = x0_1 * by + x1_1 * ay;
-    return y0 * bz + y1 * az;
+    return trilerp(f2(g0.w, g1.w), f2(g0.z, g1.z), f2(g0.x, g1.x), f2(g0.y, g1.y), axy, az);
 #endif
 }
 
@@ -362,6 +457,7 @@ struct BrickCursor {
         br = BrickRef{};
     }
     // o's cell changed (or may have): redo floor(o) and the thumbnail lookups
+    template <bool GATHER = false>
     __device__ __forceinline__ void locate(const DevVolume &V, float ox, float oy, float oz) {
         const float fgx = float(V.gx), fgy = float(V.gy), fgz = float(V.gz);
         ipx = floorf(ox);
@@ -374,10 +470,11 @@ struct BrickCursor {
             cd = in.x;
             pg = in.y;
             sample = cd == 0 && pg != -1;
-            if (cd == 0 && pg >= 0) br = load_brick(V, pg);
+            if (cd == 0 && pg >= 0) br = load_brick<GATHER>(V, pg);
         }
     }
     // brick-local coordinates of o, relocating first when o left the cell
+    template <bool GATHER = false>
     __device__ __forceinline__ void update(const DevVolume &V, float ox, float oy, float oz,
                                            float &lx, float &ly, float &lz) {
 #if HY_F32X2
@@ -390,7 +487,7 @@ struct BrickCursor {
 #endif
         lz = oz - ipz;
         if (unit_interval(lx) & unit_interval(ly) & unit_interval(lz)) return;
-        locate(V, ox, oy, oz);
+        locate<GATHER>(V, ox, oy, oz);
         lx = ox - ipx;
         ly = oy - ipy;
         lz = oz - ipz;
@@ -400,9 +497,11 @@ struct BrickCursor {
 // VolumeShaderKernel::main (volume_shader.cu:32-81) as the per-ray state and
 // one loop iteration; volume_main is the loop.  PADDED: the volume has an
 // apron of >= 1 voxel, so the interior sampler applies.
+// The reciprocals the empty-brick skip needs (1/d and 1/compMax(|d|)) are
+// computed where a skip happens rather than held for the whole ray: the
+// same floats, four registers fewer in the march.
 struct VolumeMarch {
     BrickCursor c;
-    float cdu, rx, ry, rz;
     float sx, sy, sz;  // (d * step) * step_size, redone only when step_size changes
 
     __device__ __forceinline__ void set_step(const Px &p, float step) {
@@ -414,10 +513,6 @@ struct VolumeMarch {
 
     // p.step_size is 1 for a new ray, or what a film pass left
     __device__ __forceinline__ void init(const Px &p, float step) {
-        cdu = 1.f / gmax(gmax(fabsf(p.dx), fabsf(p.dy)), fabsf(p.dz));
-        rx = 1.f / p.dx;
-        ry = 1.f / p.dy;
-        rz = 1.f / p.dz;
         c.reset();
         set_step(p, step);
     }
@@ -426,18 +521,24 @@ struct VolumeMarch {
     // on an absent brick (volume_shader.cu:50).  LEAN: Default mode and
     // nobody reads theta / phi (no film, aux output or per-brick
     // compositing), so their updates are left out; v is unchanged.
-    template <int PC, int DT, bool PADDED, bool LEAN = false>
+    // GATHER: u8 bricks with an apron sampled through their gather textures.
+    template <int PC, int DT, bool PADDED, bool LEAN = false, bool GATHER = false>
     __device__ __forceinline__ bool step(Px &p, const ShadeArgs &A, const Shared &S,
                                          unsigned int &samples) {
         const DevVolume &V = A.vol;
         float lx, ly, lz;
-        c.update(V, p.ox, p.oy, p.oz, lx, ly, lz);
+        c.update<GATHER>(V, p.ox, p.oy, p.oz, lx, ly, lz);
         if (!c.sample) {
             if (c.cd == 0) return false;  // absent brick (pg == -1)
-            p.nsteps -= skip_nblock_steps(p, rx, ry, rz, c.ipx, c.ipy, c.ipz, c.cd, cdu,
-                                          A.step * float(p.step_size));
+            const float cdu = 1.f / gmax(gmax(fabsf(p.dx), fabsf(p.dy)), fabsf(p.dz));
+            p.nsteps -= skip_nblock_steps(p, 1.f / p.dx, 1.f / p.dy, 1.f / p.dz, c.ipx, c.ipy,
+                                          c.ipz, c.cd, cdu, A.step * float(p.step_size));
         } else {
-            float s = sample_brick<PC, DT, PADDED>(c.br, V.P, lx, ly, lz, S.lut);
+            float s;
+            if constexpr (GATHER)
+                s = sample_brick_gather<PC>(V, c.br, V.P, lx, ly, lz);
+            else
+                s = sample_brick<PC, DT, PADDED>(c.br, V.P, lx, ly, lz, S.lut);
             ++samples;
             float4 ub = sample_tf<DT == HY_DTYPE_U8>(S.tf, S.ntf, S.fntf, s);
             if (LEAN) {
@@ -500,13 +601,13 @@ struct VolumeMarch {
     }
 };
 
-template <int PC, int DT, bool PADDED, bool LEAN = false>
+template <int PC, int DT, bool PADDED, bool LEAN = false, bool GATHER = false>
 __device__ __forceinline__ long long volume_main(Px &p, const ShadeArgs &A, const Shared &S) {
     unsigned int samples = 0;
     VolumeMarch m;
     m.init(p, A.step);
     while (p.nsteps > 0)
-        if (!m.step<PC, DT, PADDED, LEAN>(p, A, S, samples)) break;
+        if (!m.step<PC, DT, PADDED, LEAN, GATHER>(p, A, S, samples)) break;
     return samples;
 }
 
@@ -724,10 +825,10 @@ __device__ __forceinline__ long long iso_main(Px &p, const ShadeArgs &A, const V
     return samples;
 }
 
-template <int SHADER, int PC, int DT, bool PADDED, bool LEAN = false>
+template <int SHADER, int PC, int DT, bool PADDED, bool LEAN = false, bool GATHER = false>
 __device__ __forceinline__ long long run_main(Px &p, const ShadeArgs &A, const ViewArgs &Vw,
                                              const Shared &S) {
-    if (SHADER == HY_SHADER_VOLUME) return volume_main<PC, DT, PADDED, LEAN>(p, A, S);
+    if (SHADER == HY_SHADER_VOLUME) return volume_main<PC, DT, PADDED, LEAN, GATHER>(p, A, S);
     if (SHADER == HY_SHADER_BLOCKS) return blocks_main(p, A);
     if (SHADER == HY_SHADER_PAGING) return paging_main(p, A);
     return iso_main<PC, DT, PADDED>(p, A, Vw, S);
@@ -793,14 +894,14 @@ __device__ __forceinline__ bool emit_setup(Px &p, const ShadeArgs &A, float ox, 
 }
 
 // ray_emit_shader_impl: emit_setup, then main on a hit (shader.hpp:113-137).
-template <int SHADER, int PC, int DT, bool PADDED, bool LEAN = false>
+template <int SHADER, int PC, int DT, bool PADDED, bool LEAN = false, bool GATHER = false>
 __device__ __forceinline__ long long emit(Px &p, const ShadeArgs &A, const ViewArgs &Vw,
                                           const Shared &S, float ox,
                                           float oy, float oz, float dx, float dy, float dz,
                                           float x0, float y0, float z0, float x1, float y1,
                                           float z1) {
     if (emit_setup<SHADER>(p, A, ox, oy, oz, dx, dy, dz, x0, y0, z0, x1, y1, z1))
-        return run_main<SHADER, PC, DT, PADDED, LEAN>(p, A, Vw, S);
+        return run_main<SHADER, PC, DT, PADDED, LEAN, GATHER>(p, A, Vw, S);
     return 0;
 }
 

@@ -19,6 +19,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <mutex>
 
 #include "hy_internal.h"
 
@@ -128,7 +129,163 @@ void chebyshev_transform(const std::vector<unsigned int> &nonempty, const int g[
         if (out[i] < 0) out[i] = cap;
 }
 
+// ---- gather textures ---------------------------------------------------------
+//
+// Every resident brick of a u8 volume with an apron is also placed in a 2-D
+// u8 texture made for gather: its P slices stacked as P x P tiles in one
+// column of texels (slice z at rows y0 + z * P).  The interior sampler then
+// fetches the eight taps of a trilinear footprint with two gathers (slices
+// z and z + 1), each returning the 2x2 texels at rows y, y + 1 and columns
+// x, x + 1 as floats, normalised by the texture unit.  The coordinates are
+// whole texel edges (x + 1, y + 1 with x, y integral), so the footprint the
+// hardware picks is exactly (x, y) .. (x + 1, y + 1).  Bricks with P^2 rows
+// taller than a gather texture allows keep the plain loads.
+
+__global__ void gather_check_kernel(cudaTextureObject_t t, unsigned int *bad) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= 255) return;
+    // row 0 holds u = column, row 1 holds 255 - column
+    const float4 g = tex2Dgather<float4>(t, float(x) + 1.f, 1.f, 0);
+    const float ew = __fdiv_rn(float(x), 255.f), ez = __fdiv_rn(float(x + 1), 255.f);
+    const float ex = __fdiv_rn(float(255 - x), 255.f), ey = __fdiv_rn(float(254 - x), 255.f);
+    if (__float_as_uint(g.w) != __float_as_uint(ew) || __float_as_uint(g.z) != __float_as_uint(ez) ||
+        __float_as_uint(g.x) != __float_as_uint(ex) || __float_as_uint(g.y) != __float_as_uint(ey))
+        atomicAdd(bad, 1u);
+}
+
+cudaTextureObject_t make_gather_texture(cudaArray_t arr, cudaError_t *err) {
+    cudaResourceDesc rd;
+    std::memset(&rd, 0, sizeof(rd));
+    rd.resType = cudaResourceTypeArray;
+    rd.res.array.array = arr;
+    cudaTextureDesc td;
+    std::memset(&td, 0, sizeof(td));
+    td.addressMode[0] = td.addressMode[1] = cudaAddressModeClamp;
+    td.filterMode = cudaFilterModePoint;
+    td.readMode = cudaReadModeNormalizedFloat;
+    td.normalizedCoords = 0;
+    cudaTextureObject_t t = 0;
+    *err = cudaCreateTextureObject(&t, &rd, &td, nullptr);
+    return t;
+}
+
+// Once per device: the gather order and the u8 -> u / 255 normalisation
+// of the texture unit equal what the sampler assumes (for all 256 values,
+// against IEEE division).  A device that fails renders with the plain loads.
+constexpr int kMaxCheckDevices = 64;
+std::mutex g_gather_mu;
+int g_gather_ok[kMaxCheckDevices] = {};  // 0 unknown, 1 passed, -1 failed
+
+int gather_check(hy_ctx *ctx, bool *ok) {
+    *ok = false;
+    if (ctx->device < 0 || ctx->device >= kMaxCheckDevices) return HY_OK;
+    std::lock_guard<std::mutex> lock(g_gather_mu);
+    if (g_gather_ok[ctx->device] == 0) {
+        cudaChannelFormatDesc cd = cudaCreateChannelDesc(8, 0, 0, 0, cudaChannelFormatKindUnsigned);
+        cudaArray_t arr = nullptr;
+        unsigned int *bad = nullptr;
+        cudaTextureObject_t t = 0;
+        unsigned char host[2 * 256];
+        for (int c = 0; c < 256; ++c) {
+            host[c] = (unsigned char)c;
+            host[256 + c] = (unsigned char)(255 - c);
+        }
+        unsigned int nbad = 1;
+        cudaError_t e = cudaMallocArray(&arr, &cd, 256, 2, cudaArrayTextureGather);
+        if (e == cudaSuccess)
+            e = cudaMemcpy2DToArrayAsync(arr, 0, 0, host, 256, 256, 2, cudaMemcpyHostToDevice,
+                                         ctx->stream);
+        if (e == cudaSuccess) t = make_gather_texture(arr, &e);
+        if (e == cudaSuccess) e = cudaMalloc(&bad, sizeof(unsigned int));
+        if (e == cudaSuccess) e = cudaMemsetAsync(bad, 0, sizeof(unsigned int), ctx->stream);
+        if (e == cudaSuccess) {
+            gather_check_kernel<<<1, 256, 0, ctx->stream>>>(t, bad);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(&nbad, bad, sizeof(unsigned int), cudaMemcpyDeviceToHost,
+                                ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (t) cudaDestroyTextureObject(t);
+        if (arr) cudaFreeArray(arr);
+        if (bad) cudaFree(bad);
+        if (e != cudaSuccess) return hy_cuda_fail(ctx, e, "volume: gather texture check");
+        g_gather_ok[ctx->device] = nbad == 0 ? 1 : -1;
+    }
+    *ok = g_gather_ok[ctx->device] == 1;
+    return HY_OK;
+}
+
+void free_gather(hy_volume *v) {
+    for (auto t : v->atlas_tex) cudaDestroyTextureObject(cudaTextureObject_t(t));
+    for (auto a : v->atlas) cudaFreeArray(a);
+    if (v->tex_dev) cudaFree(v->tex_dev);
+    v->atlas_tex.clear();
+    v->atlas.clear();
+    v->tex_dev = nullptr;
+}
+
+int build_gather(hy_volume *vol) {
+    hy_ctx *ctx = vol->ctx;
+    const int P = vol->P;
+    if (vol->desc.dtype != HY_DTYPE_U8 || vol->desc.padding < 1 || vol->resident <= 0) return HY_OK;
+    int gw = 0, gh = 0;
+    HY_CUDA(ctx, cudaDeviceGetAttribute(&gw, cudaDevAttrMaxTexture2DGatherWidth, ctx->device));
+    HY_CUDA(ctx, cudaDeviceGetAttribute(&gh, cudaDevAttrMaxTexture2DGatherHeight, ctx->device));
+    const long long brick_rows = (long long)P * P;
+    if (P > gw || brick_rows > gh) return HY_OK;  // too tall for a gather texture
+    bool ok = false;
+    int rc = gather_check(ctx, &ok);
+    if (rc || !ok) return rc;
+    const int cols = gw / P, rowblocks = int(gh / brick_rows), per = cols * rowblocks;
+    const int n = vol->resident;
+    if ((long long)per * hy::kMaxGatherTextures < n) return HY_OK;  // more than the textures hold
+    std::vector<hy::TexEntry> table(n);
+    cudaChannelFormatDesc cd = cudaCreateChannelDesc(8, 0, 0, 0, cudaChannelFormatKindUnsigned);
+    for (int first = 0; first < n; first += per) {
+        const int cnt = std::min(per, n - first);
+        const int ucols = std::min(cols, cnt), urows = (cnt + cols - 1) / cols;
+        cudaArray_t arr = nullptr;
+        cudaError_t e = cudaMallocArray(&arr, &cd, size_t(ucols) * P, size_t(urows) * brick_rows,
+                                        cudaArrayTextureGather);
+        if (e != cudaSuccess) {
+            free_gather(vol);
+            return hy_cuda_fail(ctx, e, "volume: gather texture allocation");
+        }
+        vol->atlas.push_back(arr);
+        cudaTextureObject_t t = make_gather_texture(arr, &e);
+        if (e != cudaSuccess) {
+            free_gather(vol);
+            return hy_cuda_fail(ctx, e, "volume: gather texture object");
+        }
+        vol->atlas_tex.push_back((unsigned long long)t);
+        for (int i = 0; i < cnt; ++i) {
+            const int slot = first + i, cx = i % cols, ry = i / cols;
+            e = cudaMemcpy2DToArrayAsync(arr, size_t(cx) * P, size_t(ry) * brick_rows,
+                                         vol->pool + size_t(slot) * vol->slot_stride, P, P,
+                                         brick_rows, cudaMemcpyDeviceToDevice, ctx->stream);
+            if (e != cudaSuccess) {
+                free_gather(vol);
+                return hy_cuda_fail(ctx, e, "volume: gather texture fill");
+            }
+            table[slot] = hy::TexEntry{float(cx * P), float(ry * brick_rows),
+                                       int(vol->atlas_tex.size()) - 1, 0};
+        }
+    }
+    cudaError_t e = cudaMalloc(&vol->tex_dev, size_t(n) * sizeof(hy::TexEntry));
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(vol->tex_dev, table.data(), size_t(n) * sizeof(hy::TexEntry),
+                            cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) {
+        free_gather(vol);
+        return hy_cuda_fail(ctx, e, "volume: gather table");
+    }
+    return HY_OK;
+}
+
 void free_volume_device(hy_volume *v) {
+    free_gather(v);
     if (v->pool) cudaFree(v->pool);
     if (v->info_dev) cudaFree(v->info_dev);
     if (v->reg_dev) cudaFree(v->reg_dev);
@@ -234,7 +391,7 @@ int upload_impl(hy_volume *vol, const void *host) {
 #undef HY_UP
     cleanup();
     vol->uploaded = true;
-    return HY_OK;
+    return build_gather(vol);
 }
 
 }  // namespace
@@ -296,6 +453,28 @@ extern "C" int hy_volume_upload(hy_volume *vol, const void *host_voxels) {
     HY_CUDA(vol->ctx, cudaSetDevice(vol->ctx->device));
     if (vol->desc.dtype == HY_DTYPE_U8) return upload_impl<unsigned char>(vol, host_voxels);
     return upload_impl<float>(vol, host_voxels);
+}
+
+const hy::TexEntry *hy_volume_gather_table(const hy_volume *v) {
+    return (v->tex_sampling && v->tex_dev) ? v->tex_dev : nullptr;
+}
+
+void hy_volume_gather_view(const hy_volume *v, hy::DevVolume *dv) {
+    dv->tex = hy_volume_gather_table(v);
+    for (int i = 0; i < hy::kMaxGatherTextures; ++i)
+        dv->gtex[i] = (dv->tex && i < int(v->atlas_tex.size())) ? v->atlas_tex[i] : 0ull;
+}
+
+extern "C" int hy_volume_set_gather_sampling(hy_volume *vol, int32_t enable) {
+    if (!vol) return HY_ERR_INVALID;
+    vol->tex_sampling = enable != 0;
+    return HY_OK;
+}
+
+extern "C" int hy_volume_gather_sampling(const hy_volume *vol, int32_t *active) {
+    if (!vol || !active) return HY_ERR_INVALID;
+    *active = hy_volume_gather_table(vol) ? 1 : 0;
+    return HY_OK;
 }
 
 extern "C" int hy_volume_get_info(const hy_volume *vol, hy_volume_info *out) {

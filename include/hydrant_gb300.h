@@ -206,6 +206,18 @@ int hy_volume_destroy(hy_volume *vol);
  * Once per volume (HY_ERR_STATE after that): new data is a new volume. */
 int hy_volume_upload(hy_volume *vol, const void *host_voxels);
 int hy_volume_get_info(const hy_volume *vol, hy_volume_info *out);
+/* Sampler of the Volume shader's march over a resident u8 volume with an
+ * apron: the eight taps of a trilinear sample fetched by two texture gathers
+ * (on, the default) or by eight loads from the brick pool (off).  Both give
+ * the same floats: the upload places every brick in a gather texture whose
+ * texels the texture unit returns as u / 255, checked bit for bit against
+ * IEEE division once per device (a device that fails uses the loads).  The
+ * reference samples its bricks through textures as well (texture_3d.hpp:
+ * 78-86), there with hardware filtering; here the lerps stay in FP32 as the
+ * CPU backend computes them.  hy_volume_gather_sampling reports whether the
+ * gathers are in use (on, and the volume has gather textures). */
+int hy_volume_set_gather_sampling(hy_volume *vol, int32_t enable);
+int hy_volume_gather_sampling(const hy_volume *vol, int32_t *active);
 /* Copy the per-brick thumbnails to the host (grid x fastest). */
 int hy_volume_thumbnails(const hy_volume *vol, int32_t *chebyshev, float *mean);
 

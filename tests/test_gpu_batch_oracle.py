@@ -59,16 +59,25 @@ def _compare(got, ref, what):
     return exact / total
 
 
+@pytest.mark.parametrize("gather", [True, False], ids=["gathers", "loads"])
 @pytest.mark.parametrize("kw", [
     dict(shader="Volume", mode="Default", sample_rate=0.25, density=1e-2),
     dict(shader="Volume", mode="Default", sample_rate=0.25, density=0.5),
     dict(shader="Volume", mode="Default", sample_rate=0.25, density=0.5, composite=True),
 ], ids=["lean", "lean_dense", "composite"])
-def test_batch_matches_oracle(ctx, c3_small, kw):
+def test_batch_matches_oracle(ctx, c3_small, kw, gather):
+    """The lean march samples the bricks by texture gathers (the default for
+    u8 bricks with an apron) or by loads; a batch takes the volume's setting
+    when it is created."""
     w, vol, ov, views = c3_small
+    assert vol.gather_sampling
     p = hy.shader_params(**kw)
     ref, ref_samples = _oracle_views(w, ov, p, views)
-    b = hy.Batch(ctx, vol, p, views)
+    vol.set_gather_sampling(gather)
+    try:
+        b = hy.Batch(ctx, vol, p, views)
+    finally:
+        vol.set_gather_sampling(True)
     try:
         b.set_counting(True)
         for cfg in [(8, 1, 4, 0, 1), (16, 2, 8, 0, 0)]:
@@ -81,3 +90,22 @@ def test_batch_matches_oracle(ctx, c3_small, kw):
     finally:
         b.close()
 
+
+
+def test_gather_sampling_where_it_applies(ctx):
+    """Gather textures are built for u8 volumes with an apron (and a brick
+    column that fits a gather texture); f32 and apron-less volumes sample
+    by loads.  Switching it off and on is honoured."""
+    u8 = hy.Volume(ctx, hy.synth_blobs_u8(1, (70, 40, 50), 6), 16, 1)
+    f32 = hy.Volume(ctx, hy.synth_blobs_f32(1, (40, 40, 40), 6), 16, 1)
+    bare = hy.Volume(ctx, hy.synth_blobs_u8(1, (40, 40, 40), 6), 16, 0)
+    try:
+        assert u8.gather_sampling
+        assert not f32.gather_sampling and not bare.gather_sampling
+        u8.set_gather_sampling(False)
+        assert not u8.gather_sampling
+        u8.set_gather_sampling(True)
+        assert u8.gather_sampling
+    finally:
+        for v in (u8, f32, bare):
+            v.close()

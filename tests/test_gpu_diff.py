@@ -94,8 +94,12 @@ def test_autograd_and_adam(ctx, setup):
 
 @pytest.mark.parametrize("k", [4, 5, 1, 64])
 def test_checkpoint_interval_does_not_change_gradients(ctx, setup, k):
-    """K = 4 and 8 keep a segment in registers, other K in local memory; the
-    per-ray sums are the same, only the order of atomics between rays differs."""
+    """The image does not depend on K; the gradients agree to 1e-4 relative:
+    the adjoint recomputes each sample position from its segment's
+    checkpoint in one rounding per axis, so positions (and the trilinear
+    weights at them) differ from the forward's running sum by a few ulps
+    that grow with the segment length, and the order of atomics between
+    rays differs."""
     torch = setup["torch"]
     vol = torch.from_numpy(setup["vi"]).cuda()
     tf = torch.from_numpy(np.clip(setup["tft"] * 0.8 + 0.1, 0, 1).astype(np.float32)).cuda()
@@ -110,4 +114,4 @@ def test_checkpoint_interval_does_not_change_gradients(ctx, setup, k):
         out.append((img.cpu().numpy(), dv.cpu().numpy(), dt.cpu().numpy()))
     assert np.array_equal(out[0][0], out[1][0])
     for a, b in ((out[0][1], out[1][1]), (out[0][2], out[1][2])):
-        assert np.linalg.norm(a - b) <= 1e-5 * np.linalg.norm(a), np.linalg.norm(a - b)
+        assert np.linalg.norm(a - b) <= 1e-4 * np.linalg.norm(a), np.linalg.norm(a - b)
