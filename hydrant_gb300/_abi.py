@@ -58,6 +58,7 @@ class HyShaderParams(C.Structure):
         ("composite", C.c_int32),
         ("srgb", C.c_int32),
         ("count_samples", C.c_int32),
+        ("early_termination", C.c_float),
     ]
 
 
@@ -167,6 +168,8 @@ _PROTOS = {
     "hy_batch_set_config": (C.c_int, [P, C.POINTER(HyBatchConfig)]),
     "hy_batch_get_config": (C.c_int, [P, C.POINTER(HyBatchConfig)]),
     "hy_batch_set_counting": (C.c_int, [P, C.c_int32]),
+    "hy_batch_update_views": (C.c_int, [P, P, C.c_int32]),
+    "hy_batch_view_bytes": (C.c_int, [P, C.POINTER(C.c_int64)]),
     "hy_batch_render_device": (C.c_int, [P, P]),
     "hy_batch_render": (C.c_int, [P, P]),
     "hy_batch_autotune": (C.c_int, [P, P, C.c_int32, C.POINTER(HyBatchConfig)]),

@@ -170,6 +170,7 @@ def shader_params(
     composite: bool = False,
     srgb: bool = False,
     count_samples: bool = False,
+    early_termination: float = 0.0,
 ) -> HyShaderParams:
     p = HyShaderParams()
     p.shader = SHADERS[shader] if isinstance(shader, str) else int(shader)
@@ -185,6 +186,7 @@ def shader_params(
     p.composite = int(bool(composite))
     p.srgb = int(bool(srgb))
     p.count_samples = int(bool(count_samples))
+    p.early_termination = early_termination
     return p
 
 
@@ -307,6 +309,27 @@ class Batch:
         nb = C.c_int64()
         ctx.check(lib().hy_batch_output_bytes(self.handle, C.byref(nb)))
         self.nbytes = int(nb.value)
+        ctx.check(lib().hy_batch_view_bytes(self.handle, C.byref(nb)))
+        self.view_bytes = int(nb.value)
+
+    def view_array(self, views, lighting=None):
+        """hy_batch_view array of (HyView, W, H) views at this batch's offsets."""
+        n = len(views)
+        arr = (HyBatchView * n)()
+        for i, (v, W, H) in enumerate(views):
+            arr[i].view = v
+            arr[i].width = W
+            arr[i].height = H
+            arr[i].rgba_offset = self.offsets[i]
+            if lighting is not None:
+                arr[i].eye_pos = (C.c_float * 3)(*lighting[i][0])
+                arr[i].light_pos = (C.c_float * 3)(*lighting[i][1])
+        return arr
+
+    def update_views(self, views, lighting=None) -> None:
+        """New cameras (same sizes) for the following renders."""
+        arr = views if isinstance(views, C.Array) else self.view_array(views, lighting)
+        self.ctx.check(lib().hy_batch_update_views(self.handle, arr, len(arr)))
 
     def close(self) -> None:
         if self.handle:

@@ -52,7 +52,7 @@ constexpr int kMaxBlockThreads = 256;
 #endif
 
 // Shades one pixel of a batch view and stores its RGBA8 value.
-template <int SHADER, int PC, int DT, bool PADDED, int COMPOSITE, bool LEAN, bool GATHER>
+template <int SHADER, int PC, int DT, bool PADDED, int COMPOSITE, bool LEAN, bool GATHER, bool ERT>
 __device__ __forceinline__ long long shade_batch_pixel(const BatchArgs &B, const Shared &S,
                                                        const BatchView &bv, int x, int y) {
     const ShadeArgs &A = B.A;
@@ -67,7 +67,7 @@ __device__ __forceinline__ long long shade_batch_pixel(const BatchArgs &B, const
                                                         aux);
     } else {
         Px p;
-        samples = emit<SHADER, PC, DT, PADDED, LEAN, GATHER>(p, A, bv.view, S, ox, oy, oz, dx, dy,
+        samples = emit<SHADER, PC, DT, PADDED, LEAN, GATHER, ERT>(p, A, bv.view, S, ox, oy, oz, dx, dy,
                                                              dz, 0.f, 0.f, 0.f, A.bbox_max[0],
                                                              A.bbox_max[1], A.bbox_max[2]);
         v = make_float4(p.vx, p.vy, p.vz, p.vw);
@@ -99,7 +99,8 @@ __device__ __forceinline__ int find_view(const int *starts, int n, int t) {
 // warps of an SM work on neighbouring rays and share L1 lines).
 // LEAN: Volume shader in Default mode without compositing (theta / phi are
 // not needed for an RGBA image; see VolumeMarch::step).
-template <int SHADER, int PC, int DT, bool PADDED, int COMPOSITE, bool LEAN, bool GATHER = false>
+template <int SHADER, int PC, int DT, bool PADDED, int COMPOSITE, bool LEAN, bool GATHER = false,
+          bool ERT = false>
 __device__ __forceinline__ void batch_body(const BatchArgs &B) {
     extern __shared__ float4 smem[];
     __shared__ unsigned int s_t0;
@@ -133,7 +134,7 @@ __device__ __forceinline__ void batch_body(const BatchArgs &B) {
                 const int x = (ux * B.bx + wx) * B.tile_w + lx;
                 const int y = (uy * B.by + wy) * B.tile_h + ly;
                 samples +=
-                    shade_batch_pixel<SHADER, PC, DT, PADDED, COMPOSITE, LEAN, GATHER>(B, S, bv, x, y);
+                    shade_batch_pixel<SHADER, PC, DT, PADDED, COMPOSITE, LEAN, GATHER, ERT>(B, S, bv, x, y);
             }
         }
     } else {
@@ -149,7 +150,7 @@ __device__ __forceinline__ void batch_body(const BatchArgs &B) {
                 const BatchView &bv = B.views[vi];
                 const int local = t - starts[vi];
                 const int ty = local / bv.tiles_x, tx = local - ty * bv.tiles_x;
-                samples += shade_batch_pixel<SHADER, PC, DT, PADDED, COMPOSITE, LEAN, GATHER>(
+                samples += shade_batch_pixel<SHADER, PC, DT, PADDED, COMPOSITE, LEAN, GATHER, ERT>(
                     B, S, bv, tx * B.tile_w + lx, ty * B.tile_h + ly);
             }
         }
@@ -186,10 +187,10 @@ template <int DT, bool PADDED, bool GATHER>
 constexpr int lean_regs() {
     return GATHER ? HY_BATCH_GATHER_REGS : (DT == HY_DTYPE_U8 && PADDED) ? HY_BATCH_LEAN_REGS : 64;
 }
-template <int SHADER, int PC, int DT, bool PADDED, bool GATHER>
+template <int SHADER, int PC, int DT, bool PADDED, bool GATHER, bool ERT>
 __global__ void __maxnreg__((lean_regs<DT, PADDED, GATHER>()))
     batch_lean_kernel(const __grid_constant__ BatchArgs B) {
-    batch_body<SHADER, PC, DT, PADDED, 0, true, GATHER>(B);
+    batch_body<SHADER, PC, DT, PADDED, 0, true, GATHER, ERT>(B);
 }
 
 template <int SHADER, int PC, int DT, bool PADDED>
@@ -198,12 +199,18 @@ const void *pick_c(const ShadeArgs &a) {
         return reinterpret_cast<const void *>(&batch_kernel<SHADER, PC, DT, PADDED, 1>);
     if constexpr (SHADER == HY_SHADER_VOLUME) {
         if (a.mode == HY_VOLUME_DEFAULT) {
+            const bool ert = a.ert > 0.f;
             if constexpr (DT == HY_DTYPE_U8 && PADDED) {
                 if (a.vol.tex)  // bricks in gather textures
-                    return reinterpret_cast<const void *>(
-                        &batch_lean_kernel<SHADER, PC, DT, PADDED, true>);
+                    return ert ? reinterpret_cast<const void *>(
+                                     &batch_lean_kernel<SHADER, PC, DT, PADDED, true, true>)
+                               : reinterpret_cast<const void *>(
+                                     &batch_lean_kernel<SHADER, PC, DT, PADDED, true, false>);
             }
-            return reinterpret_cast<const void *>(&batch_lean_kernel<SHADER, PC, DT, PADDED, false>);
+            return ert ? reinterpret_cast<const void *>(
+                             &batch_lean_kernel<SHADER, PC, DT, PADDED, false, true>)
+                       : reinterpret_cast<const void *>(
+                             &batch_lean_kernel<SHADER, PC, DT, PADDED, false, false>);
         }
     }
     return reinterpret_cast<const void *>(&batch_kernel<SHADER, PC, DT, PADDED, 0>);
@@ -261,6 +268,12 @@ struct hy_batch {
     cudaGraphExec_t exec = nullptr;
     uint8_t *graph_out = nullptr;
     int graph_count = -1;
+    // new cameras between renders (hy_batch_update_views): descriptors staged
+    // in pinned host memory, copied to views_dev on the stream; the event
+    // marks when the staging buffer may be rewritten
+    BatchView *views_pinned = nullptr;
+    cudaEvent_t upd_ev = nullptr;
+    bool upd_pending = false;
 };
 
 namespace {
@@ -296,6 +309,24 @@ void unit_shape(const hy_batch_config &c, int &bx, int &by) {
     by = c.block_warps / bx;
 }
 
+// One view's device descriptor: camera, lighting, size, output offset and
+// its place in the tile queue.
+void fill_view(BatchView &d, const hy_batch_view &v, int tiles_x, int tile0) {
+    std::memset(&d, 0, sizeof(d));
+    std::memcpy(d.view.trans, v.view.trans, sizeof(d.view.trans));
+    d.view.ctg = v.view.ctg_fovy_2;
+    for (int k = 0; k < 3; ++k) {
+        d.view.ray_o[k] = v.view.ray_o[k];
+        d.view.eye[k] = v.eye_pos[k];
+        d.view.light[k] = v.light_pos[k];
+    }
+    d.view.W = v.width;
+    d.view.H = v.height;
+    d.out_off = v.rgba_offset;
+    d.tiles_x = tiles_x;
+    d.tile0 = tile0;
+}
+
 // (Re)build the tile layout for the current config and the persistent grid.
 int layout(hy_batch *b) {
     hy_ctx *ctx = b->ctx;
@@ -309,19 +340,7 @@ int layout(hy_batch *b) {
     for (size_t i = 0; i < b->in.size(); ++i) {
         const hy_batch_view &v = b->in[i];
         BatchView &d = b->views[i];
-        std::memset(&d, 0, sizeof(d));
-        std::memcpy(d.view.trans, v.view.trans, sizeof(d.view.trans));
-        d.view.ctg = v.view.ctg_fovy_2;
-        for (int k = 0; k < 3; ++k) {
-            d.view.ray_o[k] = v.view.ray_o[k];
-            d.view.eye[k] = v.eye_pos[k];
-            d.view.light[k] = v.light_pos[k];
-        }
-        d.view.W = v.width;
-        d.view.H = v.height;
-        d.out_off = v.rgba_offset;
-        d.tiles_x = (v.width + tw - 1) / tw;
-        d.tile0 = int(tile);
+        fill_view(d, v, (v.width + tw - 1) / tw, int(tile));
         b->starts[i] = int(tile);
         tile += (long long)d.tiles_x * ((v.height + th - 1) / th);
     }
@@ -441,6 +460,9 @@ extern "C" int hy_batch_create(hy_ctx *ctx, const hy_volume *vol, const hy_shade
     cudaError_t e = cudaMalloc(&b->views_dev, sizeof(BatchView) * nviews);
     if (e == cudaSuccess) e = cudaMalloc(&b->starts_dev, sizeof(int) * nviews);
     if (e == cudaSuccess) e = cudaMalloc(&b->queue_dev, sizeof(unsigned int));
+    if (e == cudaSuccess)
+        e = cudaHostAlloc(&b->views_pinned, sizeof(BatchView) * nviews, cudaHostAllocDefault);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->upd_ev, cudaEventDisableTiming);
     if (e != cudaSuccess) {
         hy_batch_destroy(b);
         return hy_cuda_fail(ctx, e, "batch: allocation");
@@ -462,7 +484,45 @@ extern "C" int hy_batch_destroy(hy_batch *b) {
     if (b->views_dev) cudaFree(b->views_dev);
     if (b->starts_dev) cudaFree(b->starts_dev);
     if (b->queue_dev) cudaFree(b->queue_dev);
+    if (b->views_pinned) cudaFreeHost(b->views_pinned);
+    if (b->upd_ev) cudaEventDestroy(b->upd_ev);
     delete b;
+    return HY_OK;
+}
+
+// New cameras for the next renders: the views keep their sizes and output
+// offsets (so the tile queue, the launch and the captured graph stay), only
+// the ViewArgs and lighting change.  The descriptors go through a pinned
+// staging buffer and one copy on the context's stream, ordered before the
+// next render; the call returns without waiting for it (it waits only for
+// the previous update's copy before rewriting the staging buffer).
+extern "C" int hy_batch_update_views(hy_batch *b, const hy_batch_view *views, int32_t nviews) {
+    if (!b) return HY_ERR_INVALID;
+    hy_ctx *ctx = b->ctx;
+    if (!views || nviews != int32_t(b->in.size()))
+        return hy_fail(ctx, HY_ERR_INVALID, "batch: update needs the batch's number of views");
+    for (int i = 0; i < nviews; ++i)
+        if (views[i].width != b->in[i].width || views[i].height != b->in[i].height ||
+            views[i].rgba_offset != b->in[i].rgba_offset)
+            return hy_fail(ctx, HY_ERR_INVALID,
+                           "batch: an update keeps every view's size and output offset");
+    HY_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (b->upd_pending) HY_CUDA(ctx, cudaEventSynchronize(b->upd_ev));
+    for (int i = 0; i < nviews; ++i) {
+        b->in[i] = views[i];
+        fill_view(b->views[i], views[i], b->views[i].tiles_x, b->views[i].tile0);
+    }
+    std::memcpy(b->views_pinned, b->views.data(), sizeof(BatchView) * size_t(nviews));
+    HY_CUDA(ctx, cudaMemcpyAsync(b->views_dev, b->views_pinned, sizeof(BatchView) * size_t(nviews),
+                                 cudaMemcpyHostToDevice, ctx->stream));
+    HY_CUDA(ctx, cudaEventRecord(b->upd_ev, ctx->stream));
+    b->upd_pending = true;
+    return HY_OK;
+}
+
+extern "C" int hy_batch_view_bytes(const hy_batch *b, int64_t *bytes) {
+    if (!b || !bytes) return HY_ERR_INVALID;
+    *bytes = int64_t(sizeof(BatchView)) * int64_t(b->in.size());
     return HY_OK;
 }
 

@@ -84,6 +84,7 @@ struct ShadeArgs {
     int lowest_blkcnt;
     float to_world[16];
     int composite, srgb, count;
+    float ert;  // early ray termination opacity (lean Volume march; 0 = off)
     unsigned char clear_u8[4];
     ViewArgs view;
     const float4 *tf;

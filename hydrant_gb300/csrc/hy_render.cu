@@ -50,7 +50,8 @@ __device__ __forceinline__ uchar4 quantise(const ShadeArgs &A, float4 v) {
 
 // LEAN: Volume shader, Default mode, no compositing and no aux output
 // (theta / phi are not computed; see VolumeMarch::step).
-template <int SHADER, int PC, int DT, bool PADDED, int COMPOSITE, bool LEAN, bool GATHER = false>
+template <int SHADER, int PC, int DT, bool PADDED, int COMPOSITE, bool LEAN, bool GATHER = false,
+          bool ERT = false>
 __device__ __forceinline__ void render_body(const ShadeArgs &A) {
     extern __shared__ float4 smem[];
     float4 *tf = smem;
@@ -68,7 +69,7 @@ __device__ __forceinline__ void render_body(const ShadeArgs &A) {
             samples = composite_ray<SHADER, PC, DT, PADDED>(A, A.view, S, ox, oy, oz, dx, dy, dz, v, aux);
         } else {
             Px p;
-            samples = emit<SHADER, PC, DT, PADDED, LEAN, GATHER>(
+            samples = emit<SHADER, PC, DT, PADDED, LEAN, GATHER, ERT>(
                 p, A, A.view, S, ox, oy, oz, dx, dy, dz, 0.f, 0.f, 0.f, A.bbox_max[0],
                 A.bbox_max[1], A.bbox_max[2]);
             v = make_float4(p.vx, p.vy, p.vz, p.vw);
@@ -87,9 +88,9 @@ __device__ __forceinline__ void render_body(const ShadeArgs &A) {
     count_samples(A, samples);
 }
 
-template <int SHADER, int PC, int DT, bool PADDED, int COMPOSITE, bool LEAN, bool GATHER = false>
+template <int SHADER, int PC, int DT, bool PADDED, int COMPOSITE, bool LEAN, bool ERT = false>
 __global__ void __launch_bounds__(kThreads) render_kernel(const __grid_constant__ ShadeArgs A) {
-    render_body<SHADER, PC, DT, PADDED, COMPOSITE, LEAN, GATHER>(A);
+    render_body<SHADER, PC, DT, PADDED, COMPOSITE, LEAN, false, ERT>(A);
 }
 
 // The lean march sampling by texture gathers, held to HY_RENDER_GATHER_REGS
@@ -97,10 +98,10 @@ __global__ void __launch_bounds__(kThreads) render_kernel(const __grid_constant_
 #ifndef HY_RENDER_GATHER_REGS
 #define HY_RENDER_GATHER_REGS 56
 #endif
-template <int SHADER, int PC, int DT, bool PADDED>
+template <int SHADER, int PC, int DT, bool PADDED, bool ERT>
 __global__ void __maxnreg__(HY_RENDER_GATHER_REGS)
     render_gather_kernel(const __grid_constant__ ShadeArgs A) {
-    render_body<SHADER, PC, DT, PADDED, 0, true, true>(A);
+    render_body<SHADER, PC, DT, PADDED, 0, true, true, ERT>(A);
 }
 
 // The per-brick compositing variants of the Volume and Isosurface shaders,
@@ -272,14 +273,23 @@ void launch_fused(const ShadeArgs &a, cudaStream_t s) {
     }
     if constexpr (SHADER == HY_SHADER_VOLUME) {
         if (a.mode == HY_VOLUME_DEFAULT && !a.aux) {
+            const bool ert = a.ert > 0.f;
             if constexpr (DT == HY_DTYPE_U8 && PADDED) {
                 if (a.vol.tex) {  // bricks in gather textures
-                    render_gather_kernel<SHADER, PC, DT, PADDED>
-                        <<<grid_of(a), kThreads, smem_bytes(a), s>>>(a);
+                    if (ert)
+                        render_gather_kernel<SHADER, PC, DT, PADDED, true>
+                            <<<grid_of(a), kThreads, smem_bytes(a), s>>>(a);
+                    else
+                        render_gather_kernel<SHADER, PC, DT, PADDED, false>
+                            <<<grid_of(a), kThreads, smem_bytes(a), s>>>(a);
                     return;
                 }
             }
-            render_kernel<SHADER, PC, DT, PADDED, 0, true><<<grid_of(a), kThreads, smem_bytes(a), s>>>(a);
+            if (ert)
+                render_kernel<SHADER, PC, DT, PADDED, 0, true, true>
+                    <<<grid_of(a), kThreads, smem_bytes(a), s>>>(a);
+            else
+                render_kernel<SHADER, PC, DT, PADDED, 0, true><<<grid_of(a), kThreads, smem_bytes(a), s>>>(a);
             return;
         }
     }
@@ -388,6 +398,13 @@ int hy_fill_args(hy_ctx *ctx, const hy_volume *vol, const hy_shader_params *p, c
     a->composite = p->composite;
     a->srgb = p->srgb;
     a->count = p->count_samples;
+    // early ray termination: the lean march only (Volume, Default mode, one
+    // march through the volume box; films and compositing need full rays)
+    if (!(p->early_termination >= 0.f) || p->early_termination > 1.f)
+        return hy_fail(ctx, HY_ERR_INVALID, "render: early_termination must be 0 (off) or in (0, 1]");
+    a->ert = (p->shader == HY_SHADER_VOLUME && p->mode == HY_VOLUME_DEFAULT && !p->composite)
+                 ? p->early_termination
+                 : 0.f;
     if (view) {
         std::memcpy(a->view.trans, view->trans, sizeof(a->view.trans));
         a->view.ctg = view->ctg_fovy_2;

@@ -103,6 +103,13 @@ typedef struct hy_shader_params {
                                    isosurface.cc:272-290) */
     int32_t srgb;            /* Volume: linear_to_srgb before quantising (volume.cc:282-292) */
     int32_t count_samples;   /* 1: count trilinear brick samples into hy_render_stats */
+    float early_termination; /* Volume, Default mode, no compositing: 0 = off (the
+                                reference: every ray marches to its exit).  t in
+                                (0, 1]: a warp stops marching once v.a >= t on all
+                                of its rays (one vote per step).  What the skipped
+                                samples would add is at most 1 - t per channel:
+                                t = 1 - 2^-16 keeps images within 1 LSB and 1e-4
+                                of the full march. */
 } hy_shader_params;
 
 /* Film pixel layouts of the reference (shader.hpp:26-34, pixel_template.hpp:11-20,
@@ -433,6 +440,15 @@ int hy_batch_set_config(hy_batch *batch, const hy_batch_config *cfg);
 int hy_batch_get_config(const hy_batch *batch, hy_batch_config *out);
 /* 1: count brick samples of each launch into hy_render_stats. */
 int hy_batch_set_counting(hy_batch *batch, int32_t count_samples);
+/* New cameras for the following renders, as a frame loop supplies them (the
+ * reference builds ViewArgs from the camera for every frame,
+ * raycaster.hpp:126-135): `views` must keep the batch's number of views and
+ * each view's size and output offset; ViewArgs and lighting may change.  The
+ * captured graph is kept: the descriptors are copied to the device on the
+ * context's stream (hy_batch_view_bytes bytes), ordered before the next
+ * render.  Returns without waiting for the copy; `views` may be reused at once. */
+int hy_batch_update_views(hy_batch *batch, const hy_batch_view *views, int32_t nviews);
+int hy_batch_view_bytes(const hy_batch *batch, int64_t *bytes);
 /* Device output, asynchronous on the context's stream. */
 int hy_batch_render_device(hy_batch *batch, uint8_t *rgba_dev);
 /* Host output; returns when the images are on the host.  rgba_host must

@@ -45,6 +45,7 @@ typedef struct orc_params {
     int32_t composite;
     int32_t srgb;
     int32_t count_samples;
+    float early_termination;  /* ignored: every ray marches to its exit */
 } orc_params;
 
 /* Bricks a raw volume (x fastest) the way the dataset is defined for this

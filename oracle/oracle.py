@@ -39,6 +39,7 @@ class OrcParams(C.Structure):
         ("composite", C.c_int32),
         ("srgb", C.c_int32),
         ("count_samples", C.c_int32),
+        ("early_termination", C.c_float),  # ignored: the oracle marches every ray to its exit
     ]
 
 
@@ -100,7 +101,7 @@ MODES = {0: {"Default": 0, "Partition": 1, "Paging": 2}, 1: {"Volume": 0, "Solid
 def shader_params(shader="Volume", mode=0, sample_rate=1.0, max_steps=4000000, density=1.0,
                   isovalue=0.5, surface_color=(1.0, 1.0, 1.0), clear_color=(0.0, 0.0, 0.0),
                   rank=0.0, lowest_blkcnt=0, composite=False, srgb=False,
-                  count_samples=False) -> OrcParams:
+                  count_samples=False, early_termination=0.0) -> OrcParams:
     """Shader parameters by name, with the product's defaults (the CPU side
     of the measurement builds them without loading the product library;
     tests/test_oracle_synth.py holds the bytes equal)."""
@@ -118,6 +119,7 @@ def shader_params(shader="Volume", mode=0, sample_rate=1.0, max_steps=4000000, d
     p.composite = int(bool(composite))
     p.srgb = int(bool(srgb))
     p.count_samples = int(bool(count_samples))
+    p.early_termination = early_termination
     return p
 
 

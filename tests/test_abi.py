@@ -35,7 +35,7 @@ def test_struct_sizes_match_reference_layouts(built_lib):
 
     # film pixel layouts of the reference (shader.hpp:26-34 etc.)
     assert C.sizeof(_abi.HyView) == 80
-    assert C.sizeof(_abi.HyShaderParams) == 4 * (2 + 4 + 3 + 3 + 2 + 16 + 3 + 3 + 3)
+    assert C.sizeof(_abi.HyShaderParams) == 4 * (2 + 4 + 3 + 3 + 2 + 16 + 3 + 3 + 3 + 1)
 
 
 def test_ctx_create_without_gpu_fails_cleanly(built_lib):

@@ -193,3 +193,35 @@ def test_batch_renders_into_pinned_host_memory(ctx, tubes):
         assert pageable.any()
     finally:
         b.close()
+
+
+def test_batch_takes_new_cameras_without_a_new_batch(ctx, tubes):
+    """hy_batch_update_views: new ViewArgs and lighting for the same sizes are
+    rendered by the same batch (its captured graph replayed), equal to the
+    per-view path for the new cameras; an update that changes a size is
+    refused."""
+    torch = pytest.importorskip("torch")
+    sizes = SIZES[:5]
+    kw = dict(shader="Isosurface", mode="Color", isovalue=0.5)
+    views_a, cams_a = _views(tubes, sizes, seed=3)
+    views_b, cams_b = _views(tubes, sizes, seed=4)
+    p = hy.shader_params(**kw)
+    hy.iso_lighting(tubes, cams_a[0], p)
+    b = hy.Batch(ctx, tubes, p, views_a, _lighting(tubes, cams_a, kw))
+    try:
+        out = torch.empty(b.nbytes, dtype=torch.uint8, device="cuda")
+        for views, cams in ((views_b, cams_b), (views_a, cams_a), (views_b, cams_b)):
+            ref, _ = _per_view(ctx, tubes, kw, views, cams)
+            b.update_views(views, _lighting(tubes, cams, kw))
+            out.zero_()
+            b.render_device(out.data_ptr())
+            ctx.synchronize()
+            for g, r in zip(b.split(out.cpu().numpy()), ref):
+                assert np.array_equal(g, r)
+        bad = b.view_array(views_a)
+        bad[1].width = bad[1].width + 1
+        with pytest.raises(hy.HydrantError):
+            b.update_views(bad)
+        assert b.view_bytes > 0
+    finally:
+        b.close()
