@@ -484,7 +484,8 @@ def ert_leg(hy, ctx, dev, reps=5):
     import numpy as np
     import torch
 
-    wl = workloads_module()
+    from hydrant_gb300 import workloads as wl
+
     w = wl.tubes_c1()
     vol = hy.Volume(ctx, hy.synth_tubes_u8(w.seed, w.dim, w.count), w.block_size, w.padding)
     try:
@@ -752,7 +753,11 @@ def main_ours(args):
     t_e2e = time.perf_counter() - te
     if ws > 1:
         (t_e2e,) = max_over_ranks([t_e2e], dev)
+    # back to the step's own cameras: `out` holds their images for the
+    # parity check against the oracle
     batch.update_views(batch.view_array(views))
+    batch.render_device(out.data_ptr())
+    ctx.synchronize()
 
     # ---- the configuration's compositing variant and the differentiable
     # configuration, each at its stated size (rank 0 of a 1-GPU run) -------
@@ -1050,6 +1055,8 @@ def diff_leg(hy, ctx, dev, reps=5, fd_params=4, ckpt_k=None):
         checks.append(("knot direction", -1, float((dtf * d).sum()), fd))
     torch.cuda.synchronize()
     rel = [abs(a - f) / max(abs(f), 1e-30) for _, _, a, f in checks]
+    l2 = math.sqrt(sum((a - f) ** 2 for _, _, a, f in checks) /
+                   max(sum(f ** 2 for _, _, _, f in checks), 1e-300))
     out.update({
         "config": {"workload": f"diff_{n}cube_{nv}x{res}px_{ntf}knots_K{K}", "volume": [n, n, n],
                    "dtype": "f32", "views": nv, "resolution": res, "knots": ntf, "ckpt_k": K},
@@ -1060,7 +1067,7 @@ def diff_leg(hy, ctx, dev, reps=5, fd_params=4, ckpt_k=None):
         "fwd_adjoint_over_forward": (fwd_k + bwd) / fwd,
         "fwd_adjoint_over_forward_ckpt": (fwd_k + bwd) / fwd_k,
         "fd_check": {"eps": eps, "loss": "mean squared image error (float64)",
-                     "max_rel_err": max(rel),
+                     "max_rel_err": max(rel), "l2_rel_err": l2,
                      "cases": [{"param": k, "index": i, "adjoint": a, "fd": f,
                                 "rel_err": e} for (k, i, a, f), e in zip(checks, rel)]},
         "timing": "CUDA events on the library stream, mean of %d launches after 2 warm-up" % reps,

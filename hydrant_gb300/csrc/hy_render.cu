@@ -93,16 +93,6 @@ __global__ void __launch_bounds__(kThreads) render_kernel(const __grid_constant_
     render_body<SHADER, PC, DT, PADDED, COMPOSITE, LEAN, false, ERT>(A);
 }
 
-// The lean march sampling by texture gathers, held to HY_RENDER_GATHER_REGS
-// registers (the gathers' latency wants resident warps).
-#ifndef HY_RENDER_GATHER_REGS
-#define HY_RENDER_GATHER_REGS 56
-#endif
-template <int SHADER, int PC, int DT, bool PADDED, bool ERT>
-__global__ void __maxnreg__(HY_RENDER_GATHER_REGS)
-    render_gather_kernel(const __grid_constant__ ShadeArgs A) {
-    render_body<SHADER, PC, DT, PADDED, 0, true, true, ERT>(A);
-}
 
 // The per-brick compositing variants of the Volume and Isosurface shaders,
 // held to 64 registers (8 resident blocks): on the 512^3 tubes at 1024^2,
@@ -273,18 +263,9 @@ void launch_fused(const ShadeArgs &a, cudaStream_t s) {
     }
     if constexpr (SHADER == HY_SHADER_VOLUME) {
         if (a.mode == HY_VOLUME_DEFAULT && !a.aux) {
+            // (the per-view kernel samples by loads: with gathers it measured
+            // slower, 177.0 vs 186.5 Gsamples/s on the 64-view step)
             const bool ert = a.ert > 0.f;
-            if constexpr (DT == HY_DTYPE_U8 && PADDED) {
-                if (a.vol.tex) {  // bricks in gather textures
-                    if (ert)
-                        render_gather_kernel<SHADER, PC, DT, PADDED, true>
-                            <<<grid_of(a), kThreads, smem_bytes(a), s>>>(a);
-                    else
-                        render_gather_kernel<SHADER, PC, DT, PADDED, false>
-                            <<<grid_of(a), kThreads, smem_bytes(a), s>>>(a);
-                    return;
-                }
-            }
             if (ert)
                 render_kernel<SHADER, PC, DT, PADDED, 0, true, true>
                     <<<grid_of(a), kThreads, smem_bytes(a), s>>>(a);
