@@ -73,6 +73,10 @@ def parse_args():
                     help="paging, lossless: bricks per batch (the reference caps it at 4096)")
     ap.add_argument("--cache-gib", type=float, default=8.0,
                     help="paging workload: device brick cache of the realtime pager")
+    ap.add_argument("--no-tune-cache", action="store_true",
+                    help="paging: a cache of the whole --cache-gib (no sizing to the orbit)")
+    ap.add_argument("--eviction", choices=["lru", "reference"], default="lru",
+                    help="paging, realtime: least recently visible, or the reference's order")
     ap.add_argument("--max-uploads", type=int, default=0,
                     help="paging: brick uploads per frame (0 = every missing brick)")
     ap.add_argument("--launch-shape", default="",
@@ -192,7 +196,8 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def profile_per_sample(block_queue: int, what: str = "dram_bytes_per_sample"):
+def profile_per_sample(block_queue: int, what: str = "dram_bytes_per_sample",
+                       sampler: str = "gather"):
     """A per-sample figure of the batch kernel (DRAM bytes, warp instructions)
     from the committed ncu summary (one capture of 4 views of the same volume;
     both grow with the samples processed, so they scale to a full launch by
@@ -200,7 +205,7 @@ def profile_per_sample(block_queue: int, what: str = "dram_bytes_per_sample"):
     p = ROOT / "profiles" / "batch_kernel_multiview.txt"
     if not p.exists():
         return None
-    tag = f"{what}[block_queue={block_queue}]:"
+    tag = f"{what}[sampler={sampler},block_queue={block_queue}]:"
     for line in p.read_text().splitlines():
         if line.startswith(tag):
             try:
@@ -781,9 +786,10 @@ def main_ours(args):
     overridden = (args.shader or args.mode or args.composite or args.sample_rate > 0
                   or args.density is not None)
     if args.workload == "multiview" and not overridden:
-        tps = profile_per_sample(int(tuned.get("block_queue", 1)))
+        smp = "gather" if vol.gather_sampling else "loads"
+        tps = profile_per_sample(int(tuned.get("block_queue", 1)), sampler=smp)
         ipsm = profile_per_sample(int(tuned.get("block_queue", 1)),
-                                  "warp_instructions_per_sample")
+                                  "warp_instructions_per_sample", sampler=smp)
     if rank == 0:
         from oracle import oracle as orc
 
@@ -903,8 +909,17 @@ def main_paging(args):
         slots = args.lossless_batch
         pg = hy.Pager(ctx, store, slots, _abi.PAGER_LOSSLESS)
     else:
-        slots = int((args.cache_gib * 2**30) // si.slot_bytes)
-        pg = hy.Pager(ctx, store, slots, _abi.PAGER_REALTIME, args.max_uploads)
+        budget = int(args.cache_gib * 2**30)
+        frames_ = max(1, args.frames)
+        path = [hy.camera_orbit((3.0 * f, 30.0, 2.2)) for f in range(frames_)]
+        if args.no_tune_cache:
+            slots, most = int(budget // si.slot_bytes), None
+        else:
+            # the cache sized to the orbit (the most visible bricks + 10 %),
+            # within the --cache-gib budget
+            slots, most = hy.Pager.tune_slots(ctx, store, path, budget)
+        ev = _abi.EVICT_REFERENCE if args.eviction == "reference" else _abi.EVICT_LRU
+        pg = hy.Pager(ctx, store, slots, _abi.PAGER_REALTIME, args.max_uploads, ev)
     p = hy.shader_params(shader="Volume", sample_rate=0.25, density=5e-3)
     pc = hy.shader_params(shader="Volume", sample_rate=0.25, density=5e-3, count_samples=True)
     out = torch.empty(res * res * 4, dtype=torch.uint8, device=f"cuda:{local}")
@@ -952,6 +967,11 @@ def main_paging(args):
                    "pager": args.pager,
                    "cache_gib": args.cache_gib if args.pager == "realtime" else None,
                    "cache_slots": slots, "store_bricks": si.nonempty,
+                   "cache_tuned": None if args.pager != "realtime" or args.no_tune_cache else {
+                       "slots": slots, "gib": slots * si.slot_bytes / 2**30,
+                       "most_visible_bricks": most, "budget_gib": args.cache_gib,
+                       "rule": "most visible bricks over the orbit + 10 %, within the budget"},
+                   "eviction": args.eviction if args.pager == "realtime" else None,
                    "store_gb": si.pool_bytes / 1e9, "store_build_s": t_store,
                    "coarse_level": args.coarse_level, "coarse_build_s": t_coarse,
                    "max_uploads_per_frame": args.max_uploads},

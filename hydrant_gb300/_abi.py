@@ -101,10 +101,13 @@ class HyBatchConfig(C.Structure):
 
 
 PAGER_LOSSLESS, PAGER_REALTIME = 0, 1
+EVICT_LRU = 0
+EVICT_REFERENCE = 1
 
 
 class HyPagerDesc(C.Structure):
-    _fields_ = [("slots", C.c_int32), ("mode", C.c_int32), ("max_uploads_per_frame", C.c_int32)]
+    _fields_ = [("slots", C.c_int32), ("mode", C.c_int32), ("max_uploads_per_frame", C.c_int32),
+                ("eviction", C.c_int32)]
 
 
 class HyPagerStats(C.Structure):
@@ -192,6 +195,8 @@ _PROTOS = {
     "hy_store_ingest_raw": (C.c_int, [P, C.c_char_p, C.POINTER(HyVolumeDesc), C.POINTER(P)]),
     "hy_cull": (C.c_int, [P, C.POINTER(HyView), P, C.c_int32, P, P, C.POINTER(C.c_int32)]),
     "hy_pager_create": (C.c_int, [P, P, C.POINTER(HyPagerDesc), C.POINTER(P)]),
+    "hy_pager_tune_slots": (C.c_int, [P, P, P, C.c_int32, C.c_int64, C.POINTER(C.c_int32),
+                                     C.POINTER(C.c_int32)]),
     "hy_pager_destroy": (C.c_int, [P]),
     "hy_pager_volume": (C.c_int, [P, C.POINTER(P)]),
     "hy_pager_stats_get": (C.c_int, [P, C.POINTER(HyPagerStats)]),

@@ -478,10 +478,19 @@ class _PagedVolume:
 class Pager:
     """Brick cache kept filled from a Store (hy_pager)."""
 
+    @staticmethod
+    def tune_slots(ctx: Context, store: "Store", cams, budget_bytes: int):
+        """hy_pager_tune_slots: (slots, most visible bricks) for a camera path."""
+        arr = (HyCamera * len(cams))(*cams)
+        slots, most = C.c_int32(), C.c_int32()
+        ctx.check(lib().hy_pager_tune_slots(ctx.handle, store.handle, arr, len(cams),
+                                            int(budget_bytes), C.byref(slots), C.byref(most)))
+        return int(slots.value), int(most.value)
+
     def __init__(self, ctx: Context, store: Store, slots: int, mode: int = _abi.PAGER_REALTIME,
-                 max_uploads_per_frame: int = 0):
+                 max_uploads_per_frame: int = 0, eviction: int = _abi.EVICT_LRU):
         self.ctx = ctx
-        d = _abi.HyPagerDesc(slots, mode, max_uploads_per_frame)
+        d = _abi.HyPagerDesc(slots, mode, max_uploads_per_frame, eviction)
         h = C.c_void_p()
         ctx.check(lib().hy_pager_create(ctx.handle, store.handle, C.byref(d), C.byref(h)))
         self.handle = h

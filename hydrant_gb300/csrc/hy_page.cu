@@ -739,6 +739,8 @@ struct hy_pager {
     int ncoarse = 0;
     int reg_base = 0;
     int next_free = 0;           // realtime: slots never used yet
+    // realtime, LRU: per slot the last frame its brick was visible
+    std::vector<int64_t> stamp;
     int2 *info_stage[2] = {nullptr, nullptr};  // pinned staging of the page table
     // realtime frames overlap: a frame culls on its own stream, from a copy
     // of the chebyshev values, while the previous frame still renders
@@ -829,6 +831,8 @@ extern "C" int hy_pager_create(hy_ctx *ctx, hy_store *store, const hy_pager_desc
     if (desc->slots <= 0) return hy_fail(ctx, HY_ERR_INVALID, "pager: slots must be > 0");
     if (desc->mode != HY_PAGER_LOSSLESS && desc->mode != HY_PAGER_REALTIME)
         return hy_fail(ctx, HY_ERR_INVALID, "pager: unknown mode");
+    if (desc->eviction != HY_EVICT_LRU && desc->eviction != HY_EVICT_REFERENCE)
+        return hy_fail(ctx, HY_ERR_INVALID, "pager: unknown eviction policy");
     HY_CUDA(ctx, cudaSetDevice(ctx->device));
     hy_pager *pg = new hy_pager();
     pg->ctx = ctx;
@@ -916,6 +920,7 @@ extern "C" int hy_pager_create(hy_ctx *ctx, hy_store *store, const hy_pager_desc
     if (e != cudaSuccess) return fail(hy_cuda_fail(ctx, e, "pager: registry upload"));
     pg->page.assign(v->nbricks, -1);
     pg->owner.assign(pg->nslots, -1);
+    pg->stamp.assign(pg->nslots, -1);
     rc = upload_page_table(pg);
     if (rc) return fail(rc);
     v->uploaded = true;
@@ -961,6 +966,52 @@ extern "C" int hy_pager_destroy(hy_pager *pg) {
         delete v;
     }
     delete pg;
+    return HY_OK;
+}
+
+// Cache size for a camera path: the most bricks any of the cameras sees
+// (the GPU cull over the store's chebyshev thumbnail), with 10 % headroom
+// for the bricks the next frames bring into view, within the byte budget
+// and never more than the store holds.  The reference sizes its cache from
+// a fixed mem_limit_mb alone (rt_block_paging.cc:230-236).
+extern "C" int hy_pager_tune_slots(hy_ctx *ctx, const hy_store *store, const hy_camera *cams,
+                                   int32_t ncams, int64_t budget_bytes, int32_t *slots_out,
+                                   int32_t *visible_max_out) {
+    if (!ctx || !store || !cams || ncams <= 0 || !slots_out) return HY_ERR_INVALID;
+    if (store->ctx != ctx) return hy_fail(ctx, HY_ERR_INVALID, "tune: store of another context");
+    if (budget_bytes < (int64_t)store->slot_stride)
+        return hy_fail(ctx, HY_ERR_INVALID, "tune: the budget holds no brick");
+    HY_CUDA(ctx, cudaSetDevice(ctx->device));
+    hy_volume v;
+    int rc = hy_volume_init(ctx, &store->desc, &v);
+    if (rc) return rc;
+    int *cheb_dev = nullptr;
+    HY_CUDA(ctx, cudaMalloc(&cheb_dev, size_t(v.nbricks) * sizeof(int)));
+    CullScratch cs;
+    size_t most = 0;
+    cudaError_t e = cudaMemcpyAsync(cheb_dev, store->cheb.data(), size_t(v.nbricks) * sizeof(int),
+                                    cudaMemcpyHostToDevice, ctx->stream);
+    if (e != cudaSuccess) rc = hy_cuda_fail(ctx, e, "tune: chebyshev upload");
+    for (int i = 0; i < ncams && rc == HY_OK; ++i) {
+        hy_view view;
+        rc = hy_camera_view(&v, &cams[i], &view);
+        std::vector<int> ids;
+        std::vector<float> d2;
+        if (rc == HY_OK)
+            rc = run_cull(ctx, &v, view, nullptr, -1, cs, ids, d2, nullptr, ctx->stream, cheb_dev);
+        most = std::max(most, ids.size());
+    }
+    if (cs.ids) cudaFree(cs.ids);
+    if (cs.d2) cudaFree(cs.d2);
+    if (cs.count) cudaFree(cs.count);
+    cudaFree(cheb_dev);
+    if (rc) return rc;
+    const long long budget = budget_bytes / (long long)store->slot_stride;
+    long long want = (long long)(most + (most + 9) / 10);
+    want = std::min(want, (long long)store->nonempty);
+    want = std::min(want, budget);
+    *slots_out = int32_t(std::max(want, 1ll));
+    if (visible_max_out) *visible_max_out = int32_t(most);
     return HY_OK;
 }
 
@@ -1083,7 +1134,15 @@ int render_lossless(hy_pager *pg, const hy_shader_params *p, const hy_camera *ca
 // arrival handler (rt_block_paging.cc:246-291): the nearest `slots` visible
 // bricks are required; missing ones (nearest first, at most
 // max_uploads_per_frame) go to never-used slots, then to slots of bricks that
-// are no longer required (the highest brick index first); then one frame.
+// are no longer required, chosen by the eviction policy:
+//  HY_EVICT_LRU        the least recently visible brick first (a slot's
+//                      stamp is the last frame its brick was visible; ties by
+//                      brick index), so a brick seen a few frames ago
+//                      survives bricks that left the view long before;
+//  HY_EVICT_REFERENCE  the highest brick index first (the reference's
+//                      redundant set, an ordered std::set popped from the end).
+// The whole frame's plan is checked before any page-table entry changes, so
+// a refused move leaves the cache as it was; then one frame.
 int render_realtime(hy_pager *pg, const hy_shader_params *p, const hy_view &view, int W, int H,
                     uint8_t *rgba_dev) {
     hy_ctx *ctx = pg->ctx;
@@ -1093,39 +1152,65 @@ int render_realtime(hy_pager *pg, const hy_shader_params *p, const hy_view &view
     int rc = run_cull(ctx, v, view, nullptr, pg->nslots, pg->cs, req, d2, &visible,
                       pg->cull_stream, pg->cheb_dev);
     if (rc) return rc;
+    const int64_t frame = pg->stats.frames;
     std::vector<char> required(v->nbricks, 0);
     for (int b : req) required[b] = 1;
+    // visible resident bricks are used this frame
+    for (int b : visible)
+        if (pg->page[b] >= 0) pg->stamp[pg->page[b]] = frame;
     std::vector<std::pair<float, int>> missing;
+    int64_t hits = 0;
     for (size_t i = 0; i < req.size(); ++i)
         if (pg->page[req[i]] < 0) missing.push_back({d2[i], req[i]});
-        else ++pg->stats.hits;
+        else ++hits;
     std::sort(missing.begin(), missing.end());
-    std::vector<int> redundant;  // ascending brick index
-    for (int s = 0; s < pg->nslots; ++s)
-        if (pg->owner[s] >= 0 && !required[pg->owner[s]]) redundant.push_back(pg->owner[s]);
-    std::sort(redundant.begin(), redundant.end());
-    pg->stats.misses += int64_t(missing.size());
+    // eviction candidates, the next victim at the back
+    std::vector<std::pair<int64_t, int>> victims;  // (key, slot)
+    for (int s = 0; s < pg->nslots; ++s) {
+        const int b = pg->owner[s];
+        if (b < 0 || required[b]) continue;
+        if (pg->desc.eviction == HY_EVICT_REFERENCE)
+            victims.push_back({int64_t(b), s});  // highest brick index last
+        else
+            victims.push_back({-(pg->stamp[s] * int64_t(v->nbricks) + b), s});  // oldest last
+    }
+    std::sort(victims.begin(), victims.end());
     const int budget = pg->desc.max_uploads_per_frame > 0 ? pg->desc.max_uploads_per_frame
                                                            : int(missing.size());
-    std::vector<int> move_b, move_s;
+    std::vector<int> move_b, move_s, evicted;
+    int next_free = pg->next_free;
     for (int i = 0; i < int(missing.size()) && int(move_b.size()) < budget; ++i) {
         const int b = missing[i].second;
         int slot;
-        if (pg->next_free < pg->nslots) {
-            slot = pg->next_free++;
-        } else if (!redundant.empty()) {
-            const int old = redundant.back();
-            redundant.pop_back();
-            slot = pg->page[old];
-            pg->page[old] = -1;
-            ++pg->stats.evictions;
+        if (next_free < pg->nslots) {
+            slot = next_free++;
+        } else if (!victims.empty()) {
+            slot = victims.back().second;
+            victims.pop_back();
+            evicted.push_back(pg->owner[slot]);
         } else {
             break;  // no slot: the brick stays absent this frame
         }
-        pg->owner[slot] = b;
-        pg->page[b] = slot;
         move_b.push_back(b);
         move_s.push_back(slot);
+    }
+    for (size_t i = 0; i < move_b.size(); ++i) {
+        const long long off = pg->store->offset[move_b[i]];
+        if (off < 0 || off + (long long)v->slot_stride > (long long)pg->store->host_bytes)
+            return hy_fail(ctx, HY_ERR_STATE, "pager: a planned brick is not in the store");
+    }
+    // commit the plan
+    pg->stats.hits += hits;
+    pg->stats.misses += int64_t(missing.size());
+    pg->next_free = next_free;
+    for (int old : evicted) {
+        pg->page[old] = -1;
+        ++pg->stats.evictions;
+    }
+    for (size_t i = 0; i < move_b.size(); ++i) {
+        pg->owner[move_s[i]] = move_b[i];
+        pg->page[move_b[i]] = move_s[i];
+        pg->stamp[move_s[i]] = frame;
     }
     // one gather kernel on the render stream moves every brick of the frame:
     // it runs after the previous frame's render, so reused slots are free

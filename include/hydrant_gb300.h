@@ -278,11 +278,19 @@ typedef struct hy_store hy_store;
 typedef struct hy_pager hy_pager;
 
 enum { HY_PAGER_LOSSLESS = 0, HY_PAGER_REALTIME = 1 };
+/* Realtime eviction: which slot a missing brick takes once no slot is free
+ * (only slots of bricks the frame does not require are candidates).
+ * LRU: the brick visible least recently (a brick counts as used in every
+ * frame in which the cull finds it visible); REFERENCE: the highest brick
+ * index, as RtBlockPagingServer pops its redundant set (rt_block_paging.cc:
+ * 256-265, 299-326). */
+enum { HY_EVICT_LRU = 0, HY_EVICT_REFERENCE = 1 };
 
 typedef struct hy_pager_desc {
     int32_t slots;                 /* bricks per batch (lossless) / cache size (realtime) */
     int32_t mode;                  /* HY_PAGER_* */
     int32_t max_uploads_per_frame; /* realtime: 0 = every missing brick */
+    int32_t eviction;              /* realtime: HY_EVICT_* */
 } hy_pager_desc;
 
 typedef struct hy_pager_stats {
@@ -344,6 +352,14 @@ int hy_cull(const hy_volume *vol, const hy_view *view, const float rect[4], int3
  * coarse level must be built before the pager is created. */
 int hy_pager_create(hy_ctx *ctx, hy_store *store, const hy_pager_desc *desc, hy_pager **out);
 int hy_pager_destroy(hy_pager *pager);
+/* Realtime cache size for a camera path: slots for the most visible bricks
+ * any of `cams` sees plus 10 % (new bricks come into view between frames),
+ * at most budget_bytes / slot bytes and the store's non-empty bricks; the
+ * most visible bricks are returned too.  The reference derives its cache
+ * from mem_limit_mb alone (rt_block_paging.cc:230-236); this sizes it to
+ * the path, within the same kind of limit. */
+int hy_pager_tune_slots(hy_ctx *ctx, const hy_store *store, const hy_camera *cams, int32_t ncams,
+                        int64_t budget_bytes, int32_t *slots, int32_t *visible_max);
 /* The paged volume (for hy_cull / hy_render); owned by the pager. */
 int hy_pager_volume(hy_pager *pager, hy_volume **out);
 int hy_pager_stats_get(const hy_pager *pager, hy_pager_stats *out);
@@ -361,7 +377,8 @@ int hy_pager_present(const hy_pager *pager, uint8_t *mask);
  *  REALTIME: RtBlockPagingServer::update (rt_block_paging.cc:296-326): the
  *    nearest `slots` visible bricks are required; missing ones, nearest first,
  *    go to never-used slots and then to slots of bricks no longer required
- *    (highest index first); one emit pass renders with what is resident.
+ *    (desc.eviction: least recently visible, or highest index first as in the
+ *    reference); one emit pass renders with what is resident.
  *    With a coarse level in the store (created before the pager), the coarse
  *    bricks stay resident and registry ids 0..nbricks-1 sample them, brick b
  *    through its sub-box of the coarse brick (k = bs/P/s, b = pad/P + d*k,

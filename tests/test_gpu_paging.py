@@ -128,13 +128,19 @@ def test_lossless_pager_matches_oracle(ctx, tubes, shader, slots):
         pg.close()
 
 
+@pytest.mark.parametrize("policy", ["reference", "lru"])
 @pytest.mark.parametrize("budget", [0, 9])
-def test_realtime_pager_follows_reference_policy(ctx, tubes, budget):
+def test_realtime_pager_follows_its_policy(ctx, tubes, budget, policy):
+    """A host replay of the replacement policy with the oracle's cull gives
+    the pager's resident set frame by frame: the reference's redundant-set
+    swap (highest brick index evicted first) or LRU (the brick visible least
+    recently, ties by index); each frame equals the oracle given that set."""
     torch = pytest.importorskip("torch")
     vol, ov, store = tubes
     slots = 40
-    pg = hy.Pager(ctx, store, slots, _abi.PAGER_REALTIME, budget)
-    page, owner, next_free = {}, {}, 0
+    ev = _abi.EVICT_REFERENCE if policy == "reference" else _abi.EVICT_LRU
+    pg = hy.Pager(ctx, store, slots, _abi.PAGER_REALTIME, budget, ev)
+    page, owner, next_free, stamp = {}, {}, 0, {}
     try:
         W, H = 64, 48
         for f in range(6):
@@ -147,8 +153,15 @@ def test_realtime_pager_follows_reference_policy(ctx, tubes, budget):
             view = view_array(hy.camera_view(vol, c))
             ids, d2 = orc.cull(ov, view, slots)
             req = set(ids.tolist())
+            for b in orc.cull(ov, view, -1)[0].tolist():  # visible resident: used now
+                if b in page:
+                    stamp[b] = f
             missing = sorted((float(d), int(b)) for b, d in zip(ids, d2) if int(b) not in page)
-            redundant = sorted(b for b in page if b not in req)
+            if policy == "reference":
+                redundant = sorted(b for b in page if b not in req)
+            else:  # least recently visible at the end, ties: lowest index at the end
+                redundant = sorted((b for b in page if b not in req),
+                                   key=lambda b: (-stamp[b], -b))
             n = 0
             for _, b in missing:
                 if budget and n >= budget:
@@ -163,6 +176,7 @@ def test_realtime_pager_follows_reference_policy(ctx, tubes, budget):
                     break
                 page[b] = slot
                 owner[slot] = b
+                stamp[b] = f
                 n += 1
             mask = orc.present_mask(ov, list(page))
             assert np.array_equal(pg.present(), mask), f"frame {f}: resident sets differ"
@@ -388,5 +402,86 @@ def test_realtime_pager_on_f32_store_matches_oracle(ctx):
     finally:
         ov.set_present(np.ones(nb, np.uint8))
         pg.close()
+        store.close()
+        vol.close()
+
+
+def _three_clusters():
+    """64^3 u8 volume in 8^3 bricks (apron 1): three clusters of 2x2x2
+    non-empty bricks, A at bricks (0..1, 6..7, 6..7) (the highest brick
+    indices), B at (0..1, 0..1, 0..1), C at (6..7, 0..1, 6..7); the values
+    stay two voxels inside each cluster, so no neighbouring brick's apron
+    sees them.  Returns the voxels and, per cluster, a camera (fovy 10) that
+    sees that cluster alone."""
+    n, bs = 64, 8
+    vox = np.zeros((n, n, n), np.uint8)
+    cams = {}
+    for name, (cx, cy, cz) in {"A": (0, 6, 6), "B": (0, 0, 0), "C": (6, 0, 6)}.items():
+        x0, y0, z0 = cx * bs, cy * bs, cz * bs
+        vox[z0 + 2:z0 + 14, y0 + 2:y0 + 14, x0 + 2:x0 + 14] = 200
+        c = (np.array([cx + 1, cy + 1, cz + 1]) / 8.0 - 0.5)
+        cams[name] = (tuple(4.0 * c), tuple(c))
+    return vox, cams
+
+
+@pytest.mark.parametrize("policy", ["lru", "reference"])
+def test_lru_keeps_a_revisited_brick(ctx, policy):
+    """Frames see A, B, A, C, A with room for two clusters.  At C the cache
+    must evict: LRU drops B (last seen two frames earlier), so the return to
+    A hits every brick; the reference's policy drops A (the highest brick
+    indices), so the return to A misses all eight."""
+    torch = pytest.importorskip("torch")
+    vox, cams = _three_clusters()
+    vol = hy.Volume(ctx, vox, 8, 1)
+    store = hy.Store.from_volume(vol)
+    ov = orc.OracleVolume(vox, 8, 1)
+    ev = _abi.EVICT_LRU if policy == "lru" else _abi.EVICT_REFERENCE
+    pg = hy.Pager(ctx, store, 16, _abi.PAGER_REALTIME, 0, ev)
+    try:
+        ctx.set_transfer_fn(wl.TF9)
+        p = hy.shader_params(shader="Volume", density=0.5, sample_rate=0.5)
+        out = torch.zeros(32 * 32 * 4, dtype=torch.uint8, device="cuda")
+        sets = {}
+        for name, (pos, tgt) in cams.items():
+            cam = hy.camera_ptu(pos, tgt, (0.0, 1.0, 0.0), 10.0)
+            sets[name] = set(orc.cull(ov, view_array(hy.camera_view(vol, cam)), -1)[0].tolist())
+            assert len(sets[name]) == 8, name
+        misses = []
+        for name in "ABACA":
+            pos, tgt = cams[name]
+            before = pg.stats()["misses"]
+            pg.render(p, hy.camera_ptu(pos, tgt, (0.0, 1.0, 0.0), 10.0), 32, 32, out.data_ptr())
+            ctx.synchronize()
+            misses.append(pg.stats()["misses"] - before)
+            if len(misses) == 4:  # after C
+                present = set(np.nonzero(pg.present())[0].tolist())
+                kept = "A" if policy == "lru" else "B"
+                assert present == sets[kept] | sets["C"], policy
+        assert misses[:4] == [8, 8, 0, 8]
+        assert misses[4] == (0 if policy == "lru" else 8)
+        assert pg.stats()["evictions"] == (8 if policy == "lru" else 16)
+    finally:
+        pg.close()
+        store.close()
+        vol.close()
+
+
+def test_cache_size_from_the_camera_path(ctx):
+    """hy_pager_tune_slots: the most bricks any camera of the path sees (8
+    per cluster here) plus 10 %, capped by the byte budget."""
+    vox, cams = _three_clusters()
+    vol = hy.Volume(ctx, vox, 8, 1)
+    store = hy.Store.from_volume(vol)
+    try:
+        path = [hy.camera_ptu(pos, tgt, (0.0, 1.0, 0.0), 10.0) for pos, tgt in cams.values()]
+        slot = store.info.slot_bytes
+        assert hy.Pager.tune_slots(ctx, store, path, 1 << 30) == (9, 8)
+        assert hy.Pager.tune_slots(ctx, store, path, 3 * slot + 5) == (3, 8)
+        wide = [hy.camera_orbit((30.0, 20.0, 2.5))]
+        slots, most = hy.Pager.tune_slots(ctx, store, wide, 1 << 30)
+        assert most == 24 and slots == 24  # never more than the store holds
+        with pytest.raises(hy.HydrantError):
+            hy.Pager.tune_slots(ctx, store, path, slot - 1)
+    finally:
         store.close()
         vol.close()
