@@ -534,6 +534,77 @@ def ert_leg(hy, ctx, dev, reps=5):
         vol.close()
 
 
+def configs_leg(hy, ctx, dev, reps=5, row_step=16):
+    """The plain-Volume and the tubes configurations at their stated sizes,
+    one view each (per-view fused kernel; the L2 written over between timed
+    launches, CUDA events on the library's stream), each image checked
+    against the oracle: the whole 512^2 frame for the plain Volume
+    configuration, every 16th row for the 1024^2 tubes variants (max LSB of
+    RGBA8, max abs of the floats, equal sample counts)."""
+    import numpy as np
+    import torch
+
+    from hydrant_gb300 import workloads as wl
+    from oracle import oracle as orc
+
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    flush = torch.empty(512 * 2**20, dtype=torch.uint8, device=dev)
+    out = {}
+
+    def one(name, w, vol, ov, kw, rows):
+        cam = wl.make_camera(w.views[0].camera)
+        view = hy.camera_view(vol, cam)
+        W = H = w.views[0].width
+        p = hy.shader_params(count_samples=True, **kw)
+        if p.shader == hy._abi.SHADER_ISOSURFACE:
+            hy.iso_lighting(vol, cam, p)
+        g = hy.render(ctx, vol, p, view, W, H, want_v=True)
+        y0 = 0 if rows == 1 else rows // 2
+        r = orc.render_row_step(ov, w.tf, orc.params_from(p), view_array(view), W, H, y0, rows,
+                                want_v=True)
+        q = hy.shader_params(**kw)
+        if q.shader == hy._abi.SHADER_ISOSURFACE:
+            hy.iso_lighting(vol, cam, q)
+        buf = torch.empty(W * H * 4, dtype=torch.uint8, device=dev)
+        evs = _timed_steps(torch, stream, reps,
+                           lambda: hy.render_device(ctx, vol, q, view, W, H, buf.data_ptr()),
+                           flush)
+        ctx.synchronize()
+        ms = sum(a.elapsed_time(b) for a, b in evs) / reps
+        gs = g.samples
+        # the sample count of the GPU image on the checked rows
+        lsb = int(np.abs(g.rgba[y0::rows].astype(int) - r["rgba"][y0::rows].astype(int)).max())
+        fab = float(np.abs(g.v[y0::rows].astype(np.float64) - r["v"][y0::rows]).max())
+        out[name] = {"ms_per_view": ms, "samples": gs, "gsamples_per_s": gs / ms / 1e6,
+                     "resolution": W, "parity_vs_oracle": {
+                         "rows": "all" if rows == 1 else f"every {rows}th row",
+                         "max_lsb": lsb, "max_abs": fab,
+                         "samples_equal": (gs == r["samples"]) if rows == 1 else None}}
+
+    w0 = wl.volume_c0()
+    vox = hy.synth_blobs_u8(w0.seed, w0.dim, w0.count)
+    vol = hy.Volume(ctx, vox, w0.block_size, w0.padding)
+    try:
+        ctx.set_transfer_fn(w0.tf)
+        one(w0.name + "_Volume", w0, vol, orc.OracleVolume(vox, w0.block_size, w0.padding),
+            w0.params, 1)
+    finally:
+        vol.close()
+    w1 = wl.tubes_c1()
+    vox = hy.synth_tubes_u8(w1.seed, w1.dim, w1.count)
+    vol = hy.Volume(ctx, vox, w1.block_size, w1.padding)
+    ov = orc.OracleVolume(vox, w1.block_size, w1.padding)
+    try:
+        ctx.set_transfer_fn(w1.tf)
+        one(w1.name + "_Isosurface_Color", w1, vol, ov, w1.params, row_step)
+        for mode in ("Volume", "Solid"):
+            one(f"{w1.name}_Blocks_{mode}_composite", w1, vol, ov,
+                dict(shader="Blocks", mode=mode, density=1e-2, composite=True), row_step)
+    finally:
+        vol.close()
+    return out
+
+
 def view_array(view):
     """A product view (hy_view) as the oracle's 20 floats."""
     import numpy as np
@@ -766,12 +837,16 @@ def main_ours(args):
 
     # ---- the configuration's compositing variant and the differentiable
     # configuration, each at its stated size (rank 0 of a 1-GPU run) -------
-    composite = diff = ert = None
+    composite = diff = ert = others = paging = None
     if ws == 1 and not args.no_extra:
         if not args.composite:
             composite = composite_leg(hy, ctx, vol, w, views, lighting, stream, flush, args)
         diff = diff_leg(hy, ctx, dev)
         ert = ert_leg(hy, ctx, dev)
+        others = configs_leg(hy, ctx, dev)
+        pargs = argparse.Namespace(**vars(args))
+        pargs.warmup = 3
+        paging = paging_leg(pargs, hy, ctx, local)
         ctx.set_transfer_fn(w.tf)
 
     value = aggregate_gsamples(samples, ws, args.steps, t)
@@ -865,6 +940,8 @@ def main_ours(args):
             "composite": composite,
             "diff": diff,
             "early_termination": ert,
+            "other_configs": others,
+            "paging": paging,
         }
         print(json.dumps(out_json), flush=True)
     batch.close()
@@ -882,20 +959,30 @@ def main_paging(args):
     120-frame orbit (azimuth +3 deg/frame) at 2048^2, density 5e-3.  With
     --coarse-level L the store's 2^L box-filtered level stays resident and
     bricks not (yet) in the cache are drawn from it."""
-    import numpy as np
     import torch
 
     ws, rank, local = dist_env()
     torch.cuda.set_device(local)
     build_all()
     import hydrant_gb300 as hy
+
+    ctx = hy.Context(local)
+    outj = paging_leg(args, hy, ctx, local, with_clocks=True)
+    print(json.dumps(outj), flush=True)
+    ctx.close()
+    return 0
+
+
+def paging_leg(args, hy, ctx, local, with_clocks=False):
+    """The out-of-core frames (main_paging's workload); returns its JSON line."""
+    import torch
+
     from hydrant_gb300 import _abi
     from hydrant_gb300 import workloads as wl
 
     sc = max(1, args.paging_scale)
     dim = (4096 // sc, 4096 // sc, 2048 // sc)
     res = 2048 // sc
-    ctx = hy.Context(local)
     ctx.set_transfer_fn(wl.TF9)
     t0 = time.perf_counter()
     store = hy.Store.noise(ctx, dim, 64, 1, seed=2, cell_voxels=256.0 / sc, occupancy=0.15)
@@ -930,8 +1017,9 @@ def main_paging(args):
         pg.render(p, hy.camera_orbit((-90.0 - 3 * f, 30.0, 2.2)), res, res, out.data_ptr())
     ctx.synchronize()
     st0 = pg.stats()
-    clocks = Clocks(local)
-    clocks.start()
+    clocks = Clocks(local) if with_clocks else None
+    if clocks:
+        clocks.start()
     fallback = 0
     tw = time.perf_counter()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -942,7 +1030,7 @@ def main_paging(args):
     ev1.record(stream)
     ctx.synchronize()
     wall = time.perf_counter() - tw
-    ck = clocks.stop()
+    ck = clocks.stop() if clocks else None
     gpu_s = ev0.elapsed_time(ev1) / 1e3
     st = pg.stats()
     d = {k: st[k] - st0[k] for k in st}
@@ -987,11 +1075,9 @@ def main_paging(args):
         "coarse_bricks_per_frame": fallback / frames,
         "clocks": ck,
     }
-    print(json.dumps(outj), flush=True)
     pg.close()
     store.close()
-    ctx.close()
-    return 0
+    return outj
 
 
 DIFF_CONFIG = dict(n=256, res=512, views=16, knots=32, ckpt_k=32, blobs=24)
