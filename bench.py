@@ -77,6 +77,9 @@ def parse_args():
                     help="paging: a cache of the whole --cache-gib (no sizing to the orbit)")
     ap.add_argument("--eviction", choices=["lru", "reference"], default="lru",
                     help="paging, realtime: least recently visible, or the reference's order")
+    ap.add_argument("--prefetch", action="store_true",
+                    help="paging, realtime: move the next orbit camera's bricks on the copy "
+                         "stream while each frame renders (hy_pager_prefetch)")
     ap.add_argument("--max-uploads", type=int, default=0,
                     help="paging: brick uploads per frame (0 = every missing brick)")
     ap.add_argument("--launch-shape", default="",
@@ -1024,8 +1027,11 @@ def paging_leg(args, hy, ctx, local, with_clocks=False):
     tw = time.perf_counter()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
+    prefetch = args.prefetch and args.pager == "realtime"
     for f in range(frames):
         pg.render(p, hy.camera_orbit((3.0 * f, 30.0, 2.2)), res, res, out.data_ptr())
+        if prefetch:  # the orbit's next camera, moved in while this frame renders
+            pg.prefetch(hy.camera_orbit((3.0 * (f + 1), 30.0, 2.2)))
         fallback += pg.stats()["fallback"]
     ev1.record(stream)
     ctx.synchronize()
@@ -1068,6 +1074,8 @@ def paging_leg(args, hy, ctx, local, with_clocks=False):
         "gpu_s": gpu_s, "wall_s": wall,
         "cache_hit_rate": (d["hits"] / lookups) if lookups else None,
         "uploads_per_frame": d["uploads"] / frames,
+        "prefetched_per_frame": d["prefetched"] / frames,
+        "prefetch": bool(prefetch),
         "passes_per_frame": d["passes"] / frames,
         "last_pass_ms_per_frame": last_pass_ms / frames,
         "upload_gb_per_s": d["upload_bytes"] / wall / 1e9,

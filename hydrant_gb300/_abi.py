@@ -112,7 +112,8 @@ class HyPagerDesc(C.Structure):
 
 class HyPagerStats(C.Structure):
     _fields_ = [(n, C.c_int64) for n in ("frames", "passes", "uploads", "upload_bytes", "hits",
-                                         "misses", "evictions", "visible", "fallback")]
+                                         "misses", "evictions", "visible", "fallback",
+                                         "prefetched")]
 
 
 class HyDiffParams(C.Structure):
@@ -197,6 +198,7 @@ _PROTOS = {
     "hy_pager_create": (C.c_int, [P, P, C.POINTER(HyPagerDesc), C.POINTER(P)]),
     "hy_pager_tune_slots": (C.c_int, [P, P, P, C.c_int32, C.c_int64, C.POINTER(C.c_int32),
                                      C.POINTER(C.c_int32)]),
+    "hy_pager_prefetch": (C.c_int, [P, C.POINTER(HyCamera)]),
     "hy_pager_destroy": (C.c_int, [P]),
     "hy_pager_volume": (C.c_int, [P, C.POINTER(P)]),
     "hy_pager_stats_get": (C.c_int, [P, C.POINTER(HyPagerStats)]),

@@ -508,6 +508,10 @@ class Pager:
         self.ctx.check(lib().hy_pager_render(self.handle, C.byref(params), C.byref(cam), width,
                                              height, C.c_void_p(rgba_ptr)))
 
+    def prefetch(self, next_cam: HyCamera) -> None:
+        """hy_pager_prefetch: move the next camera's bricks during this frame."""
+        self.ctx.check(lib().hy_pager_prefetch(self.handle, C.byref(next_cam)))
+
     def stats(self) -> dict:
         s = _abi.HyPagerStats()
         self.ctx.check(lib().hy_pager_stats_get(self.handle, C.byref(s)))

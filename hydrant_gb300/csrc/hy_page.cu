@@ -741,6 +741,19 @@ struct hy_pager {
     int next_free = 0;           // realtime: slots never used yet
     // realtime, LRU: per slot the last frame its brick was visible
     std::vector<int64_t> stamp;
+    // realtime prefetch (hy_pager_prefetch): the next camera's missing bricks
+    // move on the copy stream while the current frame renders, into slots
+    // that no page table of a frame still in flight references -- never-used
+    // slots, or spares: slots evicted a frame early and kept out of the page
+    // table.  Arrived bricks enter the page table at the next frame.
+    bool prefetching = false;
+    int reserve = 0;                           // spare slots kept while prefetching
+    std::vector<int> spare;
+    std::vector<std::pair<int, int>> arrived;  // (brick, slot)
+    cudaEvent_t rendered[2] = {nullptr, nullptr};  // realtime frames' renders, alternating
+    int rendered_i = 0;                            // the last frame's event
+    bool rendered_rec[2] = {false, false};
+    cudaEvent_t prefetch_ev = nullptr;
     int2 *info_stage[2] = {nullptr, nullptr};  // pinned staging of the page table
     // realtime frames overlap: a frame culls on its own stream, from a copy
     // of the chebyshev values, while the previous frame still renders
@@ -886,6 +899,9 @@ extern "C" int hy_pager_create(hy_ctx *ctx, hy_store *store, const hy_pager_desc
     if (e == cudaSuccess) e = cudaMalloc(&pg->gather_dev, 2 * pg->nslots * sizeof(GatherItem));
     for (int i = 0; i < 2 && e == cudaSuccess; ++i)
         e = cudaEventCreateWithFlags(&pg->gathered[i], cudaEventDisableTiming);
+    for (int i = 0; i < 2 && e == cudaSuccess; ++i)
+        e = cudaEventCreateWithFlags(&pg->rendered[i], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&pg->prefetch_ev, cudaEventDisableTiming);
     if (e != cudaSuccess) return fail(hy_cuda_fail(ctx, e, "pager: allocation"));
     std::vector<RegEntry> reg(nreg);
     if (pg->coarse) {
@@ -948,6 +964,9 @@ extern "C" int hy_pager_destroy(hy_pager *pg) {
     if (pg->gather_dev) cudaFree(pg->gather_dev);
     for (int i = 0; i < 2; ++i)
         if (pg->gathered[i]) cudaEventDestroy(pg->gathered[i]);
+    for (int i = 0; i < 2; ++i)
+        if (pg->rendered[i]) cudaEventDestroy(pg->rendered[i]);
+    if (pg->prefetch_ev) cudaEventDestroy(pg->prefetch_ev);
     for (int i = 0; i < 2; ++i) {
         if (pg->marched[i]) cudaEventDestroy(pg->marched[i]);
         if (pg->staged[i]) cudaEventDestroy(pg->staged[i]);
@@ -1149,10 +1168,22 @@ int render_realtime(hy_pager *pg, const hy_shader_params *p, const hy_view &view
     hy_volume *v = pg->vol;
     std::vector<int> req, visible;
     std::vector<float> d2;
-    int rc = run_cull(ctx, v, view, nullptr, pg->nslots, pg->cs, req, d2, &visible,
+    // while prefetching, `reserve` slots stay out of the required set (the
+    // nearest visible bricks) to serve as the next prefetch's spares
+    int rc = run_cull(ctx, v, view, nullptr, pg->nslots - pg->reserve, pg->cs, req, d2, &visible,
                       pg->cull_stream, pg->cheb_dev);
     if (rc) return rc;
     const int64_t frame = pg->stats.frames;
+    // bricks a prefetch moved in enter the page table now (the render
+    // stream waits for their copies before the page table is uploaded)
+    const bool had_arrivals = !pg->arrived.empty();
+    for (auto &a : pg->arrived) {
+        pg->page[a.first] = a.second;
+        pg->owner[a.second] = a.first;
+        pg->stamp[a.second] = frame;
+    }
+    const int64_t accepted = int64_t(pg->arrived.size());
+    pg->arrived.clear();
     std::vector<char> required(v->nbricks, 0);
     for (int b : req) required[b] = 1;
     // visible resident bricks are used this frame
@@ -1179,11 +1210,15 @@ int render_realtime(hy_pager *pg, const hy_shader_params *p, const hy_view &view
                                                            : int(missing.size());
     std::vector<int> move_b, move_s, evicted;
     int next_free = pg->next_free;
+    std::vector<int> spare = pg->spare;
     for (int i = 0; i < int(missing.size()) && int(move_b.size()) < budget; ++i) {
         const int b = missing[i].second;
         int slot;
         if (next_free < pg->nslots) {
             slot = next_free++;
+        } else if (!spare.empty()) {
+            slot = spare.back();
+            spare.pop_back();
         } else if (!victims.empty()) {
             slot = victims.back().second;
             victims.pop_back();
@@ -1203,6 +1238,7 @@ int render_realtime(hy_pager *pg, const hy_shader_params *p, const hy_view &view
     pg->stats.hits += hits;
     pg->stats.misses += int64_t(missing.size());
     pg->next_free = next_free;
+    pg->spare = spare;
     for (int old : evicted) {
         pg->page[old] = -1;
         ++pg->stats.evictions;
@@ -1212,8 +1248,32 @@ int render_realtime(hy_pager *pg, const hy_shader_params *p, const hy_view &view
         pg->page[move_b[i]] = move_s[i];
         pg->stamp[move_s[i]] = frame;
     }
+    // prefetching: the next prefetch needs slots that this frame's page table
+    // does not reference; as many as this frame brought in (moved plus
+    // arrived) are evicted now, in the policy's order, among the bricks this
+    // frame does not require
+    if (pg->prefetching) {
+        // the reserve follows the frames' turnover (twice the bricks this
+        // frame brought in, 16 .. slots / 8)
+        const int64_t turnover = int64_t(move_b.size()) + accepted;
+        pg->reserve = int(std::min<int64_t>(std::max<int64_t>(2 * turnover, 16),
+                                            std::max(pg->nslots / 8, 1)));
+        const int64_t want = std::min<int64_t>(pg->reserve, int64_t(pg->nslots - int(req.size())));
+        while (int64_t(pg->spare.size()) < want && !victims.empty()) {
+            const int s = victims.back().second;
+            victims.pop_back();
+            if (pg->owner[s] < 0) continue;
+            pg->page[pg->owner[s]] = -1;
+            pg->owner[s] = -1;
+            pg->spare.push_back(s);
+            ++pg->stats.evictions;
+        }
+    }
     // one gather kernel on the render stream moves every brick of the frame:
     // it runs after the previous frame's render, so reused slots are free
+    // after the prefetch's copies: its bricks are in this frame's page table,
+    // and its move list shares the device staging list with this frame's
+    if (had_arrivals) HY_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, pg->prefetch_ev, 0));
     rc = move_bricks(pg, move_b.data(), move_s.data(), int(move_b.size()), ctx->stream,
                      pg->frame_buf);
     if (rc) return rc;
@@ -1229,7 +1289,69 @@ int render_realtime(hy_pager *pg, const hy_shader_params *p, const hy_view &view
         for (int b : visible) fallback += pg->page[b] < 0;
     pg->stats.fallback = fallback;
     ++pg->stats.passes;
-    return hy_render_device(ctx, v, p, &view, W, H, rgba_dev, nullptr, nullptr);
+    rc = hy_render_device(ctx, v, p, &view, W, H, rgba_dev, nullptr, nullptr);
+    if (rc) return rc;
+    pg->rendered_i ^= 1;
+    HY_CUDA(ctx, cudaEventRecord(pg->rendered[pg->rendered_i], ctx->stream));
+    pg->rendered_rec[pg->rendered_i] = true;
+    return HY_OK;
+}
+
+// hy_pager_prefetch: the next camera's required bricks that are not resident,
+// nearest first (within max_uploads_per_frame), moved on the copy stream
+// into never-used or spare slots.  A spare slot left the page table at the
+// last frame, so only the frame before may still read it: the copy stream
+// waits for that frame's render, not for the last one.
+int prefetch_realtime(hy_pager *pg, const hy_view &view) {
+    hy_ctx *ctx = pg->ctx;
+    hy_volume *v = pg->vol;
+    pg->prefetching = true;
+    std::vector<int> req;
+    std::vector<float> d2;
+    if (pg->reserve == 0) pg->reserve = std::min(16, std::max(pg->nslots / 8, 1));
+    int rc = run_cull(ctx, v, view, nullptr, pg->nslots - pg->reserve, pg->cs, req, d2, nullptr,
+                      pg->cull_stream, pg->cheb_dev);
+    if (rc) return rc;
+    std::vector<char> coming(v->nbricks, 0);
+    for (auto &a : pg->arrived) coming[a.first] = 1;
+    std::vector<std::pair<float, int>> missing;
+    for (size_t i = 0; i < req.size(); ++i)
+        if (pg->page[req[i]] < 0 && !coming[req[i]]) missing.push_back({d2[i], req[i]});
+    std::sort(missing.begin(), missing.end());
+    const int budget = pg->desc.max_uploads_per_frame > 0 ? pg->desc.max_uploads_per_frame
+                                                           : int(missing.size());
+    std::vector<int> move_b, move_s;
+    int next_free = pg->next_free;
+    size_t nspare = pg->spare.size();
+    for (int i = 0; i < int(missing.size()) && int(move_b.size()) < budget; ++i) {
+        int slot;
+        if (next_free < pg->nslots) {
+            slot = next_free++;
+        } else if (nspare > 0) {
+            slot = pg->spare[--nspare];
+        } else {
+            break;
+        }
+        const long long off = pg->store->offset[missing[i].second];
+        if (off < 0 || off + (long long)v->slot_stride > (long long)pg->store->host_bytes)
+            return hy_fail(ctx, HY_ERR_STATE, "pager: a planned brick is not in the store");
+        move_b.push_back(missing[i].second);
+        move_s.push_back(slot);
+    }
+    if (move_b.empty()) return HY_OK;
+    // the frame before the last may still read a spare slot's old brick, and
+    // its moves used the device move list this prefetch rewrites
+    const int prev = pg->rendered_i ^ 1;
+    if (pg->rendered_rec[prev]) HY_CUDA(ctx, cudaStreamWaitEvent(pg->copy, pg->rendered[prev], 0));
+    rc = move_bricks(pg, move_b.data(), move_s.data(), int(move_b.size()), pg->copy,
+                     pg->frame_buf);
+    if (rc) return rc;
+    HY_CUDA(ctx, cudaEventRecord(pg->prefetch_ev, pg->copy));
+    pg->next_free = next_free;
+    pg->spare.resize(nspare);
+    for (size_t i = 0; i < move_b.size(); ++i) pg->arrived.push_back({move_b[i], move_s[i]});
+    pg->stats.prefetched += int64_t(move_b.size());
+    return HY_OK;
 }
 
 }  // namespace
@@ -1250,6 +1372,18 @@ extern "C" int hy_pager_render(hy_pager *pg, const hy_shader_params *p, const hy
     if (pg->desc.mode == HY_PAGER_LOSSLESS)
         return render_lossless(pg, &q, cam, view, W, H, rgba_dev);
     return render_realtime(pg, &q, view, W, H, rgba_dev);
+}
+
+extern "C" int hy_pager_prefetch(hy_pager *pg, const hy_camera *next_cam) {
+    if (!pg || !next_cam) return HY_ERR_INVALID;
+    hy_ctx *ctx = pg->ctx;
+    if (pg->desc.mode != HY_PAGER_REALTIME)
+        return hy_fail(ctx, HY_ERR_UNSUPPORTED, "pager: prefetch needs the realtime policy");
+    HY_CUDA(ctx, cudaSetDevice(ctx->device));
+    hy_view view;
+    int rc = hy_camera_view(pg->vol, next_cam, &view);
+    if (rc) return rc;
+    return prefetch_realtime(pg, view);
 }
 
 extern "C" int hy_pager_render_host(hy_pager *pg, const hy_shader_params *p, const hy_camera *cam,

@@ -296,6 +296,7 @@ typedef struct hy_pager_desc {
 typedef struct hy_pager_stats {
     int64_t frames, passes, uploads, upload_bytes, hits, misses, evictions, visible;
     int64_t fallback;  /* realtime + coarse level: visible bricks drawn coarse, last frame */
+    int64_t prefetched; /* realtime: bricks moved by hy_pager_prefetch */
 } hy_pager_stats;
 
 /* Store of a resident volume's bricks (copies its pool to pinned host memory). */
@@ -387,6 +388,19 @@ int hy_pager_present(const hy_pager *pager, uint8_t *mask);
  *    slot i is registry id nbricks + i (lowest_blkcnt = nbricks). */
 int hy_pager_render(hy_pager *pager, const hy_shader_params *params, const hy_camera *cam,
                     int32_t width, int32_t height, uint8_t *rgba_dev);
+/* REALTIME: start moving the bricks `next_cam` will require (nearest first,
+ * within max_uploads_per_frame) while the frame just rendered is still
+ * drawing: the moves run on the pager's copy stream, and the next
+ * hy_pager_render takes the arrived bricks into its page table (its render
+ * waits for their copies).  A frame loop that knows its next camera (a
+ * camera path, or one extrapolated from the last two) calls this after each
+ * hy_pager_render.  The moves may only use slots that no frame in flight can
+ * read: never-used slots, or spares -- once prefetching, each frame evicts
+ * (by the pager's policy, among the bricks it does not require) as many
+ * bricks as it brought in and keeps those slots out of its page table for
+ * the next prefetch.  The reference decodes arriving bricks on a worker
+ * thread beside the render (unarchive_pipeline.cc:12-23). */
+int hy_pager_prefetch(hy_pager *pager, const hy_camera *next_cam);
 /* Same into a host image; returns when it is there. */
 int hy_pager_render_host(hy_pager *pager, const hy_shader_params *params, const hy_camera *cam,
                          int32_t width, int32_t height, uint8_t *rgba_host);

@@ -485,3 +485,48 @@ def test_cache_size_from_the_camera_path(ctx):
     finally:
         store.close()
         vol.close()
+
+
+@pytest.mark.parametrize("policy", ["lru", "reference"])
+def test_prefetch_during_the_previous_frame(ctx, tubes, policy):
+    """hy_pager_prefetch after every frame moves the next camera's bricks on
+    the copy stream: each frame still equals the oracle given the resident
+    set the pager reports (arrived bricks in, spare slots out), the render
+    path misses fewer bricks than without prefetching, and frames stay
+    right when the prediction is wrong (the path turns back)."""
+    torch = pytest.importorskip("torch")
+    vol, ov, store = tubes
+    slots = 60
+    ev = _abi.EVICT_LRU if policy == "lru" else _abi.EVICT_REFERENCE
+    W, H = 48, 40
+    p = hy.shader_params(shader="Volume", density=0.4, sample_rate=0.5)
+    arms = [(20 + 12 * f, 35, 2.2) for f in range(8)] + [(80, 35, 2.2), (10, 35, 2.2)]
+
+    def run(prefetch):
+        pg = hy.Pager(ctx, store, slots, _abi.PAGER_REALTIME, 0, ev)
+        out = torch.zeros(W * H * 4, dtype=torch.uint8, device="cuda")
+        try:
+            for f, arm in enumerate(arms):
+                cam = hy.camera_orbit(arm)
+                pg.render(p, cam, W, H, out.data_ptr())
+                if prefetch and f + 1 < len(arms):
+                    # the path's next camera, except a wrong guess near the end
+                    guess = arms[f + 1] if f < 7 else (arm[0] + 12, 35, 2.2)
+                    pg.prefetch(hy.camera_orbit(guess))
+                ctx.synchronize()
+                mask = pg.present()
+                ov.set_present(mask)
+                view = view_array(hy.camera_view(vol, cam))
+                ref = orc.render(ov, wl.TF9, orc.params_from(p), view, W, H)["rgba"]
+                got = out.cpu().numpy().reshape(H, W, 4)
+                d = np.abs(got.astype(int) - ref.astype(int)).max()
+                assert d <= 1, f"prefetch={prefetch} frame {f}: {d} LSB"
+            return pg.stats()
+        finally:
+            ov.set_present(np.ones(ov.grid[0] * ov.grid[1] * ov.grid[2], np.uint8))
+            pg.close()
+
+    plain = run(False)
+    pre = run(True)
+    assert plain["prefetched"] == 0 and pre["prefetched"] > 0
+    assert pre["misses"] < plain["misses"], (pre["misses"], plain["misses"])
