@@ -84,7 +84,7 @@ def parse_args():
                     help="paging: brick uploads per frame (0 = every missing brick)")
     ap.add_argument("--launch-shape", default="",
                     help="fixed batch launch shape tile_w,grab,block_warps,blocks_per_sm,"
-                         "block_queue (implies --no-autotune)")
+                         "block_queue[,steps_per_iter] (implies --no-autotune)")
     ap.add_argument("--no-autotune", action="store_true",
                     help="use the default batch launch shape (profiling)")
     ap.add_argument("--cpu-row-step", type=int, default=128,
@@ -756,6 +756,7 @@ def main_ours(args):
         c = batch.config
         tuned = {"tile_w": c.tile_w, "grab": c.grab, "block_warps": c.block_warps,
                  "blocks_per_sm": c.blocks_per_sm, "block_queue": c.block_queue,
+                 "steps_per_iter": max(1, c.steps_per_iter),
                  "source": "fixed" if args.launch_shape else "default"}
     else:
         tuned = autotune.tuned_config(batch, key, out.data_ptr(), reps=1)

@@ -97,6 +97,7 @@ class HyBatchConfig(C.Structure):
         ("block_warps", C.c_int32),
         ("blocks_per_sm", C.c_int32),
         ("block_queue", C.c_int32),
+        ("steps_per_iter", C.c_int32),
     ]
 
 

@@ -342,8 +342,9 @@ class Batch:
         self.ctx.check(lib().hy_batch_get_config(self.handle, C.byref(c)))
         return c
 
-    def set_config(self, tile_w=8, grab=1, block_warps=4, blocks_per_sm=0, block_queue=1) -> None:
-        c = HyBatchConfig(tile_w, grab, block_warps, blocks_per_sm, block_queue)
+    def set_config(self, tile_w=8, grab=1, block_warps=4, blocks_per_sm=0, block_queue=1,
+                   steps_per_iter=1) -> None:
+        c = HyBatchConfig(tile_w, grab, block_warps, blocks_per_sm, block_queue, steps_per_iter)
         self.ctx.check(lib().hy_batch_set_config(self.handle, C.byref(c)))
 
     def set_counting(self, on: bool) -> None:

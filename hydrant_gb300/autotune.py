@@ -55,11 +55,12 @@ def tuned_config(batch, key: str, rgba_ptr: int, reps: int = 2, path: Path = DEF
     if not retune and key in cache:
         c = cache[key]
         batch.set_config(c["tile_w"], c["grab"], c["block_warps"], c.get("blocks_per_sm", 0),
-                         c.get("block_queue", 1))
+                         c.get("block_queue", 1), c.get("steps_per_iter", 1))
         return dict(c, source="cache")
     best = batch.autotune(rgba_ptr, reps)
     c = {"tile_w": best.tile_w, "grab": best.grab, "block_warps": best.block_warps,
-         "blocks_per_sm": best.blocks_per_sm, "block_queue": best.block_queue}
+         "blocks_per_sm": best.blocks_per_sm, "block_queue": best.block_queue,
+         "steps_per_iter": max(1, best.steps_per_iter)}
     cache[key] = c
     try:
         Path(path).write_text(json.dumps(cache, indent=1, sort_keys=True))

@@ -52,7 +52,7 @@ constexpr int kMaxBlockThreads = 256;
 #endif
 
 // Shades one pixel of a batch view and stores its RGBA8 value.
-template <int SHADER, int PC, int DT, bool PADDED, int COMPOSITE, bool LEAN, bool GATHER, bool ERT>
+template <int SHADER, int PC, int DT, bool PADDED, int COMPOSITE, bool LEAN, bool GATHER, int LOOP>
 __device__ __forceinline__ long long shade_batch_pixel(const BatchArgs &B, const Shared &S,
                                                        const BatchView &bv, int x, int y) {
     const ShadeArgs &A = B.A;
@@ -67,7 +67,7 @@ __device__ __forceinline__ long long shade_batch_pixel(const BatchArgs &B, const
                                                         aux);
     } else {
         Px p;
-        samples = emit<SHADER, PC, DT, PADDED, LEAN, GATHER, ERT>(p, A, bv.view, S, ox, oy, oz, dx, dy,
+        samples = emit<SHADER, PC, DT, PADDED, LEAN, GATHER, LOOP>(p, A, bv.view, S, ox, oy, oz, dx, dy,
                                                              dz, 0.f, 0.f, 0.f, A.bbox_max[0],
                                                              A.bbox_max[1], A.bbox_max[2]);
         v = make_float4(p.vx, p.vy, p.vz, p.vw);
@@ -100,7 +100,7 @@ __device__ __forceinline__ int find_view(const int *starts, int n, int t) {
 // LEAN: Volume shader in Default mode without compositing (theta / phi are
 // not needed for an RGBA image; see VolumeMarch::step).
 template <int SHADER, int PC, int DT, bool PADDED, int COMPOSITE, bool LEAN, bool GATHER = false,
-          bool ERT = false>
+          int LOOP = kLoopOne>
 __device__ __forceinline__ void batch_body(const BatchArgs &B) {
     extern __shared__ float4 smem[];
     __shared__ unsigned int s_t0;
@@ -134,7 +134,7 @@ __device__ __forceinline__ void batch_body(const BatchArgs &B) {
                 const int x = (ux * B.bx + wx) * B.tile_w + lx;
                 const int y = (uy * B.by + wy) * B.tile_h + ly;
                 samples +=
-                    shade_batch_pixel<SHADER, PC, DT, PADDED, COMPOSITE, LEAN, GATHER, ERT>(B, S, bv, x, y);
+                    shade_batch_pixel<SHADER, PC, DT, PADDED, COMPOSITE, LEAN, GATHER, LOOP>(B, S, bv, x, y);
             }
         }
     } else {
@@ -150,7 +150,7 @@ __device__ __forceinline__ void batch_body(const BatchArgs &B) {
                 const BatchView &bv = B.views[vi];
                 const int local = t - starts[vi];
                 const int ty = local / bv.tiles_x, tx = local - ty * bv.tiles_x;
-                samples += shade_batch_pixel<SHADER, PC, DT, PADDED, COMPOSITE, LEAN, GATHER, ERT>(
+                samples += shade_batch_pixel<SHADER, PC, DT, PADDED, COMPOSITE, LEAN, GATHER, LOOP>(
                     B, S, bv, tx * B.tile_w + lx, ty * B.tile_h + ly);
             }
         }
@@ -187,62 +187,68 @@ template <int DT, bool PADDED, bool GATHER>
 constexpr int lean_regs() {
     return GATHER ? HY_BATCH_GATHER_REGS : (DT == HY_DTYPE_U8 && PADDED) ? HY_BATCH_LEAN_REGS : 64;
 }
-template <int SHADER, int PC, int DT, bool PADDED, bool GATHER, bool ERT>
+template <int SHADER, int PC, int DT, bool PADDED, bool GATHER, int LOOP>
 __global__ void __maxnreg__((lean_regs<DT, PADDED, GATHER>()))
     batch_lean_kernel(const __grid_constant__ BatchArgs B) {
-    batch_body<SHADER, PC, DT, PADDED, 0, true, GATHER, ERT>(B);
+    batch_body<SHADER, PC, DT, PADDED, 0, true, GATHER, LOOP>(B);
+}
+
+template <int SHADER, int PC, int DT, bool PADDED, bool GATHER>
+const void *pick_lean(const ShadeArgs &a, int steps_per_iter) {
+    if (a.ert > 0.f)
+        return reinterpret_cast<const void *>(
+            &batch_lean_kernel<SHADER, PC, DT, PADDED, GATHER, kLoopErt>);
+    if (steps_per_iter == 2)
+        return reinterpret_cast<const void *>(
+            &batch_lean_kernel<SHADER, PC, DT, PADDED, GATHER, kLoopTwo>);
+    return reinterpret_cast<const void *>(&batch_lean_kernel<SHADER, PC, DT, PADDED, GATHER, kLoopOne>);
 }
 
 template <int SHADER, int PC, int DT, bool PADDED>
-const void *pick_c(const ShadeArgs &a) {
+const void *pick_c(const ShadeArgs &a, int steps_per_iter) {
     if (a.composite)
         return reinterpret_cast<const void *>(&batch_kernel<SHADER, PC, DT, PADDED, 1>);
     if constexpr (SHADER == HY_SHADER_VOLUME) {
         if (a.mode == HY_VOLUME_DEFAULT) {
-            const bool ert = a.ert > 0.f;
             if constexpr (DT == HY_DTYPE_U8 && PADDED) {
                 if (a.vol.tex)  // bricks in gather textures
-                    return ert ? reinterpret_cast<const void *>(
-                                     &batch_lean_kernel<SHADER, PC, DT, PADDED, true, true>)
-                               : reinterpret_cast<const void *>(
-                                     &batch_lean_kernel<SHADER, PC, DT, PADDED, true, false>);
+                    return pick_lean<SHADER, PC, DT, PADDED, true>(a, steps_per_iter);
             }
-            return ert ? reinterpret_cast<const void *>(
-                             &batch_lean_kernel<SHADER, PC, DT, PADDED, false, true>)
-                       : reinterpret_cast<const void *>(
-                             &batch_lean_kernel<SHADER, PC, DT, PADDED, false, false>);
+            return pick_lean<SHADER, PC, DT, PADDED, false>(a, steps_per_iter);
         }
     }
     return reinterpret_cast<const void *>(&batch_kernel<SHADER, PC, DT, PADDED, 0>);
 }
 
 template <int SHADER>
-const void *pick_shader(const ShadeArgs &a) {
+const void *pick_shader(const ShadeArgs &a, int spi) {
     if constexpr (SHADER == HY_SHADER_BLOCKS || SHADER == HY_SHADER_PAGING) {
-        return pick_c<SHADER, 0, HY_DTYPE_U8, false>(a);
+        return pick_c<SHADER, 0, HY_DTYPE_U8, false>(a, spi);
     } else {
         const bool padded = a.vol.pad > 0;
         if (a.vol.dtype == HY_DTYPE_F32) {
-            return padded ? pick_c<SHADER, 0, HY_DTYPE_F32, true>(a)
-                          : pick_c<SHADER, 0, HY_DTYPE_F32, false>(a);
+            return padded ? pick_c<SHADER, 0, HY_DTYPE_F32, true>(a, spi)
+                          : pick_c<SHADER, 0, HY_DTYPE_F32, false>(a, spi);
         }
-        if (padded && a.vol.P == 66) return pick_c<SHADER, 66, HY_DTYPE_U8, true>(a);
-        if (padded && a.vol.P == 130) return pick_c<SHADER, 130, HY_DTYPE_U8, true>(a);
-        return padded ? pick_c<SHADER, 0, HY_DTYPE_U8, true>(a)
-                      : pick_c<SHADER, 0, HY_DTYPE_U8, false>(a);
+        if (padded && a.vol.P == 66) return pick_c<SHADER, 66, HY_DTYPE_U8, true>(a, spi);
+        if (padded && a.vol.P == 130) return pick_c<SHADER, 130, HY_DTYPE_U8, true>(a, spi);
+        return padded ? pick_c<SHADER, 0, HY_DTYPE_U8, true>(a, spi)
+                      : pick_c<SHADER, 0, HY_DTYPE_U8, false>(a, spi);
     }
 }
 
-const void *pick_kernel(const ShadeArgs &a) {
+// steps_per_iter: march steps per loop iteration of the lean Volume march
+// (1 or 2; early termination keeps 1)
+const void *pick_kernel(const ShadeArgs &a, int steps_per_iter = 1) {
     switch (a.shader) {
         case HY_SHADER_VOLUME:
-            return pick_shader<HY_SHADER_VOLUME>(a);
+            return pick_shader<HY_SHADER_VOLUME>(a, steps_per_iter);
         case HY_SHADER_BLOCKS:
-            return pick_shader<HY_SHADER_BLOCKS>(a);
+            return pick_shader<HY_SHADER_BLOCKS>(a, steps_per_iter);
         case HY_SHADER_PAGING:
-            return pick_shader<HY_SHADER_PAGING>(a);
+            return pick_shader<HY_SHADER_PAGING>(a, steps_per_iter);
         default:
-            return pick_shader<HY_SHADER_ISOSURFACE>(a);
+            return pick_shader<HY_SHADER_ISOSURFACE>(a, steps_per_iter);
     }
 }
 
@@ -290,7 +296,8 @@ bool valid_config(const hy_batch_config &c) {
     const bool tw = c.tile_w == 4 || c.tile_w == 8 || c.tile_w == 16 || c.tile_w == 32;
     return tw && c.grab >= 1 && c.grab <= 16 && c.block_warps >= 1 &&
            c.block_warps * 32 <= kMaxBlockThreads && c.blocks_per_sm >= 0 &&
-           c.blocks_per_sm <= 32 && (c.block_queue == 0 || c.block_queue == 1);
+           c.blocks_per_sm <= 32 && (c.block_queue == 0 || c.block_queue == 1) &&
+           c.steps_per_iter >= 0 && c.steps_per_iter <= 2;
 }
 
 void drop_graph(hy_batch *b) {
@@ -330,7 +337,7 @@ void fill_view(BatchView &d, const hy_batch_view &v, int tiles_x, int tile0) {
 // (Re)build the tile layout for the current config and the persistent grid.
 int layout(hy_batch *b) {
     hy_ctx *ctx = b->ctx;
-    b->kernel = pick_kernel(b->base);
+    b->kernel = pick_kernel(b->base, b->cfg.steps_per_iter == 2 ? 2 : 1);
     int bx, by;
     unit_shape(b->cfg, bx, by);
     const int tw = b->cfg.tile_w * bx, th = (32 / b->cfg.tile_w) * by;
@@ -607,7 +614,7 @@ extern "C" int hy_batch_autotune(hy_batch *b, uint8_t *rgba_dev, int32_t reps,
     for (int tw : tws)
         for (int g : grabs)
             for (int w : warps) {
-                hy_batch_config c{tw, g, w, 0, bq};
+                hy_batch_config c{tw, g, w, 0, bq, 1};
                 b->cfg = c;
                 if ((rc = layout(b))) goto done;
                 if ((rc = launch(b, rgba_dev))) goto done;  // warm-up and graph build
@@ -623,6 +630,26 @@ extern "C" int hy_batch_autotune(hy_batch *b, uint8_t *rgba_dev, int32_t reps,
                     best = c;
                 }
             }
+    // samples per loop iteration on the fastest shape
+    if (b->base.shader == HY_SHADER_VOLUME && b->base.mode == HY_VOLUME_DEFAULT &&
+        !b->base.composite && !(b->base.ert > 0.f)) {
+        hy_batch_config c = best;
+        c.steps_per_iter = 2;
+        b->cfg = c;
+        if ((rc = layout(b))) goto done;
+        if ((rc = launch(b, rgba_dev))) goto done;
+        HY_CUDA(ctx, cudaEventRecord(e0, ctx->stream));
+        for (int r = 0; r < reps; ++r)
+            if ((rc = launch(b, rgba_dev))) goto done;
+        HY_CUDA(ctx, cudaEventRecord(e1, ctx->stream));
+        HY_CUDA(ctx, cudaEventSynchronize(e1));
+        float ms = 0.f;
+        HY_CUDA(ctx, cudaEventElapsedTime(&ms, e0, e1));
+        if (ms < best_ms) {
+            best_ms = ms;
+            best = c;
+        }
+    }
 done:
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);

@@ -51,7 +51,7 @@ __device__ __forceinline__ uchar4 quantise(const ShadeArgs &A, float4 v) {
 // LEAN: Volume shader, Default mode, no compositing and no aux output
 // (theta / phi are not computed; see VolumeMarch::step).
 template <int SHADER, int PC, int DT, bool PADDED, int COMPOSITE, bool LEAN, bool GATHER = false,
-          bool ERT = false>
+          int LOOP = kLoopOne>
 __device__ __forceinline__ void render_body(const ShadeArgs &A) {
     extern __shared__ float4 smem[];
     float4 *tf = smem;
@@ -69,7 +69,7 @@ __device__ __forceinline__ void render_body(const ShadeArgs &A) {
             samples = composite_ray<SHADER, PC, DT, PADDED>(A, A.view, S, ox, oy, oz, dx, dy, dz, v, aux);
         } else {
             Px p;
-            samples = emit<SHADER, PC, DT, PADDED, LEAN, GATHER, ERT>(
+            samples = emit<SHADER, PC, DT, PADDED, LEAN, GATHER, LOOP>(
                 p, A, A.view, S, ox, oy, oz, dx, dy, dz, 0.f, 0.f, 0.f, A.bbox_max[0],
                 A.bbox_max[1], A.bbox_max[2]);
             v = make_float4(p.vx, p.vy, p.vz, p.vw);
@@ -88,9 +88,9 @@ __device__ __forceinline__ void render_body(const ShadeArgs &A) {
     count_samples(A, samples);
 }
 
-template <int SHADER, int PC, int DT, bool PADDED, int COMPOSITE, bool LEAN, bool ERT = false>
+template <int SHADER, int PC, int DT, bool PADDED, int COMPOSITE, bool LEAN, int LOOP = kLoopOne>
 __global__ void __launch_bounds__(kThreads) render_kernel(const __grid_constant__ ShadeArgs A) {
-    render_body<SHADER, PC, DT, PADDED, COMPOSITE, LEAN, false, ERT>(A);
+    render_body<SHADER, PC, DT, PADDED, COMPOSITE, LEAN, false, LOOP>(A);
 }
 
 
@@ -267,7 +267,7 @@ void launch_fused(const ShadeArgs &a, cudaStream_t s) {
             // slower, 177.0 vs 186.5 Gsamples/s on the 64-view step)
             const bool ert = a.ert > 0.f;
             if (ert)
-                render_kernel<SHADER, PC, DT, PADDED, 0, true, true>
+                render_kernel<SHADER, PC, DT, PADDED, 0, true, kLoopErt>
                     <<<grid_of(a), kThreads, smem_bytes(a), s>>>(a);
             else
                 render_kernel<SHADER, PC, DT, PADDED, 0, true><<<grid_of(a), kThreads, smem_bytes(a), s>>>(a);

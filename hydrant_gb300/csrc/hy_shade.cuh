@@ -601,19 +601,29 @@ struct VolumeMarch {
     }
 };
 
-// ERT: early ray termination by warp vote (hy_shader_params.early_termination).
-// After each step the lanes still marching vote; when v.w >= A.ert on all of
-// them they stop together (a lane alone stopping would not free its warp).
-// A lane stops only when its own ray is that opaque, whichever lanes vote
-// with it, so what it leaves out adds at most 1 - A.ert per channel.
-template <int PC, int DT, bool PADDED, bool LEAN = false, bool GATHER = false, bool ERT = false>
+// LOOP: the shape of the march loop.
+//  kLoopOne  one step per iteration;
+//  kLoopErt  early ray termination by warp vote (hy_shader_params.
+//            early_termination): after each step the lanes still marching
+//            vote; when v.w >= A.ert on all of them they stop together (a lane
+//            alone stopping would not free its warp).  A lane stops only when
+//            its own ray is that opaque, whichever lanes vote with it, so what
+//            it leaves out adds at most 1 - A.ert per channel;
+//  kLoopTwo  two steps per iteration (the batch's steps_per_iter = 2): the
+//            same steps in the same order, one loop test per step still.
+constexpr int kLoopOne = 0, kLoopErt = 1, kLoopTwo = 2;
+template <int PC, int DT, bool PADDED, bool LEAN = false, bool GATHER = false, int LOOP = kLoopOne>
 __device__ __forceinline__ long long volume_main(Px &p, const ShadeArgs &A, const Shared &S) {
     unsigned int samples = 0;
     VolumeMarch m;
     m.init(p, A.step);
     while (p.nsteps > 0) {
         if (!m.step<PC, DT, PADDED, LEAN, GATHER>(p, A, S, samples)) break;
-        if (ERT && __all_sync(__activemask(), p.vw >= A.ert)) break;
+        if (LOOP == kLoopErt && __all_sync(__activemask(), p.vw >= A.ert)) break;
+        if (LOOP == kLoopTwo) {
+            if (p.nsteps <= 0) break;
+            if (!m.step<PC, DT, PADDED, LEAN, GATHER>(p, A, S, samples)) break;
+        }
     }
     return samples;
 }
@@ -833,11 +843,11 @@ __device__ __forceinline__ long long iso_main(Px &p, const ShadeArgs &A, const V
 }
 
 template <int SHADER, int PC, int DT, bool PADDED, bool LEAN = false, bool GATHER = false,
-          bool ERT = false>
+          int LOOP = kLoopOne>
 __device__ __forceinline__ long long run_main(Px &p, const ShadeArgs &A, const ViewArgs &Vw,
                                              const Shared &S) {
     if (SHADER == HY_SHADER_VOLUME)
-        return volume_main<PC, DT, PADDED, LEAN, GATHER, ERT>(p, A, S);
+        return volume_main<PC, DT, PADDED, LEAN, GATHER, LOOP>(p, A, S);
     if (SHADER == HY_SHADER_BLOCKS) return blocks_main(p, A);
     if (SHADER == HY_SHADER_PAGING) return paging_main(p, A);
     return iso_main<PC, DT, PADDED>(p, A, Vw, S);
@@ -904,14 +914,14 @@ __device__ __forceinline__ bool emit_setup(Px &p, const ShadeArgs &A, float ox, 
 
 // ray_emit_shader_impl: emit_setup, then main on a hit (shader.hpp:113-137).
 template <int SHADER, int PC, int DT, bool PADDED, bool LEAN = false, bool GATHER = false,
-          bool ERT = false>
+          int LOOP = kLoopOne>
 __device__ __forceinline__ long long emit(Px &p, const ShadeArgs &A, const ViewArgs &Vw,
                                           const Shared &S, float ox,
                                           float oy, float oz, float dx, float dy, float dz,
                                           float x0, float y0, float z0, float x1, float y1,
                                           float z1) {
     if (emit_setup<SHADER>(p, A, ox, oy, oz, dx, dy, dz, x0, y0, z0, x1, y1, z1))
-        return run_main<SHADER, PC, DT, PADDED, LEAN, GATHER, ERT>(p, A, Vw, S);
+        return run_main<SHADER, PC, DT, PADDED, LEAN, GATHER, LOOP>(p, A, Vw, S);
     return 0;
 }
 

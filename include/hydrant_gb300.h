@@ -460,6 +460,8 @@ typedef struct hy_batch_config {
     int32_t blocks_per_sm; /* persistent blocks per SM; 0 = as many as fit */
     int32_t block_queue;   /* 0: each warp takes warp tiles; 1: each block takes a block
                               tile and its warps shade neighbouring warp tiles */
+    int32_t steps_per_iter; /* lean Volume march: samples per loop iteration, 1 or 2
+                               (0 = 1); the same samples either way */
 } hy_batch_config;
 
 /* The batch keeps `vol`, which must outlive it; every render uses the
@@ -492,7 +494,8 @@ int hy_batch_render_device(hy_batch *batch, uint8_t *rgba_dev);
  * staging copy; any other buffer receives one copy from device memory. */
 int hy_batch_render(hy_batch *batch, uint8_t *rgba_host);
 /* Times every launch shape (queue per warp or per block, tile 8x4/4x8/16x2,
- * grab 1/2/4, 2/4/8 warps per block) on this batch and keeps the fastest;
+ * grab 1/2/4, 2/4/8 warps per block), then 1 or 2 march steps per loop
+ * iteration on the fastest shape, on this batch and keeps the fastest;
  * it is returned in *best.  For the Isosurface shader, params->to_world must
  * be set (hy_iso_lighting) when the batch is created. */
 int hy_batch_autotune(hy_batch *batch, uint8_t *rgba_dev, int32_t reps, hy_batch_config *best);

@@ -73,7 +73,7 @@ def test_batch_equals_per_view(ctx, tubes, kw):
         b.set_counting(True)
         for cfg in [(8, 1, 4, 0, 1), (4, 2, 2, 0, 0), (16, 4, 8, 0, 1), (32, 3, 1, 0, 0),
                     (8, 2, 4, 2, 1), (4, 1, 8, 0, 0),
-                    (8, 2, 8, 2, 1), (4, 1, 6, 0, 1)]:
+                    (8, 2, 8, 2, 1), (4, 1, 6, 0, 1), (8, 1, 4, 0, 1, 2)]:
             b.set_config(*cfg)
             got = b.render()
             assert ctx.stats().samples == ref_samples
@@ -135,7 +135,7 @@ def test_batch_equals_per_view_p66(ctx, blobs_bs64, mode):
     b = hy.Batch(ctx, blobs_bs64, hy.shader_params(**kw), views)
     try:
         b.set_counting(True)
-        for cfg in [(8, 1, 4, 0, 1), (8, 1, 8, 0, 0), (16, 2, 4, 0, 1)]:
+        for cfg in [(8, 1, 4, 0, 1), (8, 1, 8, 0, 0), (16, 2, 4, 0, 1), (8, 1, 4, 0, 1, 2)]:
             b.set_config(*cfg)
             got = b.render()
             assert ctx.stats().samples == ref_samples

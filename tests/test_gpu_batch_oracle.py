@@ -80,7 +80,7 @@ def test_batch_matches_oracle(ctx, c3_small, kw, gather):
         vol.set_gather_sampling(True)
     try:
         b.set_counting(True)
-        for cfg in [(8, 1, 4, 0, 1), (16, 2, 8, 0, 0)]:
+        for cfg in [(8, 1, 4, 0, 1), (16, 2, 8, 0, 0), (8, 1, 4, 0, 1, 2)]:
             b.set_config(*cfg)
             got = b.render()
             assert ctx.stats().samples == ref_samples, cfg
