@@ -61,6 +61,8 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sampler", choices=["gather", "loads"], default="gather",
                     help="Volume march over u8 bricks: texture gathers or loads")
+    ap.add_argument("--diff-views", type=int, default=16,
+                    help="diff workload: views of the fit (16; fewer for a small profiling case)")
     ap.add_argument("--ckpt-k", type=int, default=32,
                     help="diff workload: checkpoint interval of the differentiable march")
     ap.add_argument("--no-extra", action="store_true",
@@ -1206,7 +1208,7 @@ def main_diff(args):
     import hydrant_gb300 as hy
     from hydrant_gb300 import fit
 
-    n, res, nviews, ntf = 256, 512, 16, 32
+    n, res, nviews, ntf = 256, 512, args.diff_views, 32
     steps = args.frames if args.frames != 120 else 200
     ctx = hy.Context(local)
     vt = hy.synth_blobs_f32(4, (n, n, n), 24)
@@ -1221,7 +1223,7 @@ def main_diff(args):
     K = args.ckpt_k
     res_fit = fit.fit(ctx, vt, vi, views, res, res, tft, tfi, steps=steps, ckpt_k=K, warmup=warm)
     wall = time.perf_counter() - t0
-    kernels = diff_leg(hy, ctx, f"cuda:{local}", ckpt_k=K)
+    kernels = None if args.no_extra else diff_leg(hy, ctx, f"cuda:{local}", ckpt_k=K)
     out = {
         "metric": "fwd+adjoint ms/view", "value": res_fit.fwd_adj_ms_per_view, "unit": "ms/view",
         "n_gpus": 1, "steps": steps, "warmup": warm, "higher_is_better": False, "dtype": "f32",
