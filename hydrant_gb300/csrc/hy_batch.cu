@@ -51,36 +51,6 @@ constexpr int kMaxBlockThreads = 256;
 #define HY_BATCH_MIN_BLOCKS 4
 #endif
 
-// Shades one pixel of a batch view and stores its RGBA8 value.
-template <int SHADER, int PC, int DT, bool PADDED, int COMPOSITE, bool LEAN, bool GATHER, int LOOP>
-__device__ __forceinline__ long long shade_batch_pixel(const BatchArgs &B, const Shared &S,
-                                                       const BatchView &bv, int x, int y) {
-    const ShadeArgs &A = B.A;
-    if (x >= bv.view.W || y >= bv.view.H) return 0;
-    long long samples;
-    float ox, oy, oz, dx, dy, dz;
-    gen_ray(bv.view, x, y, ox, oy, oz, dx, dy, dz);
-    float4 v;
-    if (COMPOSITE) {
-        float4 aux;
-        samples = composite_ray<SHADER, PC, DT, PADDED>(A, bv.view, S, ox, oy, oz, dx, dy, dz, v,
-                                                        aux);
-    } else {
-        Px p;
-        samples = emit<SHADER, PC, DT, PADDED, LEAN, GATHER, LOOP>(p, A, bv.view, S, ox, oy, oz, dx, dy,
-                                                             dz, 0.f, 0.f, 0.f, A.bbox_max[0],
-                                                             A.bbox_max[1], A.bbox_max[2]);
-        v = make_float4(p.vx, p.vy, p.vz, p.vw);
-    }
-    uchar4 q;
-    if (v.w != 0.f)
-        q = make_uchar4(saturate_u8(v.x), saturate_u8(v.y), saturate_u8(v.z), saturate_u8(v.w));
-    else
-        q = make_uchar4(A.clear_u8[0], A.clear_u8[1], A.clear_u8[2], 0);
-    *reinterpret_cast<uchar4 *>(B.out + bv.out_off + (size_t(y) * bv.view.W + x) * 4) = q;
-    return samples;
-}
-
 __device__ __forceinline__ int find_view(const int *starts, int n, int t) {
     int lo = 0, hi = n - 1;  // last view with starts[v] <= t
     while (lo < hi) {
@@ -91,6 +61,72 @@ __device__ __forceinline__ int find_view(const int *starts, int n, int t) {
             hi = mid - 1;
     }
     return lo;
+}
+
+// The view and pixel of this thread in queue unit t (see batch_body).
+struct UnitPixel {
+    const BatchView *bv;
+    int x, y;
+};
+__device__ __forceinline__ UnitPixel unit_pixel(const BatchArgs &B, const int *starts, int t) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int lx = lane % B.tile_w, ly = lane / B.tile_w;
+    const int vi = find_view(starts, B.nviews, t);
+    const BatchView *bv = B.views + vi;
+    const int local = t - starts[vi];
+    const int uy = local / bv->tiles_x, ux = local - uy * bv->tiles_x;
+    if (B.block_queue) {
+        const int wx = warp % B.bx, wy = warp / B.bx;
+        return UnitPixel{bv, (ux * B.bx + wx) * B.tile_w + lx, (uy * B.by + wy) * B.tile_h + ly};
+    }
+    return UnitPixel{bv, ux * B.tile_w + lx, uy * B.tile_h + ly};
+}
+
+// Adds a unit's samples of the warp to the launch's counter (every lane of
+// the warp comes here together: the queue loops are warp-uniform).
+__device__ __forceinline__ void count_unit(const ShadeArgs &A, unsigned int n) {
+    unsigned long long s = n;
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0 && s) atomicAdd(A.counter, s);
+}
+
+// Shades this thread's pixel of queue unit t and stores its RGBA8 value.
+// The unit's view and pixel are found again after the march (the empty asm
+// with a memory clobber makes the compiler re-read them rather than hold the
+// view pointer and pixel coordinates in registers through the march).
+template <int SHADER, int PC, int DT, bool PADDED, int COMPOSITE, bool LEAN, bool GATHER, int LOOP>
+__device__ __forceinline__ unsigned int shade_batch_unit(const BatchArgs &B, const Shared &S,
+                                                         const int *starts, int t) {
+    const ShadeArgs &A = B.A;
+    unsigned int samples;
+    float4 v;
+    {
+        const UnitPixel u = unit_pixel(B, starts, t);
+        const BatchView &bv = *u.bv;
+        if (u.x >= bv.view.W || u.y >= bv.view.H) return 0;
+        float ox, oy, oz, dx, dy, dz;
+        gen_ray(bv.view, u.x, u.y, ox, oy, oz, dx, dy, dz);
+        if (COMPOSITE) {
+            float4 aux;
+            samples = unsigned(composite_ray<SHADER, PC, DT, PADDED>(A, bv.view, S, ox, oy, oz, dx,
+                                                                    dy, dz, v, aux));
+        } else {
+            Px p;
+            samples = unsigned(emit<SHADER, PC, DT, PADDED, LEAN, GATHER, LOOP>(
+                p, A, bv.view, S, ox, oy, oz, dx, dy, dz, 0.f, 0.f, 0.f, A.bbox_max[0],
+                A.bbox_max[1], A.bbox_max[2]));
+            v = make_float4(p.vx, p.vy, p.vz, p.vw);
+        }
+    }
+    asm volatile("" ::: "memory");
+    const UnitPixel u = unit_pixel(B, starts, t);
+    uchar4 q;
+    if (v.w != 0.f)
+        q = make_uchar4(saturate_u8(v.x), saturate_u8(v.y), saturate_u8(v.z), saturate_u8(v.w));
+    else
+        q = make_uchar4(A.clear_u8[0], A.clear_u8[1], A.clear_u8[2], 0);
+    *reinterpret_cast<uchar4 *>(B.out + u.bv->out_off + (size_t(u.y) * u.bv->view.W + u.x) * 4) = q;
+    return samples;
 }
 
 // Queue units: one warp tile per unit (block_queue == 0, each warp takes its
@@ -112,12 +148,9 @@ __device__ __forceinline__ void batch_body(const BatchArgs &B) {
     for (int i = threadIdx.x; i < 256; i += blockDim.x) lut[i] = float(i) / 255.f;
     for (int i = threadIdx.x; i < B.nviews; i += blockDim.x) starts[i] = B.starts[i];
     __syncthreads();
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
     const Shared S{tf, A.ntf, float(A.ntf), lut};
-    const int lx = lane % B.tile_w, ly = lane / B.tile_w;
-    long long samples = 0;
     if (B.block_queue) {
-        const int wx = warp % B.bx, wy = warp / B.bx;
         for (;;) {
             if (threadIdx.x == 0) s_t0 = atomicAdd(B.queue, unsigned(B.grab));
             __syncthreads();
@@ -127,14 +160,9 @@ __device__ __forceinline__ void batch_body(const BatchArgs &B) {
             for (int g = 0; g < B.grab; ++g) {
                 const int t = int(t0) + g;
                 if (t >= B.total_tiles) break;
-                const int vi = find_view(starts, B.nviews, t);
-                const BatchView &bv = B.views[vi];
-                const int local = t - starts[vi];
-                const int uy = local / bv.tiles_x, ux = local - uy * bv.tiles_x;
-                const int x = (ux * B.bx + wx) * B.tile_w + lx;
-                const int y = (uy * B.by + wy) * B.tile_h + ly;
-                samples +=
-                    shade_batch_pixel<SHADER, PC, DT, PADDED, COMPOSITE, LEAN, GATHER, LOOP>(B, S, bv, x, y);
+                const unsigned int n =
+                    shade_batch_unit<SHADER, PC, DT, PADDED, COMPOSITE, LEAN, GATHER, LOOP>(B, S, starts, t);
+                if (A.count) count_unit(A, n);
             }
         }
     } else {
@@ -146,19 +174,11 @@ __device__ __forceinline__ void batch_body(const BatchArgs &B) {
             for (int g = 0; g < B.grab; ++g) {
                 const int t = int(t0) + g;
                 if (t >= B.total_tiles) break;
-                const int vi = find_view(starts, B.nviews, t);
-                const BatchView &bv = B.views[vi];
-                const int local = t - starts[vi];
-                const int ty = local / bv.tiles_x, tx = local - ty * bv.tiles_x;
-                samples += shade_batch_pixel<SHADER, PC, DT, PADDED, COMPOSITE, LEAN, GATHER, LOOP>(
-                    B, S, bv, tx * B.tile_w + lx, ty * B.tile_h + ly);
+                const unsigned int n =
+                    shade_batch_unit<SHADER, PC, DT, PADDED, COMPOSITE, LEAN, GATHER, LOOP>(B, S, starts, t);
+                if (A.count) count_unit(A, n);
             }
         }
-    }
-    if (A.count) {
-        unsigned long long s = (unsigned long long)samples;
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-        if (lane == 0 && s) atomicAdd(A.counter, s);
     }
 }
 
@@ -177,9 +197,10 @@ __global__ void __launch_bounds__(kMaxBlockThreads, HY_BATCH_MIN_BLOCKS)
 #ifndef HY_BATCH_LEAN_REGS
 #define HY_BATCH_LEAN_REGS 56
 #endif
-// The lean march sampling by texture gathers: 56 registers (88 bytes
-// spilled) for 36 resident warps.  64-view step: 175.8 ms, against 187.9 at
-// 64 registers, 176.1 at 48 and 179.6 for the loads at 56.
+// The lean march sampling by texture gathers: 56 registers (no spills once
+// the unit's view and pixel are re-derived after the march) for 36 resident
+// warps.  64-view step: 171.5 ms, against 183.9 at 64 registers, 172.9 at 48
+// and 176.6 for the loads at 56.
 #ifndef HY_BATCH_GATHER_REGS
 #define HY_BATCH_GATHER_REGS 56
 #endif
