@@ -60,18 +60,19 @@ __device__ __forceinline__ void render_body(const ShadeArgs &A) {
     const Shared S{tf, A.ntf, float(A.ntf), lut};
     int x, y;
     tile_xy(x, y);
-    long long samples = 0;
+    unsigned int samples = 0;  // one ray: at most max_steps (+ 6 at a hit) samples
     if (x < A.view.W && y < A.view.H) {
         float ox, oy, oz, dx, dy, dz;
         gen_ray(A.view, x, y, ox, oy, oz, dx, dy, dz);
         float4 v, aux;
         if (COMPOSITE) {
-            samples = composite_ray<SHADER, PC, DT, PADDED>(A, A.view, S, ox, oy, oz, dx, dy, dz, v, aux);
+            samples = unsigned(
+                composite_ray<SHADER, PC, DT, PADDED>(A, A.view, S, ox, oy, oz, dx, dy, dz, v, aux));
         } else {
             Px p;
-            samples = emit<SHADER, PC, DT, PADDED, LEAN, GATHER, LOOP>(
+            samples = unsigned(emit<SHADER, PC, DT, PADDED, LEAN, GATHER, LOOP>(
                 p, A, A.view, S, ox, oy, oz, dx, dy, dz, 0.f, 0.f, 0.f, A.bbox_max[0],
-                A.bbox_max[1], A.bbox_max[2]);
+                A.bbox_max[1], A.bbox_max[2]));
             v = make_float4(p.vx, p.vy, p.vz, p.vw);
             if (SHADER == HY_SHADER_VOLUME)
                 aux = make_float4(p.e0, p.e1, p.e2, p.e3);
@@ -79,6 +80,12 @@ __device__ __forceinline__ void render_body(const ShadeArgs &A) {
                 aux = make_float4(p.e3, 0.f, 0.f, 0.f);
             else
                 aux = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        if constexpr (LEAN) {
+            // the pixel again from the thread's index, not held through the
+            // march (the memory clobber keeps the compiler from carrying it)
+            asm volatile("" ::: "memory");
+            tile_xy(x, y);
         }
         const size_t idx = size_t(y) * A.view.W + x;
         A.rgba[idx] = quantise(A, v);
@@ -91,6 +98,24 @@ __device__ __forceinline__ void render_body(const ShadeArgs &A) {
 template <int SHADER, int PC, int DT, bool PADDED, int COMPOSITE, bool LEAN, int LOOP = kLoopOne>
 __global__ void __launch_bounds__(kThreads) render_kernel(const __grid_constant__ ShadeArgs A) {
     render_body<SHADER, PC, DT, PADDED, COMPOSITE, LEAN, false, LOOP>(A);
+}
+
+// The lean march of the per-view path with its own register budget
+// (HY_RENDER_LEAN_REGS, 0: the compiler's choice, 56 registers).  64-view
+// step, one launch per view: 56 registers 199.7 ms, 48 (8 bytes spilled)
+// 211.7 ms, 40 269.0 ms -- unlike the batched kernel, more resident warps
+// do not pay here.
+#ifndef HY_RENDER_LEAN_REGS
+#define HY_RENDER_LEAN_REGS 0
+#endif
+#if HY_RENDER_LEAN_REGS > 0
+#define HY_RENDER_LEAN_BOUNDS __maxnreg__(HY_RENDER_LEAN_REGS)
+#else
+#define HY_RENDER_LEAN_BOUNDS __launch_bounds__(kThreads)
+#endif
+template <int SHADER, int PC, int DT, bool PADDED, int LOOP>
+__global__ void HY_RENDER_LEAN_BOUNDS render_lean_kernel(const __grid_constant__ ShadeArgs A) {
+    render_body<SHADER, PC, DT, PADDED, 0, true, false, LOOP>(A);
 }
 
 
@@ -267,10 +292,11 @@ void launch_fused(const ShadeArgs &a, cudaStream_t s) {
             // slower, 177.0 vs 186.5 Gsamples/s on the 64-view step)
             const bool ert = a.ert > 0.f;
             if (ert)
-                render_kernel<SHADER, PC, DT, PADDED, 0, true, kLoopErt>
+                render_lean_kernel<SHADER, PC, DT, PADDED, kLoopErt>
                     <<<grid_of(a), kThreads, smem_bytes(a), s>>>(a);
             else
-                render_kernel<SHADER, PC, DT, PADDED, 0, true><<<grid_of(a), kThreads, smem_bytes(a), s>>>(a);
+                render_lean_kernel<SHADER, PC, DT, PADDED, kLoopOne>
+                    <<<grid_of(a), kThreads, smem_bytes(a), s>>>(a);
             return;
         }
     }
