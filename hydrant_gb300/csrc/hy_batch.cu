@@ -111,7 +111,7 @@ __device__ __forceinline__ unsigned int shade_batch_unit(const BatchArgs &B, con
         gen_ray(bv.view, u.x, u.y, ox, oy, oz, dx, dy, dz);
         if (COMPOSITE) {
             float4 aux;
-            samples = unsigned(composite_ray<SHADER, PC, DT, PADDED>(A, bv.view, S, ox, oy, oz, dx,
+            samples = unsigned(composite_ray<SHADER, PC, DT, PADDED, GATHER>(A, bv.view, S, ox, oy, oz, dx,
                                                                     dy, dz, v, aux));
         } else {
             Px p;
@@ -187,10 +187,10 @@ __device__ __forceinline__ void batch_body(const BatchArgs &B) {
     }
 }
 
-template <int SHADER, int PC, int DT, bool PADDED, int COMPOSITE>
+template <int SHADER, int PC, int DT, bool PADDED, int COMPOSITE, bool GATHER = false>
 __global__ void __launch_bounds__(kMaxBlockThreads, HY_BATCH_MIN_BLOCKS)
     batch_kernel(const __grid_constant__ BatchArgs B) {
-    batch_body<SHADER, PC, DT, PADDED, COMPOSITE, false>(B);
+    batch_body<SHADER, PC, DT, PADDED, COMPOSITE, false, GATHER>(B);
 }
 
 // The lean march over u8 bricks with an apron holds its state in 56
@@ -206,6 +206,13 @@ __global__ void __launch_bounds__(kMaxBlockThreads, HY_BATCH_MIN_BLOCKS)
 // the unit's view and pixel are re-derived after the march) for 36 resident
 // warps.  64-view step: 171.5 ms, against 183.9 at 64 registers, 172.9 at 48
 // and 176.6 for the loads at 56.
+// The Volume shader's per-brick compositing in the batch samples by
+// gathers (1) or loads (0).  Loads: at the kernel's 64 registers the
+// gathers spill 148 bytes (loads 32) and the 64-view composite step takes
+// 337.6 vs 312.7 ms.
+#ifndef HY_BATCH_COMPOSITE_GATHER
+#define HY_BATCH_COMPOSITE_GATHER 0
+#endif
 #ifndef HY_BATCH_GATHER_REGS
 #define HY_BATCH_GATHER_REGS 56
 #endif
@@ -232,8 +239,14 @@ const void *pick_lean(const ShadeArgs &a, int steps_per_iter) {
 
 template <int SHADER, int PC, int DT, bool PADDED>
 const void *pick_c(const ShadeArgs &a, int steps_per_iter) {
-    if (a.composite)
+    if (a.composite) {
+        // the Volume shader's per-brick segments sample by gathers too
+        if constexpr (SHADER == HY_SHADER_VOLUME && DT == HY_DTYPE_U8 && PADDED) {
+            if (a.vol.tex && HY_BATCH_COMPOSITE_GATHER)
+                return reinterpret_cast<const void *>(&batch_kernel<SHADER, PC, DT, PADDED, 1, true>);
+        }
         return reinterpret_cast<const void *>(&batch_kernel<SHADER, PC, DT, PADDED, 1>);
+    }
     if constexpr (SHADER == HY_SHADER_VOLUME) {
         if (a.mode == HY_VOLUME_DEFAULT) {
             if constexpr (DT == HY_DTYPE_U8 && PADDED) {

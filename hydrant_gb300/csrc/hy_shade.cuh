@@ -939,7 +939,7 @@ __device__ __forceinline__ float vol_linear_to_srgb(float x) {  // volume.cc:175
 // per-partition bbox of dbuf_renderer.hpp:38-40) and the partials are
 // composited front to back with volume.cc:267-280 (Volume),
 // isosurface.cc:272-290 (depth-min, Isosurface) or the over operator (Blocks).
-template <int SHADER, int PC, int DT, bool PADDED>
+template <int SHADER, int PC, int DT, bool PADDED, bool GATHER = false>
 __device__ __forceinline__ long long composite_ray(const ShadeArgs &A, const ViewArgs &Vw,
                                                    const Shared &S, float ox,
                                                    float oy, float oz, float dx, float dy,
@@ -989,8 +989,9 @@ __device__ __forceinline__ long long composite_ray(const ShadeArgs &A, const Vie
         if (__ldg(&V.info[bid].x) == 0) {
             const float bx = float(cell[0]), by = float(cell[1]), bz = float(cell[2]);
             Px p;
-            samples += emit<SHADER, PC, DT, PADDED>(p, A, Vw, S, ox, oy, oz, dx, dy, dz, bx, by, bz, bx + 1.f,
-                                            by + 1.f, bz + 1.f);
+            samples += emit<SHADER, PC, DT, PADDED, false, GATHER>(p, A, Vw, S, ox, oy, oz, dx, dy, dz,
+                                                                   bx, by, bz, bx + 1.f, by + 1.f,
+                                                                   bz + 1.f);
             if (SHADER == HY_SHADER_VOLUME) {
                 if (first) {
                     acc = make_float4(p.vx, p.vy, p.vz, p.vw);
