@@ -93,19 +93,34 @@ def test_batch_matches_oracle(ctx, c3_small, kw, gather):
 
 
 def test_gather_sampling_where_it_applies(ctx):
-    """Gather textures are built for u8 volumes with an apron (and a brick
-    column that fits a gather texture); f32 and apron-less volumes sample
-    by loads.  Switching it off and on is honoured."""
+    """Gather textures are built for u8 volumes with an apron and a brick
+    column that fits a gather texture (P^2 rows: P = 202 does not); f32,
+    apron-less and too-tall bricks sample by loads, and render as the oracle
+    does.  Switching it off and on is honoured."""
     u8 = hy.Volume(ctx, hy.synth_blobs_u8(1, (70, 40, 50), 6), 16, 1)
     f32 = hy.Volume(ctx, hy.synth_blobs_f32(1, (40, 40, 40), 6), 16, 1)
     bare = hy.Volume(ctx, hy.synth_blobs_u8(1, (40, 40, 40), 6), 16, 0)
+    big_vox = hy.synth_blobs_u8(2, (210, 60, 50), 6)
+    big = hy.Volume(ctx, big_vox, 200, 1)
     try:
         assert u8.gather_sampling
-        assert not f32.gather_sampling and not bare.gather_sampling
+        assert not f32.gather_sampling and not bare.gather_sampling and not big.gather_sampling
+        ctx.set_transfer_fn(wl.TF9)
+        ov = orc.OracleVolume(big_vox, 200, 1)
+        p = hy.shader_params(shader="Volume", density=0.5, sample_rate=0.5)
+        cam = wl.make_camera(wl.Camera("orbit", (30.0, 20.0, 2.4)))
+        view = hy.camera_view(big, cam)
+        b = hy.Batch(ctx, big, p, [(view, 40, 30)])
+        try:
+            got = b.render()[0]
+        finally:
+            b.close()
+        ref = orc.render(ov, wl.TF9, orc.params_from(p), view_array(view), 40, 30)["rgba"]
+        assert np.abs(got.astype(int) - ref.astype(int)).max() <= LSB_TOL
         u8.set_gather_sampling(False)
         assert not u8.gather_sampling
         u8.set_gather_sampling(True)
         assert u8.gather_sampling
     finally:
-        for v in (u8, f32, bare):
+        for v in (u8, f32, bare, big):
             v.close()
