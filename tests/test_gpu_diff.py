@@ -115,3 +115,46 @@ def test_checkpoint_interval_does_not_change_gradients(ctx, setup, k):
     assert np.array_equal(out[0][0], out[1][0])
     for a, b in ((out[0][1], out[1][1]), (out[0][2], out[1][2])):
         assert np.linalg.norm(a - b) <= 1e-4 * np.linalg.norm(a), np.linalg.norm(a - b)
+
+
+def test_adjoint_matches_finite_differences_at_k32(ctx):
+    """The configuration's checkpoint interval (K = 32) on a mid-size case
+    (64^3 f32, 4 views of 96^2, 32 knots): the adjoint's gradient of the mean
+    squared image error against central finite differences (eps 1e-3, loss in
+    float64) on the largest knot and voxel gradients, within 1e-3 relative
+    in L2 over the checked set and 3e-3 for any one of them (the difference
+    quotient carries the f32 rounding of the images)."""
+    torch = pytest.importorskip("torch")
+    n, res, ntf = 64, 96, 32
+    vt = hy.synth_blobs_f32(4, (n, n, n), 12)
+    vi = hy.synth_blobs_f32(5, (n, n, n), 12)
+    holder = hy.Volume(ctx, vt, n, 1)
+    views = fit.orbit_views(holder, 4, 4)
+    holder.close()
+    tft = fit.seeded_tf(4, ntf)
+    r = fit.DiffRenderer(ctx, n, views, res, res, ntf, ckpt_k=32)
+    target = r.forward(torch.from_numpy(vt).cuda(), torch.from_numpy(tft).cuda(), keep=False).clone()
+    vol = torch.from_numpy(vi).cuda()
+    tf = torch.from_numpy(np.clip(tft * 0.8 + 0.1, 0, 1).astype(np.float32)).cuda()
+    img = r.forward(vol, tf)
+    g = (2.0 / img.numel()) * (img - target)
+    dv, dt = r.backward(vol, tf, g.contiguous())
+    torch.cuda.synchronize()
+
+    def loss(v, t):
+        im = r.forward(v, t, keep=False)
+        torch.cuda.synchronize()
+        return float(((im.double() - target.double()) ** 2).mean())
+
+    eps, pairs = 1e-3, []
+    for grad, base, is_tf in ((dt, tf, True), (dv, vol, False)):
+        for idx in torch.topk(grad.reshape(-1).abs(), 4).indices.tolist():
+            p, m = base.clone(), base.clone()
+            p.view(-1)[idx] += eps
+            m.view(-1)[idx] -= eps
+            fd = (loss(vol, p) - loss(vol, m)) if is_tf else (loss(p, tf) - loss(m, tf))
+            pairs.append((float(grad.reshape(-1)[idx]), fd / (2 * eps)))
+    a = np.array([x for x, _ in pairs])
+    f = np.array([y for _, y in pairs])
+    assert np.linalg.norm(a - f) <= 1e-3 * np.linalg.norm(f), (a, f)
+    assert np.max(np.abs(a - f) / np.abs(f)) <= 3e-3, (a, f)
