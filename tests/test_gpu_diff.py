@@ -78,7 +78,7 @@ def test_adjoint_matches_fp64_gradient(setup):
 def test_autograd_and_adam(ctx, setup):
     torch = setup["torch"]
     res = fit.fit(ctx, setup["vt"], setup["vi"], setup["views"], W, H, setup["tft"], setup["tfi"],
-                  steps=30, ckpt_k=8)
+                  steps=30, ckpt_k=8, lr_tf=2e-2, lr_vol=1e-2)
     assert res.losses[-1] < 0.5 * res.losses[0], res.losses[::5]
     # autograd gradients equal the direct backward call
     r = setup["r"]
