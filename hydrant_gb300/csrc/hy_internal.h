@@ -54,6 +54,10 @@ struct DevVolume {
     const TexEntry *tex;
     unsigned long long gtex[kMaxGatherTextures];  // cudaTextureObject_t
     float map_k, map_b;  // BlockSamplerMapping of every resident brick (with `tex`)
+    // with `tex`: per brick {chebyshev, registry id or -1, texel column x0,
+    // texel row y0 | texture << 30}: the page table and the brick's place in
+    // its gather texture in one 16-byte load
+    const int4 *info4;
 };
 
 // Per-view inputs: ViewArgs (shader.hpp:63-68) plus the image size and the
@@ -145,6 +149,7 @@ struct hy_volume {
     std::vector<cudaArray_t> atlas;
     std::vector<unsigned long long> atlas_tex;
     hy::TexEntry *tex_dev = nullptr;
+    int4 *info4_dev = nullptr;
     bool tex_sampling = true;  // hy_volume_set_gather_sampling
 };
 

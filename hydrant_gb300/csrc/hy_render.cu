@@ -383,7 +383,7 @@ int hy_fill_args(hy_ctx *ctx, const hy_volume *vol, const hy_shader_params *p, c
     std::memset(a, 0, sizeof(*a));
     a->vol = DevVolume{vol->pool, vol->info_dev, vol->reg_dev, vol->mean_dev, vol->grid[0],
                        vol->grid[1], vol->grid[2], vol->P, vol->desc.dtype, vol->desc.padding,
-                       nullptr, {0ull, 0ull}, vol->k, vol->b};
+                       nullptr, {0ull, 0ull}, vol->k, vol->b, nullptr};
     hy_volume_gather_view(vol, &a->vol);
     for (int i = 0; i < 3; ++i) a->bbox_max[i] = vol->bbox_max[i];
     a->du = vol->du;

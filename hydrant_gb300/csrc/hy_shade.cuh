@@ -466,11 +466,23 @@ struct BrickCursor {
         const int bid = thumb_index(V, fgx, fgy, fgz, ipx, ipy, ipz);
         if (bid != cur) {
             cur = bid;
-            const int2 in = __ldg(&V.info[bid]);
-            cd = in.x;
-            pg = in.y;
-            sample = cd == 0 && pg != -1;
-            if (cd == 0 && pg >= 0) br = load_brick<GATHER>(V, pg);
+            if constexpr (GATHER) {
+                // page table and texel origin in one load (no dependent
+                // second load of the brick's gather-table entry)
+                const int4 in = __ldg(&V.info4[bid]);
+                cd = in.x;
+                pg = in.y;
+                sample = cd == 0 && pg != -1;
+                br.tx = float(in.z);
+                br.ty = float(in.w & 0x3fffffff);
+                br.which = in.w >> 30;
+            } else {
+                const int2 in = __ldg(&V.info[bid]);
+                cd = in.x;
+                pg = in.y;
+                sample = cd == 0 && pg != -1;
+                if (cd == 0 && pg >= 0) br = load_brick<GATHER>(V, pg);
+            }
         }
     }
     // brick-local coordinates of o, relocating first when o left the cell

@@ -220,9 +220,11 @@ void free_gather(hy_volume *v) {
     for (auto t : v->atlas_tex) cudaDestroyTextureObject(cudaTextureObject_t(t));
     for (auto a : v->atlas) cudaFreeArray(a);
     if (v->tex_dev) cudaFree(v->tex_dev);
+    if (v->info4_dev) cudaFree(v->info4_dev);
     v->atlas_tex.clear();
     v->atlas.clear();
     v->tex_dev = nullptr;
+    v->info4_dev = nullptr;
 }
 
 int build_gather(hy_volume *vol) {
@@ -272,9 +274,24 @@ int build_gather(hy_volume *vol) {
                                        int(vol->atlas_tex.size()) - 1, 0};
         }
     }
+    // the page table with each resident brick's texel origin beside it
+    std::vector<int4> info4(vol->nbricks);
+    for (int b = 0; b < vol->nbricks; ++b) {
+        const int reg = vol->reg_of_brick[b];
+        int4 q = make_int4(vol->cheb[b], reg, 0, 0);
+        if (reg >= 0) {
+            q.z = int(table[reg].x0);
+            q.w = int(table[reg].y0) | (table[reg].which << 30);
+        }
+        info4[b] = q;
+    }
     cudaError_t e = cudaMalloc(&vol->tex_dev, size_t(n) * sizeof(hy::TexEntry));
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(vol->tex_dev, table.data(), size_t(n) * sizeof(hy::TexEntry),
+                            cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMalloc(&vol->info4_dev, size_t(vol->nbricks) * sizeof(int4));
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(vol->info4_dev, info4.data(), size_t(vol->nbricks) * sizeof(int4),
                             cudaMemcpyHostToDevice, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) {
@@ -461,6 +478,7 @@ const hy::TexEntry *hy_volume_gather_table(const hy_volume *v) {
 
 void hy_volume_gather_view(const hy_volume *v, hy::DevVolume *dv) {
     dv->tex = hy_volume_gather_table(v);
+    dv->info4 = dv->tex ? v->info4_dev : nullptr;
     for (int i = 0; i < hy::kMaxGatherTextures; ++i)
         dv->gtex[i] = (dv->tex && i < int(v->atlas_tex.size())) ? v->atlas_tex[i] : 0ull;
 }
