@@ -530,3 +530,68 @@ def test_prefetch_during_the_previous_frame(ctx, tubes, policy):
     pre = run(True)
     assert plain["prefetched"] == 0 and pre["prefetched"] > 0
     assert pre["misses"] < plain["misses"], (pre["misses"], plain["misses"])
+
+
+def test_out_of_core_orbit_at_quarter_scale_matches_oracle(ctx):
+    """The out-of-core configuration at a quarter of its edge: a
+    1024x1024x512 noise volume (3 octaves, 64-voxel cells, 15 % occupancy)
+    in 64^3 bricks with the level-3 coarse fallback, a realtime LRU cache of
+    a third of the visible bricks, 512^2 frames along the orbit (+3 degrees
+    per frame), density 5e-3.  The oracle holds the same volume (assembled
+    from the store's bricks, its own bricking, thumbnails and coarse level
+    must equal the store's) and renders every 8th row of the frames with the
+    pager's resident set."""
+    torch = pytest.importorskip("torch")
+    dim, bs = (1024, 1024, 512), 64
+    store = hy.Store.noise(ctx, dim, bs, 1, seed=2, cell_voxels=64.0, occupancy=0.15)
+    try:
+        store.build_coarse(3)
+        info = store.info
+        gx, gy, gz = info.grid
+        raw = np.zeros((dim[2], dim[1], dim[0]), np.uint8)
+        for b in range(info.nbricks):
+            x, y, z = b % gx, (b // gx) % gy, b // (gx * gy)
+            raw[z * bs:(z + 1) * bs, y * bs:(y + 1) * bs, x * bs:(x + 1) * bs] = \
+                store.brick(b)[1:bs + 1, 1:bs + 1, 1:bs + 1]
+        ov = orc.OracleVolume(raw, bs, 1)
+        ov.build_coarse(3)
+        del raw
+        cheb, mean = store.thumbnails()
+        ocheb, omean = ov.thumbnails()
+        assert np.array_equal(cheb.reshape(-1), ocheb.reshape(-1))
+        cg = store.coarse_grid
+        for cb in range(0, cg[0] * cg[1] * cg[2], 7):
+            got = store.coarse_brick(cb).astype(np.float32) / np.float32(255)
+            np.testing.assert_array_equal(got, ov.coarse_brick(cb))
+        ctx.set_transfer_fn(wl.TF9)
+        res = 512
+        path = [hy.camera_orbit((3.0 * f, 30.0, 2.2)) for f in range(6)]
+        _, most = hy.Pager.tune_slots(ctx, store, path, 1 << 40)
+        slots = max(16, most // 3)
+        pg = hy.Pager(ctx, store, slots, _abi.PAGER_REALTIME, 0, _abi.EVICT_LRU)
+        p = hy.shader_params(shader="Volume", sample_rate=0.25, density=5e-3)
+        out = torch.zeros(res * res * 4, dtype=torch.uint8, device="cuda")
+        try:
+            vol = pg.volume
+            for f, cam in enumerate(path):
+                pg.render(p, cam, res, res, out.data_ptr())
+                if f + 1 < len(path):
+                    pg.prefetch(path[f + 1])
+                ctx.synchronize()
+                st = pg.stats()
+                if f in (0, len(path) - 1):
+                    assert st["fallback"] > 0  # the coarse level is in use
+                    ov.set_present(pg.present())
+                    op = orc.params_from(p)
+                    op.lowest_blkcnt = ov.lowest_blkcnt
+                    view = view_array(hy.camera_view(vol, cam))
+                    ref = orc.render_row_step(ov, wl.TF9, op, view, res, res, 4, 8)["rgba"]
+                    got = out.cpu().numpy().reshape(res, res, 4)
+                    d = np.abs(got[4::8].astype(int) - ref[4::8].astype(int)).max()
+                    assert d <= 1, f"frame {f}: {d} LSB"
+                    assert got[4::8, :, 3].any()
+        finally:
+            ov.set_present(np.ones(gx * gy * gz, np.uint8))
+            pg.close()
+    finally:
+        store.close()
