@@ -154,7 +154,7 @@ __device__ __forceinline__ void batch_body(const BatchArgs &B) {
     for (int i = threadIdx.x; i < B.nviews; i += blockDim.x) starts[i] = B.starts[i];
     __syncthreads();
     const int lane = threadIdx.x & 31;
-    const Shared S{tf, A.ntf, float(A.ntf), lut};
+    const Shared S = make_shared(tf, A.ntf, lut);
     if (B.block_queue) {
         for (;;) {
             if (threadIdx.x == 0) s_t0 = atomicAdd(B.queue, unsigned(B.grab));
@@ -202,10 +202,10 @@ __global__ void __launch_bounds__(kMaxBlockThreads, HY_BATCH_MIN_BLOCKS)
 #ifndef HY_BATCH_LEAN_REGS
 #define HY_BATCH_LEAN_REGS 56
 #endif
-// The lean march sampling by texture gathers: 56 registers (no spills once
-// the unit's view and pixel are re-derived after the march) for 36 resident
-// warps.  64-view step: 171.5 ms, against 183.9 at 64 registers, 172.9 at 48
-// and 176.6 for the loads at 56.
+// The lean march sampling by texture gathers: 48 registers (8 bytes spill)
+// for 40 resident warps.  64-view step: 148.2 ms, against 151.1 at 56
+// registers (no spills, 36 warps) and 173.1 at 40 (168 bytes spill, 48
+// warps).
 // The Volume shader's per-brick compositing in the batch samples by
 // gathers (1) or loads (0).  Loads: at the kernel's 64 registers the
 // gathers spill 148 bytes (loads 32) and the 64-view composite step takes
@@ -214,7 +214,7 @@ __global__ void __launch_bounds__(kMaxBlockThreads, HY_BATCH_MIN_BLOCKS)
 #define HY_BATCH_COMPOSITE_GATHER 0
 #endif
 #ifndef HY_BATCH_GATHER_REGS
-#define HY_BATCH_GATHER_REGS 56
+#define HY_BATCH_GATHER_REGS 48
 #endif
 template <int DT, bool PADDED, bool GATHER>
 constexpr int lean_regs() {
@@ -770,10 +770,18 @@ extern "C" int hy_render_views_noalloc(hy_ctx *ctx, const hy_volume *vol,
     int rc = hy_fill_args(ctx, vol, params, nullptr, 1, 1, &base);
     if (rc) return rc;
     base.count = 0;  // sample counting is not available on this entry point
+    HY_CUDA(ctx, cudaSetDevice(ctx->device));
+    // The descriptors are copied from this call's stack: a captured copy
+    // would replay from a dead address, so capture is refused.
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    HY_CUDA(ctx, cudaStreamIsCapturing(ctx->stream, &cap));
+    if (cap != cudaStreamCaptureStatusNone)
+        return hy_fail(ctx, HY_ERR_STATE,
+                       "noalloc: the stream is capturing (view descriptors are copied from "
+                       "host stack memory; call it outside capture)");
     unsigned char *scratch = nullptr;
     rc = noalloc_scratch(ctx, &scratch);
     if (rc) return rc;
-    HY_CUDA(ctx, cudaSetDevice(ctx->device));
 
     // default launch shape: 8x4 warp tiles, block tiles of 2x2 warp tiles,
     // one block tile per queue access

@@ -37,6 +37,23 @@ static_assert(sizeof(TexEntry) == 16, "TexEntry is one 16-byte load");
 // texture (a per-brick handle in a register would make the compiler
 // serialise the gather over the distinct handles of a warp).
 constexpr int kMaxGatherTextures = 2;
+#ifdef __CUDACC__
+// One gather of component 0 (texture unit tld4): the four texels of the
+// footprint (x - 1/2 .. x + 1/2, y - 1/2 .. y + 1/2) in the order
+// w = (x0, y0), z = (x1, y0), x = (x0, y1), y = (x1, y1).  The march and the
+// per-device gather check both call this, so the order they rely on is the
+// order checked.  Written as the PTX instruction: through tex2Dgather the
+// compiler kept a march's two textures as divergent branches around their
+// gathers; with the bare instruction it predicates both (64-view step
+// 156.9 vs 170.1 ms).
+__device__ __forceinline__ float4 gather_r(unsigned long long t, float x, float y) {
+    float4 g;
+    asm("tld4.r.2d.v4.f32.f32 {%0, %1, %2, %3}, [%4, {%5, %6}];"
+        : "=f"(g.x), "=f"(g.y), "=f"(g.z), "=f"(g.w)
+        : "l"(t), "f"(x), "f"(y));
+    return g;
+}
+#endif
 
 // Device view of a volume: the brick pool, the page table + chebyshev
 // thumbnail packed per brick as int2 {chebyshev, registry id or -1}, the
@@ -54,10 +71,14 @@ struct DevVolume {
     const TexEntry *tex;
     unsigned long long gtex[kMaxGatherTextures];  // cudaTextureObject_t
     float map_k, map_b;  // BlockSamplerMapping of every resident brick (with `tex`)
-    // with `tex`: per brick {chebyshev, registry id or -1, texel column x0,
-    // texel row y0 | texture << 30}: the page table and the brick's place in
-    // its gather texture in one 16-byte load
+    // with `tex`: per brick {chebyshev, registry id or -1, texel column x0
+    // (float bits), texel row y0 (float bits, negated -- -0 for 0 -- in
+    // texture 1)}: the page table and the brick's place in its gather
+    // texture in one 16-byte load
     const int4 *info4;
+    // the thumbnail grid as floats: g - 1 per axis (the clamp bounds) and
+    // gx, gy (the index strides); exact, nbricks <= 2^24
+    float gmx, gmy, gmz, fgx, fgy;
 };
 
 // Per-view inputs: ViewArgs (shader.hpp:63-68) plus the image size and the

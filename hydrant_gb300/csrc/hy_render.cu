@@ -57,7 +57,7 @@ __device__ __forceinline__ void render_body(const ShadeArgs &A) {
     float4 *tf = smem;
     float *lut = reinterpret_cast<float *>(smem + A.ntf + kTfPad);
     load_shared(A, tf, lut);
-    const Shared S{tf, A.ntf, float(A.ntf), lut};
+    const Shared S = make_shared(tf, A.ntf, lut);
     int x, y;
     tile_xy(x, y);
     unsigned int samples = 0;  // one ray: at most max_steps (+ 6 at a hit) samples
@@ -184,7 +184,7 @@ __global__ void __launch_bounds__(kThreads) emit_pass_kernel(const __grid_consta
     float4 *tf = smem;
     float *lut = reinterpret_cast<float *>(smem + A.ntf + kTfPad);
     load_shared(A, tf, lut);
-    const Shared S{tf, A.ntf, float(A.ntf), lut};
+    const Shared S = make_shared(tf, A.ntf, lut);
     int x, y;
     tile_xy(x, y);
     long long samples = 0;
@@ -206,7 +206,7 @@ __global__ void __launch_bounds__(kThreads) march_pass_kernel(const __grid_const
     float4 *tf = smem;
     float *lut = reinterpret_cast<float *>(smem + A.ntf + kTfPad);
     load_shared(A, tf, lut);
-    const Shared S{tf, A.ntf, float(A.ntf), lut};
+    const Shared S = make_shared(tf, A.ntf, lut);
     int x, y;
     tile_xy(x, y);
     long long samples = 0;
@@ -384,6 +384,11 @@ int hy_fill_args(hy_ctx *ctx, const hy_volume *vol, const hy_shader_params *p, c
     a->vol = DevVolume{vol->pool, vol->info_dev, vol->reg_dev, vol->mean_dev, vol->grid[0],
                        vol->grid[1], vol->grid[2], vol->P, vol->desc.dtype, vol->desc.padding,
                        nullptr, {0ull, 0ull}, vol->k, vol->b, nullptr};
+    a->vol.gmx = float(vol->grid[0] - 1);
+    a->vol.gmy = float(vol->grid[1] - 1);
+    a->vol.gmz = float(vol->grid[2] - 1);
+    a->vol.fgx = float(vol->grid[0]);
+    a->vol.fgy = float(vol->grid[1]);
     hy_volume_gather_view(vol, &a->vol);
     for (int i = 0; i < 3; ++i) a->bbox_max[i] = vol->bbox_max[i];
     a->du = vol->du;

@@ -87,13 +87,15 @@ __device__ __forceinline__ bool intersect(float ox, float oy, float oz, float rx
 
 // Thumbnail / page-table lookup: non-normalised nearest texel with Clamp
 // (cpu_sampler.hpp:142-166, filter_none 72-76).  ip is integral and the
-// clamp bounds are integers, so floor() after the float clamp is the identity.
-__device__ __forceinline__ int thumb_index(const DevVolume &V, float fgx, float fgy, float fgz,
-                                           float ipx, float ipy, float ipz) {
-    int x = iclamp(int(fclamp(ipx, 0.f, fgx)), 0, V.gx - 1);
-    int y = iclamp(int(fclamp(ipy, 0.f, fgy)), 0, V.gy - 1);
-    int z = iclamp(int(fclamp(ipz, 0.f, fgz)), 0, V.gz - 1);
-    return (z * V.gy + y) * V.gx + x;
+// clamp bounds are integers, so floor() after the clamp is the identity.
+// In float arithmetic with one conversion at the end: fmaxf(ip, 0) maps NaN
+// to 0 (as the integer conversion of NaN does), clamping to [0, g - 1]
+// equals clamping to [0, g] and the index then to g - 1, and the index sum
+// is of whole numbers below 2^24 -- every step is exact.
+__device__ __forceinline__ int thumb_index(const DevVolume &V, float ipx, float ipy, float ipz) {
+    const float x = fminf(fmaxf(ipx, 0.f), V.gmx), y = fminf(fmaxf(ipy, 0.f), V.gmy),
+                z = fminf(fmaxf(ipz, 0.f), V.gmz);
+    return int((z * V.fgy + y) * V.fgx + x);
 }
 
 // skip_nblock_steps (volume_shader.cu:5-14, same in blocks/isosurface).
@@ -318,11 +320,11 @@ __device__ __forceinline__ float sample_brick(const BrickRef &b, int Prt, float 
 __device__ __forceinline__ void gather2(const DevVolume &V, int which, float X, float Y, float fd,
                                         float4 &g0, float4 &g1) {
     if (which == 0) {
-        g0 = tex2Dgather<float4>(V.gtex[0], X, Y, 0);
-        g1 = tex2Dgather<float4>(V.gtex[0], X, Y + fd, 0);
+        g0 = gather_r(V.gtex[0], X, Y);
+        g1 = gather_r(V.gtex[0], X, Y + fd);
     } else {
-        g0 = tex2Dgather<float4>(V.gtex[1], X, Y, 0);
-        g1 = tex2Dgather<float4>(V.gtex[1], X, Y + fd, 0);
+        g0 = gather_r(V.gtex[1], X, Y);
+        g1 = gather_r(V.gtex[1], X, Y + fd);
     }
 }
 
@@ -351,8 +353,9 @@ __device__ __forceinline__ float sample_brick_gather(const DevVolume &V, const B
     // column of tap x + 1 and row of tap (y + 1, z): whole numbers below
     // 2^24, so the sums are exact and the gather's footprint is (x, y) ..
     // (x + 1, y + 1) of slice z (and, P rows further down, of slice z + 1)
+    // (b.ty is negative for texture 1: its magnitude is the row)
     const float X = (b.tx + flx) + 1.f;
-    const float Y = (b.ty + (flz * fd + fly)) + 1.f;
+    const float Y = (fabsf(b.ty) + (flz * fd + fly)) + 1.f;
     float4 g0, g1;
     gather2(V, b.which, X, Y, fd, g0, g1);
     // gather order: w = (x, y), z = (x + 1, y), x = (x, y + 1), y = (x + 1, y + 1)
@@ -378,14 +381,16 @@ __device__ __forceinline__ float sample_brick_gather(const DevVolume &V, const B
 }
 
 // The transfer function's knots in shared memory with the end knots
-// repeated: tfs[0] = knot 0, tfs[i + 1] = knot i, tfs[n + 1] = knot n - 1
+// repeated and two zero knots after them: tfs[0] = knot 0, tfs[i + 1] =
+// knot i, tfs[n + 1] = knot n - 1, tfs[n + 2] = tfs[n + 3] = 0
 // (n + kTfPad entries).
 // Nothing is staged without knots (the Isosurface and Blocks shaders run
 // without a transfer function and never call sample_tf).
-constexpr int kTfPad = 2;
+constexpr int kTfPad = 4;
 __device__ __forceinline__ void stage_tf(const float4 *__restrict__ tf, int n, float4 *tfs) {
     if (n <= 0) return;
-    for (int i = threadIdx.x; i < n + kTfPad; i += blockDim.x) tfs[i] = tf[min(max(i - 1, 0), n - 1)];
+    for (int i = threadIdx.x; i < n + kTfPad; i += blockDim.x)
+        tfs[i] = i <= n + 1 ? tf[min(max(i - 1, 0), n - 1)] : make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
 // TransferFn lookup: 1-D, normalised, Border, Linear (transfer_fn.hpp:16-23,
@@ -397,7 +402,24 @@ template <bool NONNEG = false>
 __device__ __forceinline__ float4 sample_tf(const float4 *__restrict__ tfs, int n, float fn,
                                             float s) {
     float fx = fn * s;
-    if (NONNEG ? !(fx <= fn) : !(0.f <= fx && fx <= fn)) return make_float4(0.f, 0.f, 0.f, 0.f);
+    if (NONNEG) {
+        // The Border test as two selects rather than a branch: out of range
+        // (fx > n, or NaN) reads the two zero knots past the end at fx = 0,
+        // and their lerp is +0 in every channel, the value returned below.
+        const bool in = fx <= fn;
+        fx = in ? fx : 0.f;
+        float u = fx - .5f;
+        float flr = floorf(u);
+        float a = u - flr;
+        const float4 *k = tfs + (in ? int(flr) + 1 : n + 2);
+        float4 x = k[0], y = k[1];
+        float b = 1.f - a;
+        const float2 bb = f2(b, b), aa = f2(a, a);
+        const float2 rg = lerp2(f2(x.x, x.y), bb, f2(y.x, y.y), aa);
+        const float2 ba = lerp2(f2(x.z, x.w), bb, f2(y.z, y.w), aa);
+        return make_float4(rg.x, rg.y, ba.x, ba.y);
+    }
+    if (!(0.f <= fx && fx <= fn)) return make_float4(0.f, 0.f, 0.f, 0.f);
     // fx in [0, n] so fi = floor(fx - 0.5) is in [-1, n-1] and the clamped
     // neighbours knot[max(fi, 0)], knot[min(fi + 1, n - 1)] are tfs[fi + 1],
     // tfs[fi + 2].  The upper one is ceil(u) = floor(u) + 1, or floor(u) when
@@ -425,6 +447,9 @@ struct Shared {
     float fntf;
     const float *lut;
 };
+__device__ __forceinline__ Shared make_shared(const float4 *tf, int ntf, const float *lut) {
+    return Shared{tf, ntf, float(ntf), lut};
+}
 
 // v.w > 0.93 and v.w > 0.85 are double comparisons in the reference
 // (volume_shader.cu:71-75).  Both constants round up to float, so for a
@@ -459,12 +484,13 @@ struct BrickCursor {
     // o's cell changed (or may have): redo floor(o) and the thumbnail lookups
     template <bool GATHER = false>
     __device__ __forceinline__ void locate(const DevVolume &V, float ox, float oy, float oz) {
-        const float fgx = float(V.gx), fgy = float(V.gy), fgz = float(V.gz);
         ipx = floorf(ox);
         ipy = floorf(oy);
         ipz = floorf(oz);
-        const int bid = thumb_index(V, fgx, fgy, fgz, ipx, ipy, ipz);
-        if (bid != cur) {
+        const int bid = thumb_index(V, ipx, ipy, ipz);
+        // with GATHER a cell change is a brick change (the cell is the
+        // brick): the entry is loaded without comparing indices
+        if (GATHER || bid != cur) {
             cur = bid;
             if constexpr (GATHER) {
                 // page table and texel origin in one load (no dependent
@@ -473,9 +499,9 @@ struct BrickCursor {
                 cd = in.x;
                 pg = in.y;
                 sample = cd == 0 && pg != -1;
-                br.tx = float(in.z);
-                br.ty = float(in.w & 0x3fffffff);
-                br.which = in.w >> 30;
+                br.tx = __int_as_float(in.z);
+                br.ty = __int_as_float(in.w);  // negative: texture 1
+                br.which = in.w < 0;
             } else {
                 const int2 in = __ldg(&V.info[bid]);
                 cd = in.x;
@@ -646,14 +672,13 @@ __device__ __forceinline__ long long blocks_main(Px &p, const ShadeArgs &A) {
     long long samples = 0;
     const float cdu = 1.f / gmax(gmax(fabsf(p.dx), fabsf(p.dy)), fabsf(p.dz));
     const float rx = 1.f / p.dx, ry = 1.f / p.dy, rz = 1.f / p.dz;
-    const float fgx = float(V.gx), fgy = float(V.gy), fgz = float(V.gz);
     const float opacity_threshold = 0.95f;
     const float hx = A.bbox_max[0] - 1.f, hy = A.bbox_max[1] - 1.f, hz = A.bbox_max[2] - 1.f;
     const float ex = A.bbox_max[0] - 0.f, ey = A.bbox_max[1] - 0.f, ez = A.bbox_max[2] - 0.f;
     const float sx = p.dx * A.step, sy = p.dy * A.step, sz = p.dz * A.step;
     while (p.nsteps > 0) {
         float ipx = floorf(p.ox), ipy = floorf(p.oy), ipz = floorf(p.oz);
-        int bid = thumb_index(V, fgx, fgy, fgz, ipx, ipy, ipz);
+        int bid = thumb_index(V, ipx, ipy, ipz);
         int cd = __ldg(&V.info[bid].x);
         if (cd) {
             p.nsteps -= skip_nblock_steps(p, rx, ry, rz, ipx, ipy, ipz, cd, cdu, A.step);
@@ -701,12 +726,11 @@ __device__ __forceinline__ long long paging_main(Px &p, const ShadeArgs &A) {
     long long samples = 0;
     const float cdu = 1.f / gmax(gmax(fabsf(p.dx), fabsf(p.dy)), fabsf(p.dz));
     const float rx = 1.f / p.dx, ry = 1.f / p.dy, rz = 1.f / p.dz;
-    const float fgx = float(V.gx), fgy = float(V.gy), fgz = float(V.gz);
     const float opacity_threshold = 0.95f;
     const float sx = p.dx * A.step, sy = p.dy * A.step, sz = p.dz * A.step;
     while (p.nsteps > 0) {
         float ipx = floorf(p.ox), ipy = floorf(p.oy), ipz = floorf(p.oz);
-        int bid = thumb_index(V, fgx, fgy, fgz, ipx, ipy, ipz);
+        int bid = thumb_index(V, ipx, ipy, ipz);
         const int2 in = __ldg(&V.info[bid]);
         if (in.x) {
             p.nsteps -= skip_nblock_steps(p, rx, ry, rz, ipx, ipy, ipz, in.x, cdu, A.step);

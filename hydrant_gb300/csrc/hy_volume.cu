@@ -145,7 +145,7 @@ __global__ void gather_check_kernel(cudaTextureObject_t t, unsigned int *bad) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     if (x >= 255) return;
     // row 0 holds u = column, row 1 holds 255 - column
-    const float4 g = tex2Dgather<float4>(t, float(x) + 1.f, 1.f, 0);
+    const float4 g = hy::gather_r((unsigned long long)t, float(x) + 1.f, 1.f);
     const float ew = __fdiv_rn(float(x), 255.f), ez = __fdiv_rn(float(x + 1), 255.f);
     const float ex = __fdiv_rn(float(255 - x), 255.f), ey = __fdiv_rn(float(254 - x), 255.f);
     if (__float_as_uint(g.w) != __float_as_uint(ew) || __float_as_uint(g.z) != __float_as_uint(ez) ||
@@ -280,8 +280,11 @@ int build_gather(hy_volume *vol) {
         const int reg = vol->reg_of_brick[b];
         int4 q = make_int4(vol->cheb[b], reg, 0, 0);
         if (reg >= 0) {
-            q.z = int(table[reg].x0);
-            q.w = int(table[reg].y0) | (table[reg].which << 30);
+            // texel origin as floats, the texture in the sign of y0 (-0 for
+            // y0 = 0 in texture 1)
+            const float y0 = table[reg].which ? -table[reg].y0 : table[reg].y0;
+            std::memcpy(&q.z, &table[reg].x0, 4);
+            std::memcpy(&q.w, &y0, 4);
         }
         info4[b] = q;
     }

@@ -507,8 +507,9 @@ int hy_batch_autotune(hy_batch *batch, uint8_t *rgba_dev, int32_t reps, hy_batch
  * lends its inputs and outputs, or a frame loop that cannot take the
  * synchronisation cost of cudaMalloc/cudaFree mid-frame.  Scratch lives in a
  * fixed ~33 KiB static device array that every GPU loading the library keeps
- * until exit; the first call on a device looks up its address and should
- * come before any stream capture.  Calls share that array: calls that overlap
+ * until exit.  The view descriptors are copied from host stack memory, so a
+ * call on a stream that is capturing returns HY_ERR_STATE (capture the batch
+ * path, hy_batch_*, instead).  Calls share that array: calls that overlap
  * on the GPU race.  More than 256 views is rejected with HY_ERR_INVALID.
  * rgba_dev must hold at least max over views of rgba_offset + width*height*4
  * bytes (there is no size argument to check it against).

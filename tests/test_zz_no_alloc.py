@@ -165,3 +165,28 @@ def test_noalloc_at_the_view_limit(ctx):
         assert expect.any()
     finally:
         vol.close()
+
+
+def test_noalloc_refuses_a_capturing_stream(ctx):
+    """The view descriptors are copied from the call's stack, so a captured
+    copy would replay from a dead address: on a stream that is capturing the
+    entry point returns HY_ERR_STATE and enqueues nothing (the capture is
+    opened and closed through the driver API, relaxed mode, and the empty
+    graph destroyed)."""
+    cuda = C.CDLL("libcuda.so.1")
+    vol, p, views, light, arr, nbytes = _setup(ctx, "Volume")
+    try:
+        ctx.synchronize()
+        stream = C.c_void_p(ctx.stream)
+        assert cuda.cuStreamBeginCapture_v2(stream, 2) == 0  # CU_STREAM_CAPTURE_MODE_RELAXED
+        rc = hy.lib().hy_render_views_noalloc(ctx.handle, vol.handle, C.byref(p), arr, len(SIZES),
+                                              C.c_void_p(1 << 20))
+        graph = C.c_void_p()
+        end = cuda.cuStreamEndCapture(stream, C.byref(graph))
+        if graph.value:
+            cuda.cuGraphDestroy(graph)
+        assert end == 0
+        assert rc == _abi.HY_ERR_STATE
+        assert b"capturing" in hy.lib().hy_last_error(ctx.handle)
+    finally:
+        vol.close()
