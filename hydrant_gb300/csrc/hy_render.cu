@@ -117,6 +117,21 @@ template <int SHADER, int PC, int DT, bool PADDED, int LOOP>
 __global__ void HY_RENDER_LEAN_BOUNDS render_lean_kernel(const __grid_constant__ ShadeArgs A) {
     render_body<SHADER, PC, DT, PADDED, 0, true, false, LOOP>(A);
 }
+// The same march sampling by texture gathers (u8 bricks with an apron in
+// the volume's gather textures): 64-view step, one launch per view, 169.6
+// ms at 48 registers against 172.4 at 56, 173.1 at 64 and 198.8 for the
+// loads (HY_RENDER_GATHER=0 builds the per-view path without it).
+#ifndef HY_RENDER_GATHER
+#define HY_RENDER_GATHER 1
+#endif
+#ifndef HY_RENDER_GATHER_REGS
+#define HY_RENDER_GATHER_REGS 48
+#endif
+template <int SHADER, int PC, int DT, bool PADDED, int LOOP>
+__global__ void __maxnreg__(HY_RENDER_GATHER_REGS)
+    render_lean_gather_kernel(const __grid_constant__ ShadeArgs A) {
+    render_body<SHADER, PC, DT, PADDED, 0, true, true, LOOP>(A);
+}
 
 
 // The per-brick compositing variants of the Volume and Isosurface shaders,
@@ -288,9 +303,18 @@ void launch_fused(const ShadeArgs &a, cudaStream_t s) {
     }
     if constexpr (SHADER == HY_SHADER_VOLUME) {
         if (a.mode == HY_VOLUME_DEFAULT && !a.aux) {
-            // (the per-view kernel samples by loads: with gathers it measured
-            // slower, 177.0 vs 186.5 Gsamples/s on the 64-view step)
             const bool ert = a.ert > 0.f;
+            if constexpr (HY_RENDER_GATHER && DT == HY_DTYPE_U8 && PADDED) {
+                if (a.vol.tex) {  // bricks in gather textures
+                    if (ert)
+                        render_lean_gather_kernel<SHADER, PC, DT, PADDED, kLoopErt>
+                            <<<grid_of(a), kThreads, smem_bytes(a), s>>>(a);
+                    else
+                        render_lean_gather_kernel<SHADER, PC, DT, PADDED, kLoopOne>
+                            <<<grid_of(a), kThreads, smem_bytes(a), s>>>(a);
+                    return;
+                }
+            }
             if (ert)
                 render_lean_kernel<SHADER, PC, DT, PADDED, kLoopErt>
                     <<<grid_of(a), kThreads, smem_bytes(a), s>>>(a);

@@ -213,12 +213,11 @@ int hy_volume_destroy(hy_volume *vol);
  * Once per volume (HY_ERR_STATE after that): new data is a new volume. */
 int hy_volume_upload(hy_volume *vol, const void *host_voxels);
 int hy_volume_get_info(const hy_volume *vol, hy_volume_info *out);
-/* Sampler of the batched Volume march (hy_batch_*, hy_render_views_noalloc;
- * Default mode, no compositing) over a resident u8 volume with an apron: the
- * eight taps of a trilinear sample fetched by two texture gathers (on, the
- * default) or by eight loads from the brick pool (off; the per-view entry
- * points always load, which measured faster there).  A batch takes the
- * setting when it is created.  Both give the same floats: the upload places every brick in a gather texture whose
+/* Sampler of the Volume march in Default mode without compositing or aux
+ * output (hy_render*, hy_batch_*, hy_render_views_noalloc) over a resident
+ * u8 volume with an apron: the eight taps of a trilinear sample fetched by
+ * two texture gathers (on, the default) or by eight loads from the brick
+ * pool (off).  A batch takes the setting when it is created.  Both give the same floats: the upload places every brick in a gather texture whose
  * texels the texture unit returns as u / 255, checked bit for bit against
  * IEEE division once per device (a device that fails uses the loads).  The
  * reference samples its bricks through textures as well (texture_3d.hpp:

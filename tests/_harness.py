@@ -40,7 +40,9 @@ class Case:
         Volume shader in Default mode takes the lean march (the instantiation
         the benchmark times), so both kernel instantiations face the oracle;
         the lean one is checked here (images, floats, sample count) and the
-        full one is returned for the caller's own checks."""
+        full one is returned for the caller's own checks.  Where the lean
+        march samples by texture gathers (u8 bricks with an apron), it also
+        renders with the loads and both must agree bit for bit."""
         p = hy.shader_params(count_samples=True, **kw)
         if p.shader == hy._abi.SHADER_ISOSURFACE:
             hy.iso_lighting(self.vol, cam, p)
@@ -52,6 +54,15 @@ class Case:
         assert_parity(lean, r, check_aux=False, what=f"no-aux render {kw}")
         assert np.array_equal(lean.rgba, g.rgba) and np.array_equal(lean.v, g.v), \
             f"no-aux render differs from the aux render {kw}"
+        if self.vol.gather_sampling:
+            self.vol.set_gather_sampling(False)
+            try:
+                loads = hy.render(self.ctx, self.vol, p, view, W, H, want_v=True, want_aux=False)
+            finally:
+                self.vol.set_gather_sampling(True)
+            assert np.array_equal(loads.rgba, lean.rgba) and np.array_equal(loads.v, lean.v), \
+                f"lean march: loads and gathers differ {kw}"
+            assert loads.samples == lean.samples
         return g, r, p, view
 
 
