@@ -187,8 +187,17 @@ __device__ __forceinline__ void batch_body(const BatchArgs &B) {
     }
 }
 
+// The per-brick compositing march sampling by gathers: five 256-thread
+// blocks (48 registers, 256 bytes spilled) -- 64-view composite step 293.1
+// ms, against 304.9 at four blocks (64 registers) and 298.6 for the loads at
+// four (which spill 304 bytes at five, 327.9 ms).
+#ifndef HY_BATCH_COMPOSITE_GATHER_MIN_BLOCKS
+#define HY_BATCH_COMPOSITE_GATHER_MIN_BLOCKS 5
+#endif
 template <int SHADER, int PC, int DT, bool PADDED, int COMPOSITE, bool GATHER = false>
-__global__ void __launch_bounds__(kMaxBlockThreads, HY_BATCH_MIN_BLOCKS)
+__global__ void __launch_bounds__(kMaxBlockThreads,
+                                  (COMPOSITE && GATHER) ? HY_BATCH_COMPOSITE_GATHER_MIN_BLOCKS
+                                                        : HY_BATCH_MIN_BLOCKS)
     batch_kernel(const __grid_constant__ BatchArgs B) {
     batch_body<SHADER, PC, DT, PADDED, COMPOSITE, false, GATHER>(B);
 }
@@ -207,11 +216,9 @@ __global__ void __launch_bounds__(kMaxBlockThreads, HY_BATCH_MIN_BLOCKS)
 // registers (no spills, 36 warps) and 173.1 at 40 (168 bytes spill, 48
 // warps).
 // The Volume shader's per-brick compositing in the batch samples by
-// gathers (1) or loads (0).  Loads: at the kernel's 64 registers the
-// gathers spill 148 bytes (loads 32) and the 64-view composite step takes
-// 337.6 vs 312.7 ms.
+// gathers (1) or loads (0).
 #ifndef HY_BATCH_COMPOSITE_GATHER
-#define HY_BATCH_COMPOSITE_GATHER 0
+#define HY_BATCH_COMPOSITE_GATHER 1
 #endif
 #ifndef HY_BATCH_GATHER_REGS
 #define HY_BATCH_GATHER_REGS 48
