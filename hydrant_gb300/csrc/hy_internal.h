@@ -71,10 +71,10 @@ struct DevVolume {
     const TexEntry *tex;
     unsigned long long gtex[kMaxGatherTextures];  // cudaTextureObject_t
     float map_k, map_b;  // BlockSamplerMapping of every resident brick (with `tex`)
-    // with `tex`: per brick {chebyshev, registry id or -1, texel column x0
-    // (float bits), texel row y0 (float bits, negated -- -0 for 0 -- in
-    // texture 1)}: the page table and the brick's place in its gather
-    // texture in one 16-byte load
+    // with `tex`: per brick {chebyshev, registry id or -1, x0 + 1, y0 + 1}
+    // (texel column and row of the brick's origin plus one, as float bits;
+    // the row negated in texture 1): the page table and the brick's place in
+    // its gather texture in one 16-byte load
     const int4 *info4;
     // the thumbnail grid as floats: g - 1 per axis (the clamp bounds) and
     // gx, gy (the index strides); exact, nbricks <= 2^24

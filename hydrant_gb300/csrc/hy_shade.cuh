@@ -364,12 +364,12 @@ __device__ __forceinline__ float sample_brick_gather(const DevVolume &V, const B
     const float2 axy = f2(ux - flx, uy - fly);
     const float az = uz - flz;
 #endif
-    // column of tap x + 1 and row of tap (y + 1, z): whole numbers below
-    // 2^24, so the sums are exact and the gather's footprint is (x, y) ..
-    // (x + 1, y + 1) of slice z (and, P rows further down, of slice z + 1)
-    // (b.ty is negative for texture 1: its magnitude is the row)
-    const float X = (b.tx + flx) + 1.f;
-    const float Y = (fabsf(b.ty) + (flz * fd + fly)) + 1.f;
+    // column of tap x + 1 and row of tap (y + 1, z) -- b.tx, |b.ty| are the
+    // brick's texel origin + 1 (b.ty negative in texture 1): whole numbers
+    // below 2^24, so the sums are exact and the gather's footprint is (x, y)
+    // .. (x + 1, y + 1) of slice z (and, P rows further down, of slice z + 1)
+    const float X = b.tx + flx;
+    const float Y = fabsf(b.ty) + (flz * fd + fly);
     float4 g0, g1;
     gather2(V, b.which, X, Y, fd, g0, g1);
     // gather order: w = (x, y), z = (x + 1, y), x = (x, y + 1), y = (x + 1, y + 1)

@@ -280,11 +280,12 @@ int build_gather(hy_volume *vol) {
         const int reg = vol->reg_of_brick[b];
         int4 q = make_int4(vol->cheb[b], reg, 0, 0);
         if (reg >= 0) {
-            // texel origin as floats, the texture in the sign of y0 (-0 for
-            // y0 = 0 in texture 1)
-            const float y0 = table[reg].which ? -table[reg].y0 : table[reg].y0;
-            std::memcpy(&q.z, &table[reg].x0, 4);
-            std::memcpy(&q.w, &y0, 4);
+            // texel origin + 1 as floats (the sampler's footprint column and
+            // row offsets), the texture in the sign of the row (>= 1)
+            const float x1 = table[reg].x0 + 1.f, y1 = table[reg].y0 + 1.f;
+            const float ys = table[reg].which ? -y1 : y1;
+            std::memcpy(&q.z, &x1, 4);
+            std::memcpy(&q.w, &ys, 4);
         }
         info4[b] = q;
     }
