@@ -82,6 +82,9 @@ def parse_args():
     ap.add_argument("--prefetch", action="store_true",
                     help="paging, realtime: move the next orbit camera's bricks on the copy "
                          "stream while each frame renders (hy_pager_prefetch)")
+    ap.add_argument("--pager-sampler", choices=["gathers", "loads"], default="gathers",
+                    help="paging, realtime: the cache in gather textures (the Volume march "
+                         "samples by texture gathers) or in a device pool (loads)")
     ap.add_argument("--max-uploads", type=int, default=0,
                     help="paging: brick uploads per frame (0 = every missing brick)")
     ap.add_argument("--launch-shape", default="",
@@ -1012,7 +1015,8 @@ def paging_leg(args, hy, ctx, local, with_clocks=False):
             # within the --cache-gib budget
             slots, most = hy.Pager.tune_slots(ctx, store, path, budget)
         ev = _abi.EVICT_REFERENCE if args.eviction == "reference" else _abi.EVICT_LRU
-        pg = hy.Pager(ctx, store, slots, _abi.PAGER_REALTIME, args.max_uploads, ev)
+        smp = _abi.PAGER_GATHERS if args.pager_sampler == "gathers" else _abi.PAGER_LOADS
+        pg = hy.Pager(ctx, store, slots, _abi.PAGER_REALTIME, args.max_uploads, ev, smp)
     p = hy.shader_params(shader="Volume", sample_rate=0.25, density=5e-3)
     pc = hy.shader_params(shader="Volume", sample_rate=0.25, density=5e-3, count_samples=True)
     out = torch.empty(res * res * 4, dtype=torch.uint8, device=f"cuda:{local}")
@@ -1069,6 +1073,7 @@ def paging_leg(args, hy, ctx, local, with_clocks=False):
                        "most_visible_bricks": most, "budget_gib": args.cache_gib,
                        "rule": "most visible bricks over the orbit + 10 %, within the budget"},
                    "eviction": args.eviction if args.pager == "realtime" else None,
+                   "cache_sampler": args.pager_sampler if args.pager == "realtime" else None,
                    "store_gb": si.pool_bytes / 1e9, "store_build_s": t_store,
                    "coarse_level": args.coarse_level, "coarse_build_s": t_coarse,
                    "max_uploads_per_frame": args.max_uploads},

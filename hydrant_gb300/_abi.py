@@ -104,11 +104,12 @@ class HyBatchConfig(C.Structure):
 PAGER_LOSSLESS, PAGER_REALTIME = 0, 1
 EVICT_LRU = 0
 EVICT_REFERENCE = 1
+PAGER_LOADS, PAGER_GATHERS = 0, 1
 
 
 class HyPagerDesc(C.Structure):
     _fields_ = [("slots", C.c_int32), ("mode", C.c_int32), ("max_uploads_per_frame", C.c_int32),
-                ("eviction", C.c_int32)]
+                ("eviction", C.c_int32), ("sampler", C.c_int32)]
 
 
 class HyPagerStats(C.Structure):

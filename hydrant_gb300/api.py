@@ -489,9 +489,10 @@ class Pager:
         return int(slots.value), int(most.value)
 
     def __init__(self, ctx: Context, store: Store, slots: int, mode: int = _abi.PAGER_REALTIME,
-                 max_uploads_per_frame: int = 0, eviction: int = _abi.EVICT_LRU):
+                 max_uploads_per_frame: int = 0, eviction: int = _abi.EVICT_LRU,
+                 sampler: int = _abi.PAGER_LOADS):
         self.ctx = ctx
-        d = _abi.HyPagerDesc(slots, mode, max_uploads_per_frame, eviction)
+        d = _abi.HyPagerDesc(slots, mode, max_uploads_per_frame, eviction, sampler)
         h = C.c_void_p()
         ctx.check(lib().hy_pager_create(ctx.handle, store.handle, C.byref(d), C.byref(h)))
         self.handle = h

@@ -97,7 +97,7 @@ __device__ __forceinline__ void count_unit(const ShadeArgs &A, unsigned int n) {
 // the lean march then fits 56 registers without spilling (171.5 vs 175.4 ms
 // per 64-view step).  The per-brick compositing march keeps them (re-deriving
 // measured slower there: 340.3 vs 312.6 ms).
-template <int SHADER, int PC, int DT, bool PADDED, int COMPOSITE, bool LEAN, bool GATHER, int LOOP>
+template <int SHADER, int PC, int DT, bool PADDED, int COMPOSITE, bool LEAN, int GATHER, int LOOP>
 __device__ __forceinline__ unsigned int shade_batch_unit(const BatchArgs &B, const Shared &S,
                                                          const int *starts, int t) {
     const ShadeArgs &A = B.A;
@@ -140,7 +140,7 @@ __device__ __forceinline__ unsigned int shade_batch_unit(const BatchArgs &B, con
 // warps of an SM work on neighbouring rays and share L1 lines).
 // LEAN: Volume shader in Default mode without compositing (theta / phi are
 // not needed for an RGBA image; see VolumeMarch::step).
-template <int SHADER, int PC, int DT, bool PADDED, int COMPOSITE, bool LEAN, bool GATHER = false,
+template <int SHADER, int PC, int DT, bool PADDED, int COMPOSITE, bool LEAN, int GATHER = 0,
           int LOOP = kLoopOne>
 __device__ __forceinline__ void batch_body(const BatchArgs &B) {
     extern __shared__ float4 smem[];
@@ -194,7 +194,7 @@ __device__ __forceinline__ void batch_body(const BatchArgs &B) {
 #ifndef HY_BATCH_COMPOSITE_GATHER_MIN_BLOCKS
 #define HY_BATCH_COMPOSITE_GATHER_MIN_BLOCKS 5
 #endif
-template <int SHADER, int PC, int DT, bool PADDED, int COMPOSITE, bool GATHER = false>
+template <int SHADER, int PC, int DT, bool PADDED, int COMPOSITE, int GATHER = 0>
 __global__ void __launch_bounds__(kMaxBlockThreads,
                                   (COMPOSITE && GATHER) ? HY_BATCH_COMPOSITE_GATHER_MIN_BLOCKS
                                                         : HY_BATCH_MIN_BLOCKS)
@@ -223,17 +223,17 @@ __global__ void __launch_bounds__(kMaxBlockThreads,
 #ifndef HY_BATCH_GATHER_REGS
 #define HY_BATCH_GATHER_REGS 48
 #endif
-template <int DT, bool PADDED, bool GATHER>
+template <int DT, bool PADDED, int GATHER>
 constexpr int lean_regs() {
     return GATHER ? HY_BATCH_GATHER_REGS : (DT == HY_DTYPE_U8 && PADDED) ? HY_BATCH_LEAN_REGS : 64;
 }
-template <int SHADER, int PC, int DT, bool PADDED, bool GATHER, int LOOP>
+template <int SHADER, int PC, int DT, bool PADDED, int GATHER, int LOOP>
 __global__ void __maxnreg__((lean_regs<DT, PADDED, GATHER>()))
     batch_lean_kernel(const __grid_constant__ BatchArgs B) {
     batch_body<SHADER, PC, DT, PADDED, 0, true, GATHER, LOOP>(B);
 }
 
-template <int SHADER, int PC, int DT, bool PADDED, bool GATHER>
+template <int SHADER, int PC, int DT, bool PADDED, int GATHER>
 const void *pick_lean(const ShadeArgs &a, int steps_per_iter) {
     if (a.ert > 0.f)
         return reinterpret_cast<const void *>(
@@ -494,6 +494,8 @@ extern "C" int hy_batch_create(hy_ctx *ctx, const hy_volume *vol, const hy_shade
     }
     hy::ShadeArgs base;
     int rc = hy_fill_args(ctx, vol, params, nullptr, 1, 1, &base);
+    if (rc) return rc;
+    rc = hy_check_paged_gather(ctx, base, false);
     if (rc) return rc;
     for (int i = 0; i < nviews; ++i) {
         const hy_batch_view &v = views[i];
@@ -775,6 +777,8 @@ extern "C" int hy_render_views_noalloc(hy_ctx *ctx, const hy_volume *vol,
                        "noalloc: nviews must be 1..256 (the static scratch holds 256 views)");
     ShadeArgs base;
     int rc = hy_fill_args(ctx, vol, params, nullptr, 1, 1, &base);
+    if (rc) return rc;
+    rc = hy_check_paged_gather(ctx, base, false);
     if (rc) return rc;
     base.count = 0;  // sample counting is not available on this entry point
     HY_CUDA(ctx, cudaSetDevice(ctx->device));

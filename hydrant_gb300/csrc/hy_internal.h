@@ -36,7 +36,10 @@ static_assert(sizeof(TexEntry) == 16, "TexEntry is one 16-byte load");
 // travel in the kernel parameters, so every gather names a warp-uniform
 // texture (a per-brick handle in a register would make the compiler
 // serialise the gather over the distinct handles of a warp).
-constexpr int kMaxGatherTextures = 2;
+constexpr int kMaxGatherTextures = 16;  // a power of two
+// A resident volume uses at most two of them (its march selects between two
+// textures by a warp vote); a paged cache in gather textures up to all.
+constexpr int kResidentGatherTextures = 2;
 #ifdef __CUDACC__
 // One gather of component 0 (texture unit tld4): the four texels of the
 // footprint (x - 1/2 .. x + 1/2, y - 1/2 .. y + 1/2) in the order
@@ -79,6 +82,8 @@ struct DevVolume {
     // the thumbnail grid as floats: g - 1 per axis (the clamp bounds) and
     // gx, gy (the index strides); exact, nbricks <= 2^24
     float gmx, gmy, gmz, fgx, fgy;
+    // a paged cache in gather textures (registry entries carry texel origins)
+    int paged_gather;
 };
 
 // Per-view inputs: ViewArgs (shader.hpp:63-68) plus the image size and the
@@ -172,6 +177,7 @@ struct hy_volume {
     hy::TexEntry *tex_dev = nullptr;
     int4 *info4_dev = nullptr;
     bool tex_sampling = true;  // hy_volume_set_gather_sampling
+    bool paged_gather = false;  // a pager's cache held in atlas (gather textures)
 };
 
 // Brick store: every non-empty padded brick in pinned host memory, laid out
@@ -204,6 +210,20 @@ const hy::TexEntry *hy_volume_gather_table(const hy_volume *v);
 // Fills the gather fields of a device view of the volume (table and handles,
 // or null and zeros).
 void hy_volume_gather_view(const hy_volume *v, hy::DevVolume *dv);
+// Gather textures on this device: *ok when the texture unit's gather order and
+// u8 normalisation pass the check; *cols x *rowblocks bricks of edge P fit
+// one texture (0 when a brick does not).
+int hy_gather_layout(hy_ctx *ctx, int P, bool *ok, int *cols, int *rowblocks);
+// A u8 array made for gather (width x height texels) and its texture object;
+// with `surf`, also writable by kernels through the surface object *surf.
+int hy_gather_texture_create(hy_ctx *ctx, size_t width, size_t height, cudaArray_t *arr,
+                             unsigned long long *tex, unsigned long long *surf = nullptr);
+void hy_volume_free_gather(hy_volume *v);
+// HY_OK unless the arguments' volume is a pager's cache in gather textures
+// and the launch would read its voxels other than by the lean Volume march
+// of the fused per-view kernel (`fused`: that kernel is the launch); the
+// Blocks and Paging shaders read no voxels.
+int hy_check_paged_gather(hy_ctx *ctx, const hy::ShadeArgs &a, bool fused);
 // store helpers (hy_page.cu): grid / padded edge / slot stride from a
 // descriptor, and the pinned allocation for `nonempty` bricks
 void hy_store_geometry(hy_store *s, const hy_volume_desc &d);

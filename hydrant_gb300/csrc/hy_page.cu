@@ -718,6 +718,41 @@ __global__ void gather_bricks_kernel(const unsigned char *__restrict__ store,
     for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src[i];
 }
 
+// The same moves into a cache held in gather textures: one block per brick
+// reads the record from the mapped pinned store (16 bytes per thread and
+// iteration) and writes it through the texture's surface, two texels per
+// write (P is even and every brick's column origin a multiple of P, so a
+// pair never straddles a row): record byte r = row * P + col lands at
+// texel (x0 + col, y0 + row).  Writes outside the array are dropped.
+struct GatherSurfaces {
+    unsigned long long s[hy::kMaxGatherTextures];
+};
+__global__ void fill_textures_kernel(const unsigned char *__restrict__ store,
+                                     const GatherItem *__restrict__ items, GatherSurfaces surf,
+                                     int P, int gper, int gcols, int slot0) {
+    const GatherItem it = items[blockIdx.x];
+    const int g = slot0 + it.dst;
+    const int t = g / gper, i = g % gper;
+    const int x0 = (i % gcols) * P, y0 = (i / gcols) * P * P;
+    const cudaSurfaceObject_t so = cudaSurfaceObject_t(surf.s[t & (hy::kMaxGatherTextures - 1)]);
+    const uint4 *src = reinterpret_cast<const uint4 *>(store + it.src);
+    const int nbytes = P * P * P;
+    const int nchunks = (nbytes + 15) / 16;
+    for (int j = threadIdx.x; j < nchunks; j += blockDim.x) {
+        const uint4 q = src[j];
+        const unsigned int w[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const int r = j * 16 + 2 * k;
+            if (r >= nbytes) break;
+            const unsigned int v = (w[k >> 1] >> ((k & 1) * 16)) & 0xffffu;
+            const int row = r / P, col = r - row * P;
+            surf2Dwrite(make_uchar2((unsigned char)(v & 0xff), (unsigned char)(v >> 8)), so,
+                        x0 + col, y0 + row, cudaBoundaryModeZero);
+        }
+    }
+}
+
 }  // namespace
 
 struct hy_pager {
@@ -769,6 +804,19 @@ struct hy_pager {
     void *film = nullptr;
     size_t film_bytes = 0;
     hy_pager_stats stats{};
+    // HY_PAGER_GATHERS: pool slot g (the coarse bricks, then the cache) sits
+    // in gather texture g / gper, column block (g % gper) % gcols, row block
+    // (g % gper) / gcols of the volume's atlas
+    bool gathers = false;
+    int gcols = 0, gper = 0;
+    unsigned long long surf[hy::kMaxGatherTextures] = {};  // the textures' surfaces
+    void texel_origin(int g, int &t, int &x0, int &y0) const {
+        const int P = vol->P;
+        t = g / gper;
+        const int i = g % gper;
+        x0 = (i % gcols) * P;
+        y0 = (i / gcols) * P * P;
+    }
 };
 
 namespace {
@@ -826,14 +874,34 @@ int move_bricks(hy_pager *pg, const int *bricks, const int *slots, int n, cudaSt
     HY_CUDA(ctx, cudaMemcpyAsync(dev, items, n * sizeof(GatherItem), cudaMemcpyHostToDevice,
                                  stream));
     HY_CUDA(ctx, cudaEventRecord(pg->gathered[buf], stream));
-    gather_bricks_kernel<<<n, 256, 0, stream>>>(pg->store->host_dev, dev, v->pool, pg->ncoarse,
-                                                (long long)v->slot_stride);
+    if (pg->gathers) {
+        GatherSurfaces gs;
+        for (int t = 0; t < hy::kMaxGatherTextures; ++t) gs.s[t] = pg->surf[t] ? pg->surf[t] : pg->surf[0];
+        fill_textures_kernel<<<n, 256, 0, stream>>>(pg->store->host_dev, dev, gs, v->P, pg->gper,
+                                                     pg->gcols, pg->ncoarse);
+    } else {
+        gather_bricks_kernel<<<n, 256, 0, stream>>>(pg->store->host_dev, dev, v->pool, pg->ncoarse,
+                                                    (long long)v->slot_stride);
+    }
     HY_CUDA(ctx, cudaGetLastError());
     pg->stats.uploads += n;
     pg->stats.upload_bytes += (int64_t)n * (int64_t)pg->store->slot_stride;
     return HY_OK;
 }
 
+}  // namespace
+
+namespace {
+// A registry entry of a cache in gather textures: pool offset 0 (the one
+// zero slot) and the slot's texel origin + 1 in the last two words,
+// (texture << 16 | x0 + 1, y0 + 1), as the march reads them.
+void set_texel_origin(const hy_pager *pg, RegEntry &r, int g) {
+    int t, x0, y0;
+    pg->texel_origin(g, t, x0, y0);
+    r.offset = 0;
+    r.pad_[0] = (t << 16) | (x0 + 1);
+    r.pad_[1] = y0 + 1;
+}
 }  // namespace
 
 extern "C" int hy_pager_create(hy_ctx *ctx, hy_store *store, const hy_pager_desc *desc,
@@ -846,6 +914,13 @@ extern "C" int hy_pager_create(hy_ctx *ctx, hy_store *store, const hy_pager_desc
         return hy_fail(ctx, HY_ERR_INVALID, "pager: unknown mode");
     if (desc->eviction != HY_EVICT_LRU && desc->eviction != HY_EVICT_REFERENCE)
         return hy_fail(ctx, HY_ERR_INVALID, "pager: unknown eviction policy");
+    if (desc->sampler != HY_PAGER_LOADS && desc->sampler != HY_PAGER_GATHERS)
+        return hy_fail(ctx, HY_ERR_INVALID, "pager: unknown sampler");
+    if (desc->sampler == HY_PAGER_GATHERS &&
+        (desc->mode != HY_PAGER_REALTIME || store->desc.dtype != HY_DTYPE_U8 ||
+         store->desc.padding < 1))
+        return hy_fail(ctx, HY_ERR_UNSUPPORTED,
+                       "pager: gather textures hold a realtime cache of u8 bricks with an apron");
     HY_CUDA(ctx, cudaSetDevice(ctx->device));
     hy_pager *pg = new hy_pager();
     pg->ctx = ctx;
@@ -870,8 +945,39 @@ extern "C" int hy_pager_create(hy_ctx *ctx, hy_store *store, const hy_pager_desc
     pg->ncoarse = pg->coarse ? store->ncoarse : 0;
     pg->reg_base = pg->coarse ? v->nbricks : 0;
     const int nreg = pg->reg_base + pg->nslots;
-    v->pool_bytes = size_t(pg->ncoarse + pg->nslots) * v->slot_stride;
+    const int ntotal = pg->ncoarse + pg->nslots;
+    if (desc->sampler == HY_PAGER_GATHERS) {
+        bool ok = false;
+        int rows = 0;
+        rc = hy_gather_layout(ctx, v->P, &ok, &pg->gcols, &rows);
+        if (rc) return fail(rc);
+        pg->gper = pg->gcols * rows;
+        if (!ok || pg->gper <= 0 ||
+            (long long)pg->gper * hy::kMaxGatherTextures < (long long)ntotal)
+            return fail(hy_fail(ctx, HY_ERR_UNSUPPORTED,
+                                "pager: this device's gather textures cannot hold the cache"));
+        pg->gathers = true;
+        v->paged_gather = true;
+        // the textures, each exactly as large as its bricks need
+        for (int first = 0; first < ntotal; first += pg->gper) {
+            const int cnt = std::min(pg->gper, ntotal - first);
+            const int ucols = std::min(pg->gcols, cnt), urows = (cnt + pg->gcols - 1) / pg->gcols;
+            cudaArray_t arr = nullptr;
+            unsigned long long tex = 0;
+            unsigned long long sf = 0;
+            rc = hy_gather_texture_create(ctx, size_t(ucols) * v->P,
+                                          size_t(urows) * v->P * v->P, &arr, &tex, &sf);
+            if (rc) return fail(rc);
+            pg->surf[v->atlas.size()] = sf;
+            v->atlas.push_back(arr);
+            v->atlas_tex.push_back(tex);
+        }
+    }
+    // with gathers the pool is one slot of zeros: every registry entry points
+    // there, so no launch can read outside memory it owns
+    v->pool_bytes = size_t(pg->gathers ? 1 : ntotal) * v->slot_stride;
     cudaError_t e = cudaMalloc(&v->pool, v->pool_bytes);
+    if (e == cudaSuccess && pg->gathers) e = cudaMemset(v->pool, 0, v->pool_bytes);
     if (e == cudaSuccess) e = cudaMalloc(&v->info_dev, v->nbricks * sizeof(int2));
     if (e == cudaSuccess) e = cudaMalloc(&v->reg_dev, nreg * sizeof(RegEntry));
     if (e == cudaSuccess) e = cudaMalloc(&v->mean_dev, v->nbricks * sizeof(float));
@@ -919,15 +1025,30 @@ extern "C" int hy_pager_create(hy_ctx *ctx, hy_store *store, const hy_pager_desc
             reg[b] = RegEntry{kc, b0 + float(x % sc) * kc, b0 + float(y % sc) * kc,
                               b0 + float(z % sc) * kc, (long long)cid * (long long)v->slot_stride,
                               {0, 0}};
+            if (pg->gathers) set_texel_origin(pg, reg[b], cid);
         }
-        e = cudaMemcpyAsync(v->pool, store->coarse.data(), store->coarse.size(),
-                            cudaMemcpyHostToDevice, ctx->stream);
+        if (pg->gathers) {
+            const int P = v->P;
+            for (int c = 0; c < pg->ncoarse && e == cudaSuccess; ++c) {
+                int t, x0, y0;
+                pg->texel_origin(c, t, x0, y0);
+                e = cudaMemcpy2DToArray(v->atlas[t], size_t(x0), size_t(y0),
+                                        store->coarse.data() + size_t(c) * v->slot_stride,
+                                        size_t(P), size_t(P), size_t(P) * P,
+                                        cudaMemcpyHostToDevice);
+            }
+        } else {
+            e = cudaMemcpyAsync(v->pool, store->coarse.data(), store->coarse.size(),
+                                cudaMemcpyHostToDevice, ctx->stream);
+        }
         if (e != cudaSuccess) return fail(hy_cuda_fail(ctx, e, "pager: coarse level upload"));
     }
-    for (int s = 0; s < pg->nslots; ++s)
+    for (int s = 0; s < pg->nslots; ++s) {
         reg[pg->reg_base + s] =
             RegEntry{v->k, v->b, v->b, v->b,
                      (long long)(pg->ncoarse + s) * (long long)v->slot_stride, {0, 0}};
+        if (pg->gathers) set_texel_origin(pg, reg[pg->reg_base + s], pg->ncoarse + s);
+    }
     e = cudaMemcpyAsync(v->reg_dev, reg.data(), reg.size() * sizeof(RegEntry),
                         cudaMemcpyHostToDevice, ctx->stream);
     if (e == cudaSuccess)
@@ -976,8 +1097,11 @@ extern "C" int hy_pager_destroy(hy_pager *pg) {
     if (pg->cs.d2) cudaFree(pg->cs.d2);
     if (pg->cs.count) cudaFree(pg->cs.count);
     if (pg->film) cudaFree(pg->film);
+    for (auto sf : pg->surf)
+        if (sf) cudaDestroySurfaceObject(cudaSurfaceObject_t(sf));
     if (pg->vol) {
         hy_volume *v = pg->vol;
+        hy_volume_free_gather(v);
         if (v->pool) cudaFree(v->pool);
         if (v->info_dev) cudaFree(v->info_dev);
         if (v->reg_dev) cudaFree(v->reg_dev);
@@ -1362,6 +1486,11 @@ extern "C" int hy_pager_render(hy_pager *pg, const hy_shader_params *p, const hy
     hy_ctx *ctx = pg->ctx;
     if (!hy_aligned(rgba_dev, 4)) return hy_fail(ctx, HY_ERR_INVALID, "pager: misaligned output (4-byte)");
     if (p->composite) return hy_fail(ctx, HY_ERR_UNSUPPORTED, "pager: composite not supported");
+    if (pg->gathers && !(p->shader == HY_SHADER_BLOCKS || p->shader == HY_SHADER_PAGING ||
+                         (p->shader == HY_SHADER_VOLUME && p->mode == HY_VOLUME_DEFAULT)))
+        return hy_fail(ctx, HY_ERR_UNSUPPORTED,
+                       "pager: a cache in gather textures serves the Volume shader in Default "
+                       "mode and the Blocks and Paging shaders (HY_PAGER_LOADS serves all)");
     HY_CUDA(ctx, cudaSetDevice(ctx->device));
     hy_view view;
     int rc = hy_camera_view(pg->vol, cam, &view);

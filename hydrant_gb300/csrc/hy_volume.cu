@@ -241,7 +241,7 @@ int build_gather(hy_volume *vol) {
     if (rc || !ok) return rc;
     const int cols = gw / P, rowblocks = int(gh / brick_rows), per = cols * rowblocks;
     const int n = vol->resident;
-    if ((long long)per * hy::kMaxGatherTextures < n) return HY_OK;  // more than the textures hold
+    if ((long long)per * hy::kResidentGatherTextures < n) return HY_OK;  // more than two textures hold
     std::vector<hy::TexEntry> table(n);
     cudaChannelFormatDesc cd = cudaCreateChannelDesc(8, 0, 0, 0, cudaChannelFormatKindUnsigned);
     for (int first = 0; first < n; first += per) {
@@ -481,11 +481,69 @@ const hy::TexEntry *hy_volume_gather_table(const hy_volume *v) {
 }
 
 void hy_volume_gather_view(const hy_volume *v, hy::DevVolume *dv) {
-    dv->tex = hy_volume_gather_table(v);
+    dv->tex = v->paged_gather ? nullptr : hy_volume_gather_table(v);
     dv->info4 = dv->tex ? v->info4_dev : nullptr;
+    dv->paged_gather = v->paged_gather ? 1 : 0;
+    // every entry a valid handle (the last texture repeated)
+    const int n = int(v->atlas_tex.size());
+    const bool any = (dv->tex || v->paged_gather) && n > 0;
     for (int i = 0; i < hy::kMaxGatherTextures; ++i)
-        dv->gtex[i] = (dv->tex && i < int(v->atlas_tex.size())) ? v->atlas_tex[i] : 0ull;
+        dv->gtex[i] = any ? v->atlas_tex[std::min(i, n - 1)] : 0ull;
 }
+
+int hy_gather_layout(hy_ctx *ctx, int P, bool *ok, int *cols, int *rowblocks) {
+    *ok = false;
+    *cols = *rowblocks = 0;
+    int gw = 0, gh = 0;
+    HY_CUDA(ctx, cudaDeviceGetAttribute(&gw, cudaDevAttrMaxTexture2DGatherWidth, ctx->device));
+    HY_CUDA(ctx, cudaDeviceGetAttribute(&gh, cudaDevAttrMaxTexture2DGatherHeight, ctx->device));
+    const long long brick_rows = (long long)P * P;
+    if (P <= 0 || P > gw || brick_rows > gh) return HY_OK;
+    int rc = gather_check(ctx, ok);
+    if (rc) return rc;
+    *cols = gw / P;
+    *rowblocks = int(gh / brick_rows);
+    return HY_OK;
+}
+
+int hy_gather_texture_create(hy_ctx *ctx, size_t width, size_t height, cudaArray_t *arr,
+                             unsigned long long *tex, unsigned long long *surf) {
+    *arr = nullptr;
+    *tex = 0;
+    if (surf) *surf = 0;
+    cudaChannelFormatDesc cd = cudaCreateChannelDesc(8, 0, 0, 0, cudaChannelFormatKindUnsigned);
+    const unsigned int flags = cudaArrayTextureGather | (surf ? cudaArraySurfaceLoadStore : 0u);
+    cudaError_t e = cudaMallocArray(arr, &cd, width, height, flags);
+    if (e != cudaSuccess) {
+        *arr = nullptr;
+        return hy_cuda_fail(ctx, e, "gather texture allocation");
+    }
+    cudaTextureObject_t t = make_gather_texture(*arr, &e);
+    if (e != cudaSuccess) {
+        cudaFreeArray(*arr);
+        *arr = nullptr;
+        return hy_cuda_fail(ctx, e, "gather texture object");
+    }
+    if (surf) {
+        cudaResourceDesc rd;
+        std::memset(&rd, 0, sizeof(rd));
+        rd.resType = cudaResourceTypeArray;
+        rd.res.array.array = *arr;
+        cudaSurfaceObject_t so = 0;
+        e = cudaCreateSurfaceObject(&so, &rd);
+        if (e != cudaSuccess) {
+            cudaDestroyTextureObject(t);
+            cudaFreeArray(*arr);
+            *arr = nullptr;
+            return hy_cuda_fail(ctx, e, "gather texture surface");
+        }
+        *surf = (unsigned long long)so;
+    }
+    *tex = (unsigned long long)t;
+    return HY_OK;
+}
+
+void hy_volume_free_gather(hy_volume *v) { free_gather(v); }
 
 extern "C" int hy_volume_set_gather_sampling(hy_volume *vol, int32_t enable) {
     if (!vol) return HY_ERR_INVALID;

@@ -284,12 +284,19 @@ enum { HY_PAGER_LOSSLESS = 0, HY_PAGER_REALTIME = 1 };
  * index, as RtBlockPagingServer pops its redundant set (rt_block_paging.cc:
  * 256-265, 299-326). */
 enum { HY_EVICT_LRU = 0, HY_EVICT_REFERENCE = 1 };
+/* Where a realtime cache keeps its bricks: a device pool read by loads (every
+ * shader), or gather textures (u8 stores with an apron; the Volume shader in
+ * Default mode without compositing or aux output samples them by texture
+ * gathers, Blocks and Paging read no voxels; other uses of the pager's volume
+ * return HY_ERR_UNSUPPORTED).  Same images and the same bytes per brick. */
+enum { HY_PAGER_LOADS = 0, HY_PAGER_GATHERS = 1 };
 
 typedef struct hy_pager_desc {
     int32_t slots;                 /* bricks per batch (lossless) / cache size (realtime) */
     int32_t mode;                  /* HY_PAGER_* */
     int32_t max_uploads_per_frame; /* realtime: 0 = every missing brick */
     int32_t eviction;              /* realtime: HY_EVICT_* */
+    int32_t sampler;               /* realtime: HY_PAGER_LOADS / HY_PAGER_GATHERS */
 } hy_pager_desc;
 
 typedef struct hy_pager_stats {

@@ -368,7 +368,7 @@ protected:
         if (!offline_pager || offline_mb != mem_limit_mb) {
             if (offline_pager) hy_pager_destroy(offline_pager);
             offline_pager = nullptr;
-            hy_pager_desc d{slots_for(mem_limit_mb, 4096), HY_PAGER_LOSSLESS, 0, HY_EVICT_LRU};
+            hy_pager_desc d{slots_for(mem_limit_mb, 4096), HY_PAGER_LOSSLESS, 0, HY_EVICT_LRU, HY_PAGER_LOADS};
             check(hy_pager_create(dataset->ctx, dataset->store, &d, &offline_pager), dataset->ctx,
                   "offline pager");
             offline_mb = mem_limit_mb;
@@ -381,7 +381,7 @@ protected:
         if (!realtime_pager || realtime_mb != mem_limit_mb) {
             if (realtime_pager) hy_pager_destroy(realtime_pager);
             realtime_pager = nullptr;
-            hy_pager_desc d{slots_for(mem_limit_mb, 0), HY_PAGER_REALTIME, 0, HY_EVICT_LRU};
+            hy_pager_desc d{slots_for(mem_limit_mb, 0), HY_PAGER_REALTIME, 0, HY_EVICT_LRU, HY_PAGER_LOADS};
             check(hy_pager_create(dataset->ctx, dataset->store, &d, &realtime_pager), dataset->ctx,
                   "realtime pager");
             realtime_mb = mem_limit_mb;

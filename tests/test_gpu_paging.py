@@ -569,16 +569,27 @@ def test_out_of_core_orbit_at_quarter_scale_matches_oracle(ctx):
         _, most = hy.Pager.tune_slots(ctx, store, path, 1 << 40)
         slots = max(16, most // 3)
         pg = hy.Pager(ctx, store, slots, _abi.PAGER_REALTIME, 0, _abi.EVICT_LRU)
+        # the same cache in gather textures renders the same frames
+        pgt = hy.Pager(ctx, store, slots, _abi.PAGER_REALTIME, 0, _abi.EVICT_LRU,
+                       _abi.PAGER_GATHERS)
         p = hy.shader_params(shader="Volume", sample_rate=0.25, density=5e-3)
         out = torch.zeros(res * res * 4, dtype=torch.uint8, device="cuda")
+        outt = torch.zeros(res * res * 4, dtype=torch.uint8, device="cuda")
         try:
             vol = pg.volume
             for f, cam in enumerate(path):
                 pg.render(p, cam, res, res, out.data_ptr())
+                pgt.render(p, cam, res, res, outt.data_ptr())
                 if f + 1 < len(path):
                     pg.prefetch(path[f + 1])
+                    pgt.prefetch(path[f + 1])
                 ctx.synchronize()
                 st = pg.stats()
+                assert torch.equal(out, outt), f"frame {f}: gather cache differs"
+                assert np.array_equal(pg.present(), pgt.present())
+                stt = pgt.stats()
+                assert (st["uploads"], st["evictions"], st["fallback"]) == \
+                    (stt["uploads"], stt["evictions"], stt["fallback"])
                 if f in (0, len(path) - 1):
                     assert st["fallback"] > 0  # the coarse level is in use
                     ov.set_present(pg.present())
@@ -593,5 +604,89 @@ def test_out_of_core_orbit_at_quarter_scale_matches_oracle(ctx):
         finally:
             ov.set_present(np.ones(gx * gy * gz, np.uint8))
             pg.close()
+            pgt.close()
     finally:
         store.close()
+
+
+@pytest.mark.parametrize("shader,mode", [("Volume", "Default"), ("Paging", "Default"),
+                                         ("Blocks", "Volume")])
+def test_gather_cache_matches_oracle(ctx, tubes_coarse, shader, mode):
+    """A realtime cache held in gather textures (HY_PAGER_GATHERS): the
+    frames, resident sets and counts equal the pool cache's along a path
+    with evictions and the coarse fallback, and the oracle's given that
+    resident set; the march samples fine and coarse bricks (each entry's own
+    mapping) through the textures."""
+    torch = pytest.importorskip("torch")
+    vol, ov, store = tubes_coarse
+    ctx.set_transfer_fn(wl.TF9)
+    pl = hy.Pager(ctx, store, 30, _abi.PAGER_REALTIME, 8)
+    pt = hy.Pager(ctx, store, 30, _abi.PAGER_REALTIME, 8, _abi.EVICT_LRU, _abi.PAGER_GATHERS)
+    nb = ov.grid[0] * ov.grid[1] * ov.grid[2]
+    try:
+        W, H = 64, 48
+        saw_fallback = False
+        for f in range(6):
+            c = wl.make_camera(wl.Camera("orbit", (20 + 30 * f, 35, 2.2)))
+            p = hy.shader_params(shader=shader, mode=mode, density=0.4, sample_rate=0.5,
+                                 count_samples=True)
+            a = torch.zeros(W * H * 4, dtype=torch.uint8, device="cuda")
+            b = torch.zeros(W * H * 4, dtype=torch.uint8, device="cuda")
+            pl.render(p, c, W, H, a.data_ptr())
+            sl = ctx.stats()
+            pt.render(p, c, W, H, b.data_ptr())
+            st = ctx.stats()
+            ctx.synchronize()
+            assert torch.equal(a, b), f"frame {f}"
+            assert sl.samples == st.samples
+            assert np.array_equal(pl.present(), pt.present())
+            s1, s2 = pl.stats(), pt.stats()
+            for k in ("uploads", "evictions", "hits", "misses", "fallback"):
+                assert s1[k] == s2[k], k
+            saw_fallback |= s2["fallback"] > 0
+            ov.set_present(pt.present())
+            op = orc.params_from(p)
+            op.lowest_blkcnt = ov.lowest_blkcnt
+            ref = orc.render(ov, wl.TF9, op, view_array(hy.camera_view(vol, c)), W, H)
+            d = np.abs(b.cpu().numpy().reshape(H, W, 4).astype(int) - ref["rgba"].astype(int))
+            assert d.max() <= 1, f"frame {f}: {d.max()} LSB"
+        assert saw_fallback
+    finally:
+        ov.set_present(np.ones(nb, np.uint8))
+        pl.close()
+        pt.close()
+
+
+def test_gather_cache_rejects_what_it_cannot_serve(ctx, tubes):
+    """A cache in gather textures serves the lean Volume march and the
+    shaders that read no voxels; the Isosurface shader, the Volume shader's
+    other modes and compositing, film passes, batches on its volume and a
+    lossless pager in textures are refused (HY_ERR_UNSUPPORTED) before any
+    launch."""
+    torch = pytest.importorskip("torch")
+    vol, ov, store = tubes
+    ctx.set_transfer_fn(wl.TF9)
+    with pytest.raises(hy.HydrantError) as e:
+        hy.Pager(ctx, store, 50, _abi.PAGER_LOSSLESS, 0, _abi.EVICT_LRU, _abi.PAGER_GATHERS)
+    assert e.value.code == _abi.HY_ERR_UNSUPPORTED
+    pg = hy.Pager(ctx, store, 200, _abi.PAGER_REALTIME, 0, _abi.EVICT_LRU, _abi.PAGER_GATHERS)
+    try:
+        cam = wl.make_camera(wl.Camera("orbit", (25, 65, 2.2)))
+        out = torch.zeros(32 * 32 * 4, dtype=torch.uint8, device="cuda")
+        for kw in (dict(shader="Isosurface", isovalue=0.5), dict(shader="Volume", mode="Paging"),
+                   dict(shader="Volume", composite=True)):
+            p = hy.shader_params(**kw)
+            if kw["shader"] == "Isosurface":
+                hy.iso_lighting(pg.volume, cam, p)
+            with pytest.raises(hy.HydrantError) as e:
+                pg.render(p, cam, 32, 32, out.data_ptr())
+            assert e.value.code == _abi.HY_ERR_UNSUPPORTED
+        p = hy.shader_params(shader="Volume", density=0.4)
+        pg.render(p, cam, 32, 32, out.data_ptr())  # the lean march serves it
+        view = hy.camera_view(pg.volume, cam)
+        with pytest.raises(hy.HydrantError) as e:
+            hy.Batch(ctx, pg.volume, p, [(view, 32, 32)])
+        assert e.value.code == _abi.HY_ERR_UNSUPPORTED
+        ctx.synchronize()
+    finally:
+        pg.close()
