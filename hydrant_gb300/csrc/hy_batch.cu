@@ -94,9 +94,10 @@ __device__ __forceinline__ void count_unit(const ShadeArgs &A, unsigned int n) {
 // LEAN: the unit's view and pixel are found again after the march (the empty
 // asm with a memory clobber makes the compiler re-read them rather than hold
 // the view pointer and pixel coordinates in registers through the march):
-// the lean march then fits 56 registers without spilling (171.5 vs 175.4 ms
-// per 64-view step).  The per-brick compositing march keeps them (re-deriving
-// measured slower there: 340.3 vs 312.6 ms).
+// measured when it was introduced, the lean march then fitted 56 registers
+// without spilling (171.5 vs 175.4 ms per 64-view step).  The per-brick
+// compositing march keeps them (re-deriving measured slower there: 340.3 vs
+// 312.6 ms).
 template <int SHADER, int PC, int DT, bool PADDED, int COMPOSITE, bool LEAN, int GATHER, int LOOP>
 __device__ __forceinline__ unsigned int shade_batch_unit(const BatchArgs &B, const Shared &S,
                                                          const int *starts, int t) {

@@ -100,11 +100,11 @@ __global__ void __launch_bounds__(kThreads) render_kernel(const __grid_constant_
     render_body<SHADER, PC, DT, PADDED, COMPOSITE, LEAN, false, LOOP>(A);
 }
 
-// The lean march of the per-view path with its own register budget
+// The lean march of the per-view path by loads (f32 volumes, volumes without
+// an apron or gather textures) with its own register budget
 // (HY_RENDER_LEAN_REGS, 0: the compiler's choice, 56 registers).  64-view
-// step, one launch per view: 56 registers 199.7 ms, 48 (8 bytes spilled)
-// 211.7 ms, 40 269.0 ms -- unlike the batched kernel, more resident warps
-// do not pay here.
+// step of u8 bricks by loads, one launch per view: 56 registers 199.7 ms, 48
+// (8 bytes spilled) 211.7 ms, 40 269.0 ms.
 #ifndef HY_RENDER_LEAN_REGS
 #define HY_RENDER_LEAN_REGS 0
 #endif
