@@ -7,6 +7,8 @@ reference's replacement policy, simulated here on the host with the oracle's
 culling, and render what the oracle renders with that resident set.
 """
 
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -687,6 +689,18 @@ def test_gather_cache_rejects_what_it_cannot_serve(ctx, tubes):
         with pytest.raises(hy.HydrantError) as e:
             hy.Batch(ctx, pg.volume, p, [(view, 32, 32)])
         assert e.value.code == _abi.HY_ERR_UNSUPPORTED
+        film = torch.zeros(32 * 32 * 64, dtype=torch.uint8, device="cuda")
+        with pytest.raises(hy.HydrantError) as e:
+            hy.shade_pass(ctx, pg.volume, p, _abi.PASS_RAY_EMIT, view, film.data_ptr(), 32, 32)
+        assert e.value.code == _abi.HY_ERR_UNSUPPORTED
+        arr = (_abi.HyBatchView * 1)()
+        arr[0].view = view
+        arr[0].width = arr[0].height = 32
+        rc = hy.lib().hy_render_views_noalloc(ctx.handle, pg.volume.handle, C.byref(p), arr, 1,
+                                              C.c_void_p(out.data_ptr()))
+        assert rc == _abi.HY_ERR_UNSUPPORTED
+        # the shaders that read no voxels are served
+        pg.render(hy.shader_params(shader="Blocks", mode="Solid"), cam, 32, 32, out.data_ptr())
         ctx.synchronize()
     finally:
         pg.close()
