@@ -876,7 +876,8 @@ int move_bricks(hy_pager *pg, const int *bricks, const int *slots, int n, cudaSt
     HY_CUDA(ctx, cudaEventRecord(pg->gathered[buf], stream));
     if (pg->gathers) {
         GatherSurfaces gs;
-        for (int t = 0; t < hy::kMaxGatherTextures; ++t) gs.s[t] = pg->surf[t] ? pg->surf[t] : pg->surf[0];
+        for (int t = 0; t < hy::kMaxGatherTextures; ++t)
+            gs.s[t] = pg->surf[t] ? pg->surf[t] : pg->surf[0];
         fill_textures_kernel<<<n, 256, 0, stream>>>(pg->store->host_dev, dev, gs, v->P, pg->gper,
                                                      pg->gcols, pg->ncoarse);
     } else {
@@ -916,11 +917,13 @@ extern "C" int hy_pager_create(hy_ctx *ctx, hy_store *store, const hy_pager_desc
         return hy_fail(ctx, HY_ERR_INVALID, "pager: unknown eviction policy");
     if (desc->sampler != HY_PAGER_LOADS && desc->sampler != HY_PAGER_GATHERS)
         return hy_fail(ctx, HY_ERR_INVALID, "pager: unknown sampler");
+    // (an even brick edge P: the fill writes texel pairs at multiples of P)
     if (desc->sampler == HY_PAGER_GATHERS &&
         (desc->mode != HY_PAGER_REALTIME || store->desc.dtype != HY_DTYPE_U8 ||
-         store->desc.padding < 1))
+         store->desc.padding < 1 || (store->P & 1)))
         return hy_fail(ctx, HY_ERR_UNSUPPORTED,
-                       "pager: gather textures hold a realtime cache of u8 bricks with an apron");
+                       "pager: gather textures hold a realtime cache of u8 bricks with an apron "
+                       "and an even edge");
     HY_CUDA(ctx, cudaSetDevice(ctx->device));
     hy_pager *pg = new hy_pager();
     pg->ctx = ctx;
