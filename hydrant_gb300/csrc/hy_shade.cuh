@@ -424,7 +424,8 @@ __device__ __forceinline__ float sample_brick_gather(const DevVolume &V, const B
     const float az = uz - flz;
 #endif
     // column of tap x + 1 and row of tap (y + 1, z) -- b.tx, |b.ty| are the
-    // brick's texel origin + 1 (b.ty negative in texture 1): whole numbers
+    // brick's texel origin + 1 (a resident brick's b.ty is negative in
+    // texture 1; a paged entry names its texture in b.which): whole numbers
     // below 2^24, so the sums are exact and the gather's footprint is (x, y)
     // .. (x + 1, y + 1) of slice z (and, P rows further down, of slice z + 1)
     const float X = b.tx + flx;
