@@ -334,6 +334,7 @@ protected:
     float clear_color[3] = {0, 0, 0};
     hy_pager *offline_pager = nullptr, *realtime_pager = nullptr;
     size_t offline_mb = 0, realtime_mb = 0;
+    int realtime_sampler = HY_PAGER_LOADS;
 
     void release() {
         if (offline_pager) hy_pager_destroy(offline_pager);
@@ -376,15 +377,24 @@ protected:
         return offline_pager;
     }
 
-    // RtBlockPagingServer cache: mem_limit / brick slots (rt_block_paging.cc:230-233)
-    hy_pager *realtime(size_t mem_limit_mb) {
-        if (!realtime_pager || realtime_mb != mem_limit_mb) {
+    // RtBlockPagingServer cache: mem_limit / brick slots (rt_block_paging.cc:230-233).
+    // `gathers`: the cache in gather textures (the Volume shader's Default
+    // mode samples it by texture gathers), where the dataset allows it;
+    // otherwise, and for every other use, a device pool read by loads.
+    hy_pager *realtime(size_t mem_limit_mb, bool gathers = false) {
+        const int sampler = gathers ? HY_PAGER_GATHERS : HY_PAGER_LOADS;
+        if (!realtime_pager || realtime_mb != mem_limit_mb || realtime_sampler != sampler) {
             if (realtime_pager) hy_pager_destroy(realtime_pager);
             realtime_pager = nullptr;
-            hy_pager_desc d{slots_for(mem_limit_mb, 0), HY_PAGER_REALTIME, 0, HY_EVICT_LRU, HY_PAGER_LOADS};
-            check(hy_pager_create(dataset->ctx, dataset->store, &d, &realtime_pager), dataset->ctx,
-                  "realtime pager");
+            hy_pager_desc d{slots_for(mem_limit_mb, 0), HY_PAGER_REALTIME, 0, HY_EVICT_LRU, sampler};
+            int rc = hy_pager_create(dataset->ctx, dataset->store, &d, &realtime_pager);
+            if (rc == HY_ERR_UNSUPPORTED && sampler == HY_PAGER_GATHERS) {
+                d.sampler = HY_PAGER_LOADS;  // e.g. an f32 dataset: the pool cache
+                rc = hy_pager_create(dataset->ctx, dataset->store, &d, &realtime_pager);
+            }
+            check(rc, dataset->ctx, "realtime pager");
             realtime_mb = mem_limit_mb;
+            realtime_sampler = sampler;
         }
         return realtime_pager;
     }
@@ -433,7 +443,7 @@ public:
     }
     using IRenderer::realtime_render;  // keep the loop overload visible
     Image realtime_render(CameraConfig const &camera) override {
-        return frame(realtime(mem_limit_mb), params(), camera);
+        return frame(realtime(mem_limit_mb, mode == HY_VOLUME_DEFAULT), params(), camera);
     }
 
 private:
