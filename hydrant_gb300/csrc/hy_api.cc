@@ -61,6 +61,7 @@ extern "C" int hy_ctx_destroy(hy_ctx *ctx) {
     if (ctx->tf_dev) cudaFree(ctx->tf_dev);
     if (ctx->counter_dev) cudaFree(ctx->counter_dev);
     if (ctx->stage) cudaFree(ctx->stage);
+    hy_diff_release(ctx);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);

@@ -61,6 +61,12 @@ struct DiffArgs {
     const float4 *dimage;
     float *dvol;
     float *dtf;        // ntf * 4
+    // the padded volume as a gather texture (0: none): slice s of P = n + 2
+    // in tile (s / gper, s % gper) of P x P texels, column tiles P apart,
+    // with slice (c + 1) * gper repeated as row gper of column c, so slice
+    // s + 1 of a footprint is always P rows below slice s
+    unsigned long long gtex;
+    int gper;
 };
 
 // Trilinear footprint of the padded brick at brick-local x in [0,1] (the
@@ -122,6 +128,57 @@ __device__ __forceinline__ float diff_sample(const DiffArgs &a, float lx, float 
     return diff_fetch(a, c);
 }
 
+// diff_sample through the gather texture: the same fractions and lerps, the
+// eight taps by two gathers (slices iz and iz + 1 of the padded volume,
+// whose texels repeat the clamped border exactly as diff_cell's indices do).
+// In the interior a footprint's lower index lies in [0, P - 2], so the
+// whole-number texel coordinates stay inside the slice's tile.
+__device__ __forceinline__ float diff_sample_gather(const DiffArgs &a, float lx, float ly,
+                                                    float lz) {
+    const int P = a.n + 2;
+    const float fd = float(P);
+    const float2 kl = mul2(f2(a.k, a.k), f2(lx, ly));
+    const float2 fxy = mul2(f2(fd, fd), f2(__fadd_rn(kl.x, a.b), __fadd_rn(kl.y, a.b)));
+    const float fz = fd * (a.k * lz + a.b);
+    const float ux = fxy.x - .5f, uy = fxy.y - .5f, uz = fz - .5f;
+    const float flx = floorf(ux), fly = floorf(uy), flz = floorf(uz);
+    const float2 axy = sub2(f2(ux, uy), f2(flx, fly));
+    const float az = uz - flz;
+    const int iz = int(flz);
+    const int col = iz / a.gper, row = iz - col * a.gper;
+    const float X = float(col * P + 1) + flx, Y = float(row * P + 1) + fly;
+    const float4 g0 = gather_r(a.gtex, X, Y), g1 = gather_r(a.gtex, X, Y + fd);
+    // gather order: w = (x, y), z = (x + 1, y), x = (x, y + 1), y = (x + 1, y + 1)
+    const float2 c00 = f2(g0.w, g1.w), c01 = f2(g0.z, g1.z);
+    const float2 c10 = f2(g0.x, g1.x), c11 = f2(g0.y, g1.y);
+    const float2 bxy = sub2(f2(1.f, 1.f), axy);
+    const float bz = 1.f - az;
+    const float2 bx2 = f2(bxy.x, bxy.x), ax2 = f2(axy.x, axy.x);
+    const float2 X0 = lerp2(c00, bx2, c01, ax2);
+    const float2 X1 = lerp2(c10, bx2, c11, ax2);
+    const float2 Yv = lerp2(X0, f2(bxy.y, bxy.y), X1, f2(axy.y, axy.y));
+    const float2 Z = mul2(Yv, f2(bz, az));
+    return __fadd_rn(Z.x, Z.y);
+}
+
+// The padded volume into the gather texture: one thread per texel of a
+// slice row (x), rows (y) and slices (z) on the grid's other axes.
+__global__ void diff_fill_kernel(const float *__restrict__ vol, int n, int gper,
+                                 unsigned long long surf) {
+    const int P = n + 2;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, s = blockIdx.z;
+    if (x >= P) return;
+    const int vx = min(max(x - 1, 0), n - 1), vy = min(max(y - 1, 0), n - 1),
+              vz = min(max(s - 1, 0), n - 1);
+    const float v = vol[(size_t(vz) * n + vy) * n + vx];
+    const cudaSurfaceObject_t so = cudaSurfaceObject_t(surf);
+    const int col = s / gper, row = s - col * gper;
+    surf2Dwrite(v, so, (col * P + x) * int(sizeof(float)), row * P + y, cudaBoundaryModeZero);
+    if (row == 0 && col > 0)
+        surf2Dwrite(v, so, ((col - 1) * P + x) * int(sizeof(float)), gper * P + y,
+                    cudaBoundaryModeZero);
+}
+
 // emit against the unit box; returns nsteps, sets o and d
 __device__ __forceinline__ int diff_emit(const DiffArgs &a, int view, int x, int y, float &ox,
                                          float &oy, float &oz, float &dx, float &dy, float &dz) {
@@ -180,6 +237,7 @@ __device__ __forceinline__ void pixel_of(const DiffArgs &a, int &x, int &y, int 
     view = blockIdx.z;
 }
 
+template <bool GATHER>
 __global__ void __launch_bounds__(128) diff_forward_kernel(const __grid_constant__ DiffArgs a) {
     __shared__ float4 tf[kMaxKnots];
     for (int i = threadIdx.x; i < a.ntf; i += blockDim.x) tf[i] = a.tf[i];
@@ -201,7 +259,8 @@ __global__ void __launch_bounds__(128) diff_forward_kernel(const __grid_constant
         }
         --until_ckpt;
         const float ipx = floorf(ox), ipy = floorf(oy), ipz = floorf(oz);
-        const float val = diff_sample(a, ox - ipx, oy - ipy, oz - ipz);
+        const float val = GATHER ? diff_sample_gather(a, ox - ipx, oy - ipy, oz - ipz)
+                                 : diff_sample(a, ox - ipx, oy - ipy, oz - ipz);
         int i, j;
         float al;
         bool inb;
@@ -356,6 +415,7 @@ __device__ __forceinline__ void diff_adjoint_sample(const DiffArgs &a, const flo
 #ifndef HY_DIFF_MIN_BLOCKS
 #define HY_DIFF_MIN_BLOCKS 6
 #endif
+template <bool GATHER>
 __global__ void __launch_bounds__(128, HY_DIFF_MIN_BLOCKS)
     diff_backward_kernel(const __grid_constant__ DiffArgs a) {
     __shared__ float4 tf[kMaxKnots];
@@ -387,7 +447,8 @@ __global__ void __launch_bounds__(128, HY_DIFF_MIN_BLOCKS)
             // recompute the segment: values and v.w before each sample
             for (int s = 0; s < cnt; ++s) {
                 const float ipx = floorf(ox), ipy = floorf(oy), ipz = floorf(oz);
-                const float val = diff_sample(a, ox - ipx, oy - ipy, oz - ipz);
+                const float val = GATHER ? diff_sample_gather(a, ox - ipx, oy - ipy, oz - ipz)
+                                         : diff_sample(a, ox - ipx, oy - ipy, oz - ipz);
                 seg_vw[s] = make_float2(val, vw);
                 int i, j;
                 float al;
@@ -464,6 +525,86 @@ int fill_diff(hy_ctx *ctx, const hy_diff_params *p, const float *vol, const floa
 
 dim3 diff_grid(const DiffArgs &a) { return dim3((a.W + 15) / 16, (a.H + 7) / 8, a.nviews); }
 
+// HY_DIFF_GATHER: the adjoint's segment recompute (1) -- and the forward
+// too (2) -- sample the volume through a gather texture refreshed from the
+// caller's volume at each call (the refresh inside the timed launch); 0:
+// loads only.  256^3 f32, 16 views of 512^2, 32 knots, K = 32, per view:
+//   0: forward 1.34 ms, forward + adjoint 3.70 ms (2.79x), fit iteration 59.9 ms
+//   1: forward 1.34 ms, forward + adjoint 3.45 ms (2.58x), fit iteration 55.1 ms
+//   2: forward 0.88 ms, forward + adjoint 2.97 ms (3.38x), fit iteration 47.5 ms
+// 1 is the default: 2 gives the fastest fit, but its forward + adjoint is
+// more than three times its (faster) forward.
+#ifndef HY_DIFF_GATHER
+#define HY_DIFF_GATHER 1
+#endif
+struct DiffGather {
+    cudaArray_t arr = nullptr;
+    unsigned long long tex = 0, surf = 0;
+    int n = 0, gper = 0;
+};
+
+void free_diff_gather(DiffGather *g) {
+    if (!g) return;
+    if (g->surf) cudaDestroySurfaceObject(cudaSurfaceObject_t(g->surf));
+    if (g->tex) cudaDestroyTextureObject(cudaTextureObject_t(g->tex));
+    if (g->arr) cudaFreeArray(g->arr);
+    delete g;
+}
+
+// The context's texture of an n^3 volume, (re)made for n, filled from vol on
+// the stream.  *ok = false (no error) when this device cannot hold it.
+int diff_gather_refresh(hy_ctx *ctx, const float *vol, int n, DiffArgs &a, bool *ok) {
+    *ok = false;
+    DiffGather *g = static_cast<DiffGather *>(ctx->diff_gather);
+    if (!g || g->n != n) {
+        free_diff_gather(g);
+        ctx->diff_gather = nullptr;
+        int gw = 0, gh = 0;
+        HY_CUDA(ctx, cudaDeviceGetAttribute(&gw, cudaDevAttrMaxTexture2DGatherWidth, ctx->device));
+        HY_CUDA(ctx, cudaDeviceGetAttribute(&gh, cudaDevAttrMaxTexture2DGatherHeight, ctx->device));
+        const int P = n + 2;
+        const int gper = gh / P - 1;  // slices per column, plus the repeated one
+        if (gper < 1) return HY_OK;
+        const int cols = (P - 2) / gper + 1;  // columns of the footprints' lower slices
+        if ((long long)cols * P > gw) return HY_OK;
+        g = new DiffGather();
+        g->n = n;
+        g->gper = gper;
+        cudaChannelFormatDesc cd = cudaCreateChannelDesc(32, 0, 0, 0, cudaChannelFormatKindFloat);
+        cudaError_t e = cudaMallocArray(&g->arr, &cd, size_t(cols) * P, size_t(gper + 1) * P,
+                                        cudaArrayTextureGather | cudaArraySurfaceLoadStore);
+        cudaResourceDesc rd;
+        std::memset(&rd, 0, sizeof(rd));
+        rd.resType = cudaResourceTypeArray;
+        rd.res.array.array = g->arr;
+        cudaTextureDesc td;
+        std::memset(&td, 0, sizeof(td));
+        td.addressMode[0] = td.addressMode[1] = cudaAddressModeClamp;
+        td.filterMode = cudaFilterModePoint;
+        td.readMode = cudaReadModeElementType;
+        td.normalizedCoords = 0;
+        cudaTextureObject_t t = 0;
+        cudaSurfaceObject_t so = 0;
+        if (e == cudaSuccess) e = cudaCreateTextureObject(&t, &rd, &td, nullptr);
+        if (e == cudaSuccess) g->tex = (unsigned long long)t;
+        if (e == cudaSuccess) e = cudaCreateSurfaceObject(&so, &rd);
+        if (e == cudaSuccess) g->surf = (unsigned long long)so;
+        if (e != cudaSuccess) {
+            free_diff_gather(g);
+            return hy_cuda_fail(ctx, e, "diff: gather texture");
+        }
+        ctx->diff_gather = g;
+    }
+    const int P = n + 2;
+    diff_fill_kernel<<<dim3((P + 127) / 128, P, P), 128, 0, ctx->stream>>>(vol, n, g->gper,
+                                                                          g->surf);
+    HY_CUDA(ctx, cudaGetLastError());
+    a.gtex = g->tex;
+    a.gper = g->gper;
+    *ok = true;
+    return HY_OK;
+}
+
 }  // namespace
 
 extern "C" int hy_diff_ckpt_bytes(const hy_diff_params *p, int32_t W, int32_t H, int32_t nviews,
@@ -497,8 +638,17 @@ extern "C" int hy_diff_forward(hy_ctx *ctx, const hy_diff_params *p, const float
     a.ckpt = reinterpret_cast<float4 *>(ckpt_dev);
     a.nsteps_out = nsteps_dev;
     HY_CUDA(ctx, cudaSetDevice(ctx->device));
+    // the texture's refresh is part of the timed launch
     HY_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
-    diff_forward_kernel<<<diff_grid(a), 128, 0, ctx->stream>>>(a);
+    bool gathers = false;
+    if (HY_DIFF_GATHER >= 2) {
+        rc = diff_gather_refresh(ctx, vol_dev, p->n, a, &gathers);
+        if (rc) return rc;
+    }
+    if (gathers)
+        diff_forward_kernel<true><<<diff_grid(a), 128, 0, ctx->stream>>>(a);
+    else
+        diff_forward_kernel<false><<<diff_grid(a), 128, 0, ctx->stream>>>(a);
     HY_CUDA(ctx, cudaGetLastError());
     HY_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
     ctx->stats_pending = true;
@@ -529,12 +679,27 @@ extern "C" int hy_diff_backward(hy_ctx *ctx, const hy_diff_params *p, const floa
     a.dvol = dvol_dev;
     a.dtf = dtf_dev;
     HY_CUDA(ctx, cudaSetDevice(ctx->device));
+    // the texture's refresh is part of the timed launch
     HY_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
-    diff_backward_kernel<<<diff_grid(a), 128, 0, ctx->stream>>>(a);
+    bool gathers = false;
+    if (HY_DIFF_GATHER >= 1) {
+        rc = diff_gather_refresh(ctx, vol_dev, p->n, a, &gathers);
+        if (rc) return rc;
+    }
+    if (gathers)
+        diff_backward_kernel<true><<<diff_grid(a), 128, 0, ctx->stream>>>(a);
+    else
+        diff_backward_kernel<false><<<diff_grid(a), 128, 0, ctx->stream>>>(a);
     HY_CUDA(ctx, cudaGetLastError());
     HY_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
     ctx->stats_pending = true;
     ctx->pend_count = 0;
     ctx->pend_pixels = (int64_t)W * H * nviews;
     return HY_OK;
+}
+
+void hy_diff_release(hy_ctx *ctx) {
+    if (!ctx) return;
+    free_diff_gather(static_cast<DiffGather *>(ctx->diff_gather));
+    ctx->diff_gather = nullptr;
 }

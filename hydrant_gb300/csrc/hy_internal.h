@@ -146,7 +146,11 @@ struct hy_ctx {
     // device staging for the host-pointer entry points, grown on demand
     void *stage = nullptr;
     size_t stage_bytes = 0;
+    // the differentiable path's volume as a gather texture (hy_diff.cu)
+    void *diff_gather = nullptr;
 };
+// Frees ctx->diff_gather (hy_diff.cu).
+void hy_diff_release(hy_ctx *ctx);
 
 struct hy_volume {
     hy_ctx *ctx = nullptr;
